@@ -1,0 +1,391 @@
+"""Benchmark: Mrays/s of BVH traversal on one GB300 (and N via torchrun).
+
+Workload (default): the ~1M-triangle clutter scene (4,000 seeded objects),
+N8L8 BVH from the SAH builder, one frame of 1920x1080 closest-hit primary
+rays + 1 any-hit shadow ray per hit + 8 cosine AO rays per hit (length 0.1 x
+scene diagonal). A step traces the whole frame (three launches: primary,
+shadow, AO) with the rays already resident on the GPU. ``e2e`` is the same
+frame through the C-ABI host entry point (bvhgpu_trace_host) from pinned host
+buffers, copies included.
+
+The rays (about 600 MB per frame) are larger than L2; the BVH (~75 MB) stays
+resident in L2 across steps, as in steady-state rendering.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle's C
+restatement of the ISPC fast path, OpenMP on all host cores) on a bounded
+sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s"
+LIGHT = (10.0, 3.8, 5.0)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--objects", type=int, default=4000)
+    p.add_argument("--branching", type=int, default=8)
+    p.add_argument("--leaf", type=int, default=8)
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--ao", type=int, default=8)
+    p.add_argument("--scheme", default="per_ray", choices=["per_ray", "stream"])
+    p.add_argument("--profile", default="instrumented", choices=["instrumented", "fast"])
+    p.add_argument("--cpu-sample", type=float, default=0.5,
+                   help="fraction of the frame traced by the cpu_baseline leg")
+    p.add_argument("--ref-sample", type=float, default=0.1,
+                   help="fraction of the frame traced per step by --impl reference")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload_name(a):
+    return (f"clutter-{a.objects}obj N{a.branching}L{a.leaf} {a.width}x{a.height} primary "
+            f"+1 shadow +{a.ao} AO per hit")
+
+
+def make_frame(a, scene_trace=None):
+    """Triangles, BVH and the three ray batches of one frame. The secondary
+    rays come from the primary hits (traced by ``scene_trace``)."""
+    import bvhraytracer_gb300 as pkg
+    from bvhraytracer_gb300 import scenes as S
+    tris = S.clutter(a.objects, seed=1)
+    bvh = pkg.Bvh(tris, a.branching, a.leaf)
+    primary = S.clutter_camera(a.objects, a.width, a.height)
+    return tris, bvh, primary
+
+
+def secondaries(a, tris, primary, prims):
+    from bvhraytracer_gb300 import scenes as S
+    m, p, n = S.surface(tris, primary, prims)
+    shadow = S.shadow_rays(p, n, np.array(LIGHT) * (a.objects / 4000.0) ** (1 / 3))
+    ao = S.ao_rays(p, n, a.ao, 0.1 * S.scene_diagonal(tris), seed=11)
+    return shadow, ao
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def sample_packets(rays: np.ndarray, frac: float, packet: int = 256) -> np.ndarray:
+    """Every k-th packet of ``packet`` consecutive rays (k = 1/frac), so the
+    sample spans the whole frame."""
+    k = max(1, int(round(1.0 / frac)))
+    npk = -(-rays.shape[0] // packet)
+    idx = np.concatenate([np.arange(p * packet, min((p + 1) * packet, rays.shape[0]))
+                          for p in range(0, npk, k)])
+    return rays[idx]
+
+
+def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=3):
+    """The oracle's restatement of the reference's ISPC fast path
+    (intersectWideAlternative / intersectSecondaryWideAlternative, 16x16
+    workgroups, OpenMP dynamic scheduling) on a sample of the frame."""
+    from oracle import oracle as O
+    cv = O.CompactView(bvh.export_compact())
+    fv = O.FastView(bvh.export_fast(gang=4))
+    parts = [(primary, False), (shadow, True), (ao, True)]
+    sample = [(sample_packets(r, frac), any_hit) for r, any_hit in parts]
+    n = sum(s.shape[0] for s, _ in sample)
+    cores = os.cpu_count() or 1
+
+    def once():
+        t0 = time.perf_counter()
+        for r, any_hit in sample:
+            O.trace_fast(fv, cv, r, any_hit, packet=256, threads=cores, counters=False,
+                         outputs=True)
+        return time.perf_counter() - t0
+
+    once()  # warm-up, like the reference's first render
+    ts = [once() for _ in range(repeats)]
+    med = statistics.median(ts)
+    return {"value": n / med / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{n} rays (every {int(round(1 / frac))}th 256-ray packet of each batch "
+                      "of the frame), fast profile, "
+                      f"ray-stream 16x16 packets, median of {repeats} after 1 warm-up",
+            "seconds": med}
+
+
+def run_reference(a):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import bvhraytracer_gb300 as pkg  # noqa: F401  (host builder only)
+    from oracle import oracle as O
+    tris, bvh, primary = make_frame(a)
+    cv = O.CompactView(bvh.export_compact())
+    fv = O.FastView(bvh.export_fast(gang=4))
+    # Secondary rays from the oracle's own primary hits on the sample.
+    frac = a.ref_sample
+    ps = sample_packets(primary, frac)
+    hits = O.trace_fast(fv, cv, ps, False, packet=256, counters=False)["hits"]
+    prims = hits.view(np.int32)[:, 0]
+    shadow, ao = secondaries(a, tris, ps, prims)
+    sample = [(ps, False), (shadow, True), (ao, True)]
+    n = sum(s.shape[0] for s, _ in sample)
+    cores = os.cpu_count() or 1
+
+    def step():
+        t0 = time.perf_counter()
+        for r, any_hit in sample:
+            O.trace_fast(fv, cv, r, any_hit, packet=256, threads=cores, counters=False)
+        return time.perf_counter() - t0
+
+    for _ in range(a.warmup):
+        step()
+    ts = [step() for _ in range(a.steps)]
+    total = sum(ts)
+    value = n * a.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": total / a.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded clutter scene; reference scenes not available)",
+        "config": {"workload": workload_name(a), "sample": f"{n} rays per step (every "
+                   f"{int(round(1 / frac))}th 256-ray packet of the frame's primary rays and "
+                   "their secondaries)", "profile": "fast",
+                   "scheme": "ray-stream 16x16 packets"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{n} rays per step"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(a):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import bvhraytracer_gb300 as pkg
+    from bvhraytracer_gb300 import _native as NAT
+
+    t_setup = time.time()
+    tris, bvh, primary = make_frame(a)
+    scene = pkg.Scene(bvh, device=local)
+    d_primary = torch.from_numpy(primary).to(dev)
+    hits0 = scene.trace(d_primary, scheme=a.scheme, profile=a.profile)["hits"]
+    prims = pkg.hit_prims(hits0.cpu().numpy())
+    shadow, ao = secondaries(a, tris, primary, prims)
+    d_shadow = torch.from_numpy(shadow).to(dev)
+    d_ao = torch.from_numpy(ao).to(dev)
+    n_rays = primary.shape[0] + shadow.shape[0] + ao.shape[0]
+    out_h = torch.empty((primary.shape[0], 4), dtype=torch.float32, device=dev)
+    out_s = torch.empty(shadow.shape[0], dtype=torch.uint8, device=dev)
+    out_a = torch.empty(ao.shape[0], dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    batches = [(d_primary, "closest", out_h), (d_shadow, "any", out_s), (d_ao, "any", out_a)]
+
+    def step(events=None):
+        for i, (r, kind, out) in enumerate(batches):
+            if events is not None:
+                events[i][0].record(stream)
+            scene.trace(r, kind=kind, scheme=a.scheme, profile=a.profile, out=out)
+            if events is not None:
+                events[i][1].record(stream)
+
+    # Algorithmic bytes per launch from one counting pass (untimed):
+    # node visits x node record bytes + triangle tests x 36 bytes.
+    alg = []
+    for r, kind, _ in batches:
+        c = scene.trace(r, kind=kind, scheme=a.scheme, profile=a.profile, counters=True)
+        cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
+        alg.append({"node_visits": int(cs[0]), "leaf_visits": int(cs[1]), "tri_tests": int(cs[4]),
+                    "bytes": int(cs[0]) * scene.node_record_bytes + int(cs[4]) * 36})
+    scene.status()
+    setup_s = time.time() - t_setup
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    ev = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+           for _ in batches] for _ in range(a.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        start.record(stream)
+        for k in range(a.steps):
+            step(ev[k])
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = start.elapsed_time(stop)
+    clocks = clk.summary()
+    scene.status()
+    t = torch.tensor([ms], dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        tt = t.to(dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    per_kernel_ms = [statistics.mean(e[i][0].elapsed_time(e[i][1]) for e in ev)
+                     for i in range(len(batches))]
+    value = n_rays * world * a.steps / (ms / 1e3) / 1e6
+
+    # End to end through the C-ABI host entry point, pinned host buffers.
+    h_rays = [torch.from_numpy(x).pin_memory() for x in (primary, shadow, ao)]
+    h_out = [torch.empty((primary.shape[0], 4), dtype=torch.float32).pin_memory(),
+             torch.empty(shadow.shape[0], dtype=torch.uint8).pin_memory(),
+             torch.empty(ao.shape[0], dtype=torch.uint8).pin_memory()]
+    kinds = ["closest", "any", "any"]
+
+    def e2e_step():
+        for r, o, kind in zip(h_rays, h_out, kinds):
+            scene.trace_host(r.numpy(), kind=kind, scheme=a.scheme, profile=a.profile,
+                             out=o.numpy(), stream=stream)
+
+    for _ in range(max(1, a.warmup)):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    e2e_steps = max(2, a.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_ok = (np.array_equal(h_out[0].numpy().view(np.uint32), out_h.cpu().numpy().view(np.uint32))
+              and np.array_equal(h_out[2].numpy(), out_a.cpu().numpy()))
+    h2d = sum(x.numel() * 4 for x in h_rays)
+    d2h = sum(x.numel() * x.element_size() for x in h_out)
+
+    # Roofline of the dominant kernel (largest share of the step).
+    dom = int(np.argmax(per_kernel_ms))
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg[dom]["bytes"] / (per_kernel_ms[dom] / 1e3) / 1e9
+    names = ["primary (closest)", "shadow (any)", "AO (any)"]
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a, tris, bvh, primary, shadow, ao, a.cpu_sample)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded clutter scene standing in for the reference's glTF scenes)",
+            "config": {
+                "workload": workload_name(a), "method": f"plain {a.scheme} kernel, FP32 nodes",
+                "profile": a.profile, "triangles": int(bvh.info["n_tris"]),
+                "rays_per_step": n_rays, "primary": int(primary.shape[0]),
+                "shadow": int(shadow.shape[0]), "ao": int(ao.shape[0]),
+                "l2": "inputs larger than L2 (rays ~%d MB per step); BVH stays L2-resident"
+                      % (n_rays * 32 // 2**20),
+                "bvh_bytes": {"nodes": scene.node_bytes, "leaves": scene.leaf_bytes},
+                "per_kernel_ms": dict(zip(names, per_kernel_ms)),
+                "setup_s": round(setup_s, 2),
+            },
+            "roofline": {
+                "bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks
+                else "fallback",
+                "traffic": None,
+                "algorithmic_bytes_per_launch": alg[dom]["bytes"],
+                "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
+            },
+            "e2e": {"value": n_rays * world / e2e_s / 1e6, "unit": METRIC,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "matches_device_results": bool(e2e_ok)},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": len(batches) * a.steps,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,286 @@
+"""bvhraytracer_gb300: GB300-native traversal of N-wide BVHs with L-wide leaves.
+
+Host mirror of the reference's trace interface over the C ABI of
+libbvhgpu.so (include/bvhgpu.h):
+
+* :class:`Bvh` — the reference's SAH builder (``Bvh`` + ``recursiveBvh``,
+  src/accelerationStructure/bvh.cpp:28-40, aabb.cpp:71-206), run on the host
+  in C++, with the flat exports of ``CompactNodeManager`` and
+  ``FastNodeManager``.
+* :class:`Scene` — the flat BVH resident in GPU memory, traced by sm_103a
+  kernels.
+* :class:`FastNodeManager` / :class:`CompactNodeManager` — batch versions of
+  the reference's trace calls (``intersect``, ``intersectSecondary``,
+  ``intersectWideAlternative``, ``intersectSecondaryWideAlternative``,
+  ``intersectImmediately``) with the reference's semantics per ray.
+
+Rays are ``[n, 8]`` float32 records ``(ox, oy, oz, tmax, dx, dy, dz, pad)``;
+closest hits are ``[n, 4]`` records ``(prim as int32 bits, t, u, v)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["Bvh", "Scene", "FastNodeManager", "CompactNodeManager", "sah_factor",
+           "BvhgpuError", "CLOSEST", "ANY", "PER_RAY", "STREAM", "PROFILE_INSTRUMENTED",
+           "PROFILE_FAST"]
+
+BvhgpuError = N.BvhgpuError
+CLOSEST, ANY = N.CLOSEST, N.ANY
+PER_RAY, STREAM = N.PER_RAY, N.STREAM
+PROFILE_INSTRUMENTED, PROFILE_FAST = N.PROFILE_INSTRUMENTED, N.PROFILE_FAST
+
+_KIND = {"closest": N.CLOSEST, "any": N.ANY}
+_SCHEME = {"per_ray": N.PER_RAY, "stream": N.STREAM}
+_PROFILE = {"instrumented": N.PROFILE_INSTRUMENTED, "fast": N.PROFILE_FAST}
+_FORMAT = {"fp32": N.NODES_FP32, "q8": N.NODES_Q8}
+
+
+def _ptr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def sah_factor(branching: int, leaf_size: int, gang: int = 4) -> float:
+    """sahNodeFactor of sahFactorConfigSse.txt (RayTracer::loadSahFactor)."""
+    out = C.c_float()
+    N.check(N.lib().bvhgpu_sah_factor(branching, leaf_size, gang, C.byref(out)))
+    return float(out.value)
+
+
+class Bvh:
+    """Host BVH: the reference's SAH build of a triangle soup.
+
+    ``tris``: ``[T, 9]`` (or ``[T, 3, 3]``) float32 world-space points in
+    scene-loader order; primitive ids in trace results index this array.
+    """
+
+    def __init__(self, tris, branching: int = 4, leaf_size: int = 4, *,
+                 leaf_split_option: int = 1, sah: Optional[float] = None, gang: int = 4,
+                 sort_each_split: bool = True, drop_zero_area: bool = True):
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.float32).reshape(-1, 9))
+        p = N.BuildParams(branching, leaf_size, int(sort_each_split), leaf_split_option,
+                          sah_factor(branching, leaf_size, gang) if sah is None else float(sah),
+                          int(drop_zero_area))
+        h = C.c_void_p()
+        N.check(N.lib().bvhgpu_bvh_build(t.ctypes.data, t.shape[0], C.byref(p), C.byref(h)))
+        self._h = h
+        self.params = p
+        info = N.BvhInfo()
+        N.check(N.lib().bvhgpu_bvh_info(h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in N.BvhInfo._fields_}
+        self.info["root_lo"] = list(info.root_lo)
+        self.info["root_hi"] = list(info.root_hi)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def export_compact(self) -> dict:
+        """CompactNodeV3 view (reference numbering) and sorted primitives."""
+        n = self.info["n_nodes"]
+        t = self.info["n_tris"]
+        out = {
+            "lo3": np.zeros((n, 3), np.float32), "hi3": np.zeros((n, 3), np.float32),
+            "child_begin": np.zeros(n, np.uint32), "child_count": np.zeros(n, np.uint32),
+            "prim_begin": np.zeros(n, np.uint32), "prim_count": np.zeros(n, np.uint32),
+            "order48": np.zeros((n, 48), np.int8), "depth": np.zeros(n, np.uint8),
+            "prim_ids": np.zeros(t, np.uint32), "prim_tri9": np.zeros((t, 9), np.float32),
+        }
+        N.check(N.lib().bvhgpu_bvh_export_compact(
+            self._h, *[_ptr(out[k]) for k in ("lo3", "hi3", "child_begin", "child_count",
+                                              "prim_begin", "prim_count", "order48", "depth",
+                                              "prim_ids", "prim_tri9")]))
+        return out
+
+    def export_fast(self, gang: int = 4, node_memory: int = 0, leaf_memory: int = 0) -> dict:
+        """FastNodeManager<gang, node_memory> arrays and trianglePoints."""
+        node_memory = node_memory or -(-self.info["branching"] // gang) * gang
+        leaf_memory = leaf_memory or -(-self.info["leaf_size"] // gang) * gang
+        nn, nf = C.c_uint64(), C.c_uint64()
+        N.check(N.lib().bvhgpu_bvh_fast_sizes(self._h, gang, node_memory, leaf_memory,
+                                              C.byref(nn), C.byref(nf)))
+        n = nn.value
+        out = {
+            "gang": gang, "node_memory": node_memory, "leaf_memory": leaf_memory,
+            "bounds": np.zeros((n, 6 * node_memory), np.float32),
+            "begin": np.zeros(n, np.uint32),
+            "order": np.zeros((n, 3 * node_memory), np.int8),
+            "child_type": np.zeros(n, np.uint32),
+            "tri_points": np.zeros(nf.value, np.float32),
+        }
+        N.check(N.lib().bvhgpu_bvh_export_fast(
+            self._h, gang, node_memory, leaf_memory,
+            *[_ptr(out[k]) for k in ("bounds", "begin", "order", "child_type", "tri_points")]))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().bvhgpu_bvh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """A BVH resident in GPU memory (device layout of the C ABI)."""
+
+    def __init__(self, bvh: Bvh, *, gang: int = 4, leaf_memory: int = 0,
+                 node_format: str = "fp32", top_levels: int = 0, device: int = 0):
+        p = N.SceneParams(gang, leaf_memory, _FORMAT[node_format], top_levels, device)
+        h = C.c_void_p()
+        N.check(N.lib().bvhgpu_scene_create(bvh.handle, C.byref(p), C.byref(h)))
+        self._h = h
+        self.device = device
+        self.bvh_info = dict(bvh.info)
+        self.node_format = node_format
+        b = [C.c_uint64() for _ in range(4)]
+        N.check(N.lib().bvhgpu_scene_bytes(h, *[C.byref(x) for x in b]))
+        self.node_bytes, self.leaf_bytes, self.node_record_bytes, self.leaf_record_bytes = (
+            x.value for x in b)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def trace(self, rays, *, kind: str = "closest", scheme: str = "per_ray",
+              profile: str = "instrumented", workgroup: int = 16, block: int = 128,
+              counters: bool = False, depth_hist: bool = False, out=None, stream=None) -> dict:
+        """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
+
+        Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
+        (any), plus ``"counters"`` ``[n, 8]`` int32 and ``"depth_hist"``
+        ``[2, 64]`` int64 when requested. Asynchronous on ``stream``
+        (default: torch's current stream).
+        """
+        import torch
+        assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
+        rays = rays.contiguous()
+        n = rays.shape[0]
+        k = _KIND[kind]
+        res = {}
+        dev = rays.device
+        if k == N.CLOSEST:
+            hits = out if out is not None else torch.empty((n, 4), dtype=torch.float32, device=dev)
+            res["hits"] = hits
+            hp, op = _ptr(hits), None
+        else:
+            occ = out if out is not None else torch.empty(n, dtype=torch.uint8, device=dev)
+            res["occluded"] = occ
+            hp, op = None, _ptr(occ)
+        cp = hh = None
+        if counters:
+            res["counters"] = torch.zeros((n, N.COUNTERS_PER_RAY), dtype=torch.int32, device=dev)
+            cp = _ptr(res["counters"])
+        if depth_hist:
+            res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
+            hh = _ptr(res["depth_hist"])
+        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block)
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
+                                     C.c_void_p(s.cuda_stream)))
+        return res
+
+    def trace_host(self, rays: np.ndarray, *, kind: str = "closest", scheme: str = "per_ray",
+                   profile: str = "instrumented", workgroup: int = 16, block: int = 128,
+                   out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+        """Host rays in, host results out (copies inside the call)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        k = _KIND[kind]
+        if out is None:
+            out = (np.empty((n, 4), np.float32) if k == N.CLOSEST else np.empty(n, np.uint8))
+        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block)
+        sp = 0
+        if stream is not None:
+            sp = stream.cuda_stream
+        N.check(N.lib().bvhgpu_trace_host(
+            self._h, _ptr(rays), n, C.byref(o),
+            _ptr(out) if k == N.CLOSEST else None, _ptr(out) if k == N.ANY else None,
+            C.c_void_p(sp)))
+        return out
+
+    def status(self, stream=None) -> None:
+        """Raises if a kernel of this scene recorded a device-side error."""
+        sp = stream.cuda_stream if stream is not None else 0
+        N.check(N.lib().bvhgpu_scene_status(self._h, C.c_void_p(sp)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().bvhgpu_scene_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hit_prims(hits) -> "np.ndarray":
+    """Primitive ids (int32) of a ``[n, 4]`` hit record tensor or array."""
+    if isinstance(hits, np.ndarray):
+        return hits.view(np.int32)[:, 0]
+    return hits.view(dtype=__import__("torch").int32)[:, 0]
+
+
+class FastNodeManager:
+    """Batch form of FastNodeManager's trace calls (fast profile).
+
+    Mirrors fastNodeManager.h: ``intersect`` (1328-1418), ``intersectSecondary``
+    (1420-1493), ``intersectWideAlternative`` (835-1049) and
+    ``intersectSecondaryWideAlternative`` (1051-1230). Rays use FastRay
+    semantics: the direction is used as given (not normalised).
+    """
+
+    def __init__(self, bvh: Bvh, leaf_memory: int = 0, *, gang: int = 4,
+                 work_group_size: int = 16, node_format: str = "fp32", device: int = 0):
+        self.scene = Scene(bvh, gang=gang, leaf_memory=leaf_memory, node_format=node_format,
+                           device=device)
+        self.work_group_size = work_group_size
+
+    def intersect(self, rays):
+        return self.scene.trace(rays, kind="closest", scheme="per_ray", profile="fast")["hits"]
+
+    def intersect_secondary(self, rays):
+        return self.scene.trace(rays, kind="any", scheme="per_ray", profile="fast")["occluded"]
+
+    def intersect_wide_alternative(self, rays):
+        return self.scene.trace(rays, kind="closest", scheme="stream", profile="fast",
+                                workgroup=self.work_group_size)["hits"]
+
+    def intersect_secondary_wide_alternative(self, rays):
+        return self.scene.trace(rays, kind="any", scheme="stream", profile="fast",
+                                workgroup=self.work_group_size)["occluded"]
+
+
+class CompactNodeManager:
+    """Batch form of CompactNodeManager<CompactNodeV3>'s trace calls with the
+    per-ray counters (instrumented profile): ``intersectImmediately``
+    (compactNode.cpp:604-814) and ``intersectWideAlternative`` (357-601).
+    Directions are normalised like Ray::Ray; t is in world units."""
+
+    def __init__(self, bvh: Bvh, *, gang: int = 4, work_group_size: int = 16, device: int = 0):
+        self.scene = Scene(bvh, gang=gang, device=device)
+        self.work_group_size = work_group_size
+
+    def intersect_immediately(self, rays, shadow: bool = False, counters: bool = True):
+        return self.scene.trace(rays, kind="any" if shadow else "closest", scheme="per_ray",
+                                profile="instrumented", counters=counters, depth_hist=counters)
+
+    def intersect_wide_alternative(self, rays, shadow: bool = False, counters: bool = True):
+        return self.scene.trace(rays, kind="any" if shadow else "closest", scheme="stream",
+                                profile="instrumented", workgroup=self.work_group_size,
+                                counters=counters, depth_hist=counters)

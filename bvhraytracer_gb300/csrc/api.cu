@@ -1,0 +1,416 @@
+// C ABI (include/bvhgpu.h): host BVH build and export, device scene
+// management and trace launches.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "bvh_builder.hpp"
+#include "bvh_export.hpp"
+#include "bvhgpu.h"
+#include "bvhgpu_status.hpp"
+#include "launch.cuh"
+
+namespace bvhgpu {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  if (code != BVHGPU_OK) g_last_error = msg;
+  return code;
+}
+
+static int cuda_error(cudaError_t e, const char* what) {
+  return set_error(BVHGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace bvhgpu
+
+using namespace bvhgpu;
+
+struct bvhgpu_bvh {
+  Bvh bvh;
+  uint64_t n_input = 0;
+};
+
+// Device copy of a flat BVH plus the buffers its launches reuse.
+struct bvhgpu_scene {
+  int device = 0;
+  DeviceLayout layout;  // host copy of the uploaded arrays (sizes and ids)
+  int max_stack = 0;
+  uint8_t* d_nodes = nullptr;
+  float* d_leaves = nullptr;
+  uint32_t* d_leaf_prim = nullptr;
+  uint8_t* d_leaf_depth = nullptr;
+  int* d_status = nullptr;
+  // Staging for bvhgpu_trace_host (grown on demand).
+  std::mutex staging_mu;
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+
+  dev::SceneDev dev_view() const {
+    dev::SceneDev s;
+    s.nodes = d_nodes;
+    s.leaves = d_leaves;
+    s.leaf_prim = d_leaf_prim;
+    s.leaf_depth = d_leaf_depth;
+    s.root_entry = layout.root_entry;
+    s.top_nodes = layout.top_nodes;
+    s.leaf_memory = layout.leaf_memory;
+    s.gang = layout.gang;
+    s.status = d_status;
+    return s;
+  }
+  void release() {
+    cudaFree(d_nodes);
+    cudaFree(d_leaves);
+    cudaFree(d_leaf_prim);
+    cudaFree(d_leaf_depth);
+    cudaFree(d_status);
+    cudaFree(d_stage);
+    d_nodes = nullptr;
+    d_leaves = nullptr;
+    d_leaf_prim = nullptr;
+    d_leaf_depth = nullptr;
+    d_status = nullptr;
+    d_stage = nullptr;
+  }
+};
+
+template <typename T>
+static int upload(T** dst, const std::vector<T>& src) {
+  size_t bytes = std::max<size_t>(src.size() * sizeof(T), 16);
+  cudaError_t e = cudaMalloc((void**)dst, bytes);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMalloc");
+  if (!src.empty()) {
+    e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy");
+  }
+  return BVHGPU_OK;
+}
+
+static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
+  if (!o) return set_error(BVHGPU_ERR_BAD_ARG, "null options");
+  if (o->kind != BVHGPU_CLOSEST && o->kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "kind");
+  if (o->scheme != BVHGPU_PER_RAY && o->scheme != BVHGPU_STREAM)
+    return set_error(BVHGPU_ERR_BAD_ARG, "scheme");
+  if (o->profile != BVHGPU_PROFILE_INSTRUMENTED && o->profile != BVHGPU_PROFILE_FAST)
+    return set_error(BVHGPU_ERR_BAD_ARG, "profile");
+  c.kind = o->kind;
+  c.scheme = o->scheme;
+  c.profile = o->profile;
+  c.block = o->block ? o->block : 128;
+  if (c.block != 32 && c.block != 64 && c.block != 128)
+    return set_error(BVHGPU_ERR_BAD_ARG, "block must be 32, 64 or 128");
+  int wg = o->workgroup ? o->workgroup : 16;
+  if (wg != 8 && wg != 16)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stream workgroup must be 8 or 16 (64 or 256 rays)");
+  c.packet = wg * wg;
+  return BVHGPU_OK;
+}
+
+static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, const dev::LaunchCfg& cfg,
+                  cudaStream_t st) {
+  const dev::SceneDev sc = s->dev_view();
+  cudaError_t e;
+  switch (s->layout.node_stride) {
+    case 4: e = dev::launch_trace_n4(sc, a, cfg, st); break;
+    case 8: e = dev::launch_trace_n8(sc, a, cfg, st); break;
+    case 12: e = dev::launch_trace_n12(sc, a, cfg, st); break;
+    case 16: e = dev::launch_trace_n16(sc, a, cfg, st); break;
+    default: return set_error(BVHGPU_ERR_UNSUPPORTED, "node width");
+  }
+  if (e != cudaSuccess) return cuda_error(e, "trace launch");
+  return BVHGPU_OK;
+}
+
+extern "C" {
+
+const char* bvhgpu_last_error(void) { return g_last_error.c_str(); }
+
+int bvhgpu_bvh_build(const float* tris, uint64_t n_tris, const bvhgpu_build_params_t* params,
+                     bvhgpu_bvh_t* out) {
+  if (!tris || !params || !out) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  *out = nullptr;
+  BuildParams p;
+  p.branching = params->branching;
+  p.leaf_size = params->leaf_size;
+  p.sort_each_split = params->sort_each_split;
+  p.leaf_split_option = params->leaf_split_option;
+  p.sah_factor = params->sah_factor;
+  p.drop_zero_area = params->drop_zero_area;
+  if (!std::isfinite(p.sah_factor)) return set_error(BVHGPU_ERR_BAD_ARG, "sah_factor not finite");
+  auto* h = new (std::nothrow) bvhgpu_bvh();
+  if (!h) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  int rc;
+  try {
+    rc = h->bvh.build(tris, n_tris, p);
+  } catch (const std::bad_alloc&) {
+    rc = BVHGPU_ERR_OOM;
+  }
+  if (rc != BVHGPU_OK) {
+    delete h;
+    return set_error(rc, "bvh build failed (check N in 2..16, L in 1..16, sort_each_split=1, "
+                         "finite vertices, at least one non-degenerate triangle)");
+  }
+  h->n_input = n_tris;
+  *out = h;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_info(bvhgpu_bvh_t h, bvhgpu_bvh_info_t* info) {
+  if (!h || !info) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  const Bvh& b = h->bvh;
+  info->n_input_tris = h->n_input;
+  info->n_tris = b.tris.size();
+  info->n_nodes = b.nodes.size();
+  info->n_inner = b.inner_count;
+  info->n_leaves = b.leaf_count;
+  info->depth = b.bvh_depth;
+  info->max_stack = b.max_stack;
+  info->branching = b.params.branching;
+  info->leaf_size = b.params.leaf_size;
+  for (int k = 0; k < 3; ++k) {
+    info->root_lo[k] = b.nodes[0].bmin[k];
+    info->root_hi[k] = b.nodes[0].bmax[k];
+  }
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_free(bvhgpu_bvh_t h) {
+  delete h;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_sah_factor(int32_t branching, int32_t leaf_size, int32_t gang, float* out) {
+  if (!out || branching < 1 || leaf_size < 1 || (gang != 4 && gang != 8))
+    return set_error(BVHGPU_ERR_BAD_ARG, "bad sah factor query");
+  *out = sah_factor_sse(branching, leaf_size, gang);
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_export_compact(bvhgpu_bvh_t h, float* lo3, float* hi3, uint32_t* child_begin,
+                              uint32_t* child_count, uint32_t* prim_begin, uint32_t* prim_count,
+                              int8_t* order48, uint8_t* depth, uint32_t* prim_ids,
+                              float* prim_tri9) {
+  if (!h) return set_error(BVHGPU_ERR_BAD_ARG, "null bvh");
+  const Bvh& b = h->bvh;
+  for (size_t i = 0; i < b.nodes.size(); ++i) {
+    const CompactNode& c = b.nodes[i];
+    for (int k = 0; k < 3; ++k) {
+      if (lo3) lo3[i * 3 + k] = c.bmin[k];
+      if (hi3) hi3[i * 3 + k] = c.bmax[k];
+    }
+    if (child_begin) child_begin[i] = c.child_begin;
+    if (child_count) child_count[i] = c.child_count;
+    if (prim_begin) prim_begin[i] = c.prim_begin;
+    if (prim_count) prim_count[i] = c.prim_count;
+    if (order48) std::memcpy(order48 + i * 48, &c.order[0][0], 48);
+    if (depth) depth[i] = c.depth;
+  }
+  for (size_t i = 0; i < b.prims.size(); ++i) {
+    const Triangle& t = b.tris[b.prims[i]];
+    if (prim_ids) prim_ids[i] = t.id;
+    if (prim_tri9)
+      for (int v = 0; v < 3; ++v)
+        for (int k = 0; k < 3; ++k) prim_tri9[i * 9 + v * 3 + k] = t.p[v][k];
+  }
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_fast_sizes(bvhgpu_bvh_t h, int32_t gang, int32_t node_memory, int32_t leaf_memory,
+                          uint64_t* n_nodes, uint64_t* n_tri_floats) {
+  if (!h || !n_nodes || !n_tri_floats) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  if ((gang != 4 && gang != 8) || node_memory < h->bvh.params.branching || node_memory % gang ||
+      leaf_memory < h->bvh.params.leaf_size || leaf_memory % gang || node_memory > 32)
+    return set_error(BVHGPU_ERR_BAD_ARG, "node/leaf memory must be gang multiples >= N/L");
+  *n_nodes = h->bvh.nodes.size();
+  *n_tri_floats = (uint64_t)h->bvh.leaf_count * leaf_memory * 9;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_export_fast(bvhgpu_bvh_t h, int32_t gang, int32_t node_memory, int32_t leaf_memory,
+                           float* bounds, uint32_t* begin, int8_t* order, uint32_t* child_type,
+                           float* tri_points) {
+  if (!h) return set_error(BVHGPU_ERR_BAD_ARG, "null bvh");
+  FastView v;
+  int rc = export_fast(h->bvh, gang, node_memory, leaf_memory, v);
+  if (rc) return set_error(rc, "fast export failed");
+  if (bounds) std::memcpy(bounds, v.bounds.data(), v.bounds.size() * 4);
+  if (begin) std::memcpy(begin, v.begin.data(), v.begin.size() * 4);
+  if (order) std::memcpy(order, v.order.data(), v.order.size());
+  if (child_type) std::memcpy(child_type, v.child_type.data(), v.child_type.size() * 4);
+  if (tri_points) std::memcpy(tri_points, v.tri_points.data(), v.tri_points.size() * 4);
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvhgpu_scene_t* out) {
+  if (!h || !params || !out) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return set_error(BVHGPU_ERR_NO_DEVICE, "no CUDA device");
+  if (params->device < 0 || params->device >= ndev)
+    return set_error(BVHGPU_ERR_BAD_ARG, "device ordinal out of range");
+  if (params->node_format != BVHGPU_NODES_FP32)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "node format not built yet");
+  auto* s = new (std::nothrow) bvhgpu_scene();
+  if (!s) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  s->device = params->device;
+  int rc = build_device_layout(h->bvh, params->gang, params->leaf_memory, params->node_format,
+                               params->top_levels, s->layout);
+  if (rc) {
+    delete s;
+    return set_error(rc, "device layout failed (gang 4/8, leaf_memory >= L and a gang multiple <= 16)");
+  }
+  s->max_stack = h->bvh.max_stack;
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_error(e, "cudaSetDevice");
+  }
+  if ((rc = upload(&s->d_nodes, s->layout.nodes)) || (rc = upload(&s->d_leaves, s->layout.leaves)) ||
+      (rc = upload(&s->d_leaf_prim, s->layout.leaf_prim)) ||
+      (rc = upload(&s->d_leaf_depth, s->layout.leaf_depth))) {
+    s->release();
+    delete s;
+    return rc;
+  }
+  e = cudaMalloc((void**)&s->d_status, 16);
+  if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, 16);
+  if (e != cudaSuccess) {
+    s->release();
+    delete s;
+    return cuda_error(e, "status word");
+  }
+  // The host copy of the big arrays is not needed after the upload.
+  s->layout.nodes.clear();
+  s->layout.nodes.shrink_to_fit();
+  s->layout.leaves.clear();
+  s->layout.leaves.shrink_to_fit();
+  *out = s;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_free(bvhgpu_scene_t s) {
+  if (!s) return BVHGPU_OK;
+  cudaSetDevice(s->device);
+  s->release();
+  delete s;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_bytes(bvhgpu_scene_t s, uint64_t* node_bytes, uint64_t* leaf_bytes,
+                       uint64_t* node_record_bytes, uint64_t* leaf_record_bytes) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  const DeviceLayout& L = s->layout;
+  if (node_bytes) *node_bytes = (uint64_t)L.n_inner * L.record_bytes;
+  if (leaf_bytes) *leaf_bytes = (uint64_t)L.n_leaves * L.leaf_memory * 9 * 4;
+  if (node_record_bytes) *node_record_bytes = (uint64_t)L.record_bytes;
+  if (leaf_record_bytes) *leaf_record_bytes = (uint64_t)L.leaf_memory * 9 * 4;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
+                 const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                 uint32_t* counters, uint64_t* depth_hist, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  dev::LaunchCfg cfg;
+  int rc = check_opts(opts, cfg);
+  if (rc) return rc;
+  if (n == 0) return BVHGPU_OK;
+  if (!rays || ((uintptr_t)rays & 15)) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null or not 16-byte aligned");
+  if (cfg.kind == BVHGPU_CLOSEST && (!hits || ((uintptr_t)hits & 15)))
+    return set_error(BVHGPU_ERR_BAD_ARG, "hits: null or not 16-byte aligned");
+  if (cfg.kind == BVHGPU_ANY && !occluded) return set_error(BVHGPU_ERR_BAD_ARG, "occluded: null");
+  if (n > (1ull << 40)) return set_error(BVHGPU_ERR_BAD_ARG, "too many rays");
+  cfg.count = counters != nullptr || depth_hist != nullptr;
+  dev::TraceArgs a;
+  a.rays = rays;
+  a.n = n;
+  a.hits = hits;
+  a.occluded = occluded;
+  a.counters = counters;
+  a.depth_hist = reinterpret_cast<unsigned long long*>(depth_hist);
+  a.stack_cap = s->max_stack;
+  if (cfg.scheme == BVHGPU_STREAM &&
+      dev::stream_smem_bytes(cfg.packet, a.stack_cap, cfg.count) > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet does not fit shared memory for this tree depth");
+  if (cfg.scheme == BVHGPU_PER_RAY && (size_t)a.stack_cap * cfg.block * 4 > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  return launch(s, a, cfg, (cudaStream_t)stream);
+}
+
+int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
+                      const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                      void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  dev::LaunchCfg cfg;
+  int rc = check_opts(opts, cfg);
+  if (rc) return rc;
+  if (n == 0) return BVHGPU_OK;
+  if (!rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
+  const bool closest = cfg.kind == BVHGPU_CLOSEST;
+  if (closest ? !hits : !occluded) return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  std::lock_guard<std::mutex> lock(s->staging_mu);
+  const size_t ray_bytes = n * sizeof(bvhgpu_ray_t);
+  const size_t out_bytes = closest ? n * sizeof(bvhgpu_hit_t) : ((n + 15) / 16) * 16;
+  const size_t need = ray_bytes + out_bytes;
+  if (need > s->stage_bytes) {
+    cudaStreamSynchronize(st);
+    cudaFree(s->d_stage);
+    s->d_stage = nullptr;
+    s->stage_bytes = 0;
+    e = cudaMalloc(&s->d_stage, need);
+    if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "staging allocation failed");
+    s->stage_bytes = need;
+  }
+  auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(s->d_stage);
+  uint8_t* d_out = reinterpret_cast<uint8_t*>(s->d_stage) + ray_bytes;
+  e = cudaMemcpyAsync(d_rays, rays, ray_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_error(e, "copy rays in");
+  dev::TraceArgs a;
+  a.rays = d_rays;
+  a.n = n;
+  a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
+  a.occluded = closest ? nullptr : d_out;
+  a.counters = nullptr;
+  a.depth_hist = nullptr;
+  a.stack_cap = s->max_stack;
+  rc = launch(s, a, cfg, st);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(closest ? (void*)hits : (void*)occluded, d_out,
+                      closest ? n * sizeof(bvhgpu_hit_t) : n, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_error(e, "copy results out");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "synchronise");
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_status(bvhgpu_scene_t s, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  int code = 0;
+  e = cudaMemcpyAsync(&code, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "status read");
+  if (code != 0) {
+    cudaMemsetAsync(s->d_status, 0, sizeof(int), (cudaStream_t)stream);
+    cudaStreamSynchronize((cudaStream_t)stream);
+    return set_error(code, code == BVHGPU_ERR_STACK_OVERFLOW ? "device: traversal stack overflow"
+                                                            : "device: bounded wait timed out");
+  }
+  return BVHGPU_OK;
+}
+
+}  // extern "C"

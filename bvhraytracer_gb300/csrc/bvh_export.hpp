@@ -1,0 +1,74 @@
+// Flat exports of a built BVH: the reference's FastNodeManager view and the
+// device layout used by the sm_103a kernels.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "bvh_builder.hpp"
+
+namespace bvhgpu {
+
+// FastNodeManager<gang, node_memory, wg> arrays (fastNodeManager.h:1495-1688).
+struct FastView {
+  int gang = 4, node_memory = 4, leaf_memory = 4;
+  std::vector<float> bounds;       // n_nodes * 6 * node_memory
+  std::vector<uint32_t> begin;     // childIdBegin / primIdBegin
+  std::vector<int8_t> order;       // n_nodes * 3 * node_memory
+  std::vector<uint32_t> child_type;
+  std::vector<float> tri_points;   // trianglePoints
+};
+int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, FastView& out);
+
+// Device layout.
+//
+// Inner-node record for branching N (Nm = N rounded up to 4), 16-byte aligned:
+//   float    box[6][Nm]     child boxes, SoA: lo.x lo.y lo.z hi.x hi.y hi.z
+//   uint32   inner_base     index of the first inner child
+//   uint32   leaf_base      index of the first leaf child
+//   uint16   leaf_mask      bit j: child j is a leaf
+//   uint8    count          number of children
+//   uint8    depth          tree depth of this node
+//   uint8    order[3][Nm]   traverseOrderEachAxis
+//   uint8    leaf_cnt[Nm]   triangles of leaf child j (0 for inner children)
+// Leaves are not given node records: leaf k is the k-th leaf of the
+// reference's customTreeOrder and its triangle block is exactly the
+// reference's trianglePoints block (9 * leaf_memory floats, SoA with stride
+// = count rounded up to the gang, sentinel (stride, NaN) in the last two
+// floats when the stride is below leaf_memory).
+//
+// Q8 record (branching N, Nm as above), 16-byte aligned:
+//   float    origin[3]      parent box lower corner (the quantisation frame)
+//   int8     exp[3], pad    per-axis power-of-two step: step = 2^exp
+//   uint32   inner_base, leaf_base
+//   uint16   leaf_mask; uint8 count; uint8 depth
+//   uint8    order[3][Nm]; uint8 leaf_cnt[Nm]
+//   uint8    q[6][Nm]       child boxes: lo = origin + q_lo*step (rounded
+//                           down), hi = origin + q_hi*step (rounded up)
+struct DeviceLayout {
+  int branching = 4, node_stride = 4, leaf_memory = 4, gang = 4;
+  int node_format = 0;
+  int record_bytes = 0;
+  std::vector<uint8_t> nodes;         // n_inner * record_bytes
+  std::vector<float> leaves;          // n_leaves * 9 * leaf_memory
+  std::vector<uint32_t> leaf_prim;    // n_leaves * leaf_memory (input ids)
+  std::vector<uint8_t> leaf_depth;    // n_leaves
+  uint32_t n_inner = 0, n_leaves = 0;
+  uint32_t root_entry = 0;            // stack entry of the root
+  uint32_t top_nodes = 0;             // inner nodes laid out first
+};
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kLeafCountShift = 27;
+constexpr uint32_t kLeafIndexMask = (1u << 27) - 1;
+
+inline int round_up(int v, int m) { return ((v + m - 1) / m) * m; }
+inline int fp32_record_bytes(int nm) { return round_up(28 * nm + 12, 16); }
+inline int q8_record_bytes(int nm) { return round_up(32 + 4 * nm + 6 * nm, 16); }
+
+int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_format,
+                        int top_levels, DeviceLayout& out);
+
+// sahFactorConfigSse.txt (branchFactor, leafSize, sahNodeFactor).
+float sah_factor_sse(int branching, int leaf_size, int gang);
+
+}  // namespace bvhgpu

@@ -1,0 +1,72 @@
+// Host-side launch helpers: pick the kernel instance for a trace request.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "traverse.cuh"
+
+namespace bvhgpu {
+namespace dev {
+
+struct LaunchCfg {
+  int kind = BVHGPU_CLOSEST;
+  int scheme = BVHGPU_PER_RAY;
+  int profile = BVHGPU_PROFILE_INSTRUMENTED;
+  bool count = false;
+  int block = 128;      // per-ray scheme threads per block
+  int packet = 256;     // stream scheme rays per block
+};
+
+template <typename K>
+inline cudaError_t set_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int NM, int PROFILE, int KIND, bool COUNT>
+inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& cfg,
+                              cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  if (cfg.scheme == BVHGPU_PER_RAY) {
+    const int bs = cfg.block;
+    const size_t smem = (size_t)a.stack_cap * bs * 4;
+    auto k = trace_dfs_kernel<NM, PROFILE, KIND, COUNT>;
+    cudaError_t e = set_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    const uint64_t grid = (a.n + bs - 1) / bs;
+    k<<<(unsigned)grid, bs, smem, s>>>(sc, a);
+  } else {
+    const int p = cfg.packet;
+    const size_t smem = stream_smem_bytes(p, a.stack_cap, COUNT);
+    auto k = trace_stream_kernel<NM, PROFILE, KIND, COUNT>;
+    cudaError_t e = set_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    const uint64_t grid = (a.n + p - 1) / p;
+    k<<<(unsigned)grid, p, smem, s>>>(sc, a);
+  }
+  return cudaGetLastError();
+}
+
+template <int NM>
+inline cudaError_t launch_for_width(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& c,
+                                    cudaStream_t s) {
+  const int code = (c.profile << 2) | (c.kind << 1) | (c.count ? 1 : 0);
+  switch (code) {
+    case 0: return launch_one<NM, 0, 0, false>(sc, a, c, s);
+    case 1: return launch_one<NM, 0, 0, true>(sc, a, c, s);
+    case 2: return launch_one<NM, 0, 1, false>(sc, a, c, s);
+    case 3: return launch_one<NM, 0, 1, true>(sc, a, c, s);
+    case 4: return launch_one<NM, 1, 0, false>(sc, a, c, s);
+    case 5: return launch_one<NM, 1, 0, true>(sc, a, c, s);
+    case 6: return launch_one<NM, 1, 1, false>(sc, a, c, s);
+    case 7: return launch_one<NM, 1, 1, true>(sc, a, c, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_trace_n4(const SceneDev&, const TraceArgs&, const LaunchCfg&, cudaStream_t);
+cudaError_t launch_trace_n8(const SceneDev&, const TraceArgs&, const LaunchCfg&, cudaStream_t);
+cudaError_t launch_trace_n12(const SceneDev&, const TraceArgs&, const LaunchCfg&, cudaStream_t);
+cudaError_t launch_trace_n16(const SceneDev&, const TraceArgs&, const LaunchCfg&, cudaStream_t);
+
+}  // namespace dev
+}  // namespace bvhgpu

@@ -1,0 +1,11 @@
+// Kernel instantiations for node records with 12 child slots.
+#include "launch.cuh"
+
+namespace bvhgpu {
+namespace dev {
+cudaError_t launch_trace_n12(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& cfg,
+                              cudaStream_t s) {
+  return launch_for_width<12>(sc, a, cfg, s);
+}
+}  // namespace dev
+}  // namespace bvhgpu

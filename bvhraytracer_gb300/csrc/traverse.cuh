@@ -1,0 +1,597 @@
+// Traversal kernels, templated on the branching factor N (node record size),
+// the profile (instrumented / fast), the ray kind (closest / any) and whether
+// per-ray counters are recorded.
+//
+// Semantics (identical for both schemes and matching the reference per ray):
+//   * the root's own box is never tested; traversal starts by popping it
+//     (fastNodeManager.h:1334-1349, compactNode.cpp:610-621);
+//   * an inner node tests every child box with the ray's current tMax and
+//     pushes the hit children in traverseOrderEachAxis[code] order, ascending
+//     when direction[code] <= 0 and descending otherwise, so the child nearest
+//     along the major axis is popped first (compactNode.cpp:781-809). Fast
+//     any-hit rays push in child-index order (fastNodeManager.h:1481-1488);
+//   * stack entries are not re-culled when popped (useDistance == false);
+//   * a leaf tests all its triangles; closest hits shrink tMax as they go;
+//     any-hit rays end at the first leaf with a hit (compactNode.cpp:690-706,
+//     fastNodeManager.h:1444-1461).
+#pragma once
+#include "device_common.cuh"
+
+namespace bvhgpu {
+namespace dev {
+
+struct SceneDev {
+  const uint8_t* nodes;       // inner-node records
+  const float* leaves;        // leaf triangle blocks (9 * leaf_memory floats each)
+  const uint32_t* leaf_prim;  // leaf_memory input ids per leaf
+  const uint8_t* leaf_depth;  // tree depth per leaf
+  uint32_t root_entry;
+  uint32_t top_nodes;         // inner records laid out first (staged in shared memory)
+  int leaf_memory;
+  int gang;
+  int* status;                // first device-side error (0 = none)
+};
+
+struct TraceArgs {
+  const bvhgpu_ray_t* rays;
+  uint64_t n;
+  bvhgpu_hit_t* hits;
+  uint8_t* occluded;
+  uint32_t* counters;
+  unsigned long long* depth_hist;
+  int stack_cap;              // stack entries per ray
+};
+
+struct Counters {
+  uint32_t node_visits = 0, leaf_visits = 0, box_tests = 0, box_hits = 0;
+  uint32_t tri_tests = 0, tri_hits = 0, max_stack = 0;
+};
+
+constexpr int round4(int n) { return (n + 3) / 4 * 4; }
+template <int N>
+struct NodeFmt {
+  static constexpr int NM = round4(N);
+  static constexpr int REC = ((28 * NM + 12) + 15) / 16 * 16;
+  static constexpr int META = 24 * NM;            // byte offset of the metadata
+  static constexpr int ORDER = META + 12;         // order[3][NM]
+  static constexpr int LCNT = ORDER + 3 * NM;     // leaf_cnt[NM]
+};
+
+// Byte i (0 <= i < 16) of a little-endian 16-byte group held as two words.
+BVHGPU_DEV int byte_at(uint64_t lo, uint64_t hi, int i) {
+  uint64_t w = i >= 8 ? hi : lo;
+  return (int)((w >> ((i & 7) * 8)) & 0xFFu);
+}
+
+template <int NM>
+BVHGPU_DEV void load_bytes(const uint8_t* p, uint64_t& lo, uint64_t& hi) {
+  // NM bytes at a 4-byte aligned address.
+  uint32_t w0 = ldgu(p), w1 = NM > 4 ? ldgu(p + 4) : 0u;
+  uint32_t w2 = NM > 8 ? ldgu(p + 8) : 0u, w3 = NM > 12 ? ldgu(p + 12) : 0u;
+  lo = (uint64_t)w0 | ((uint64_t)w1 << 32);
+  hi = (uint64_t)w2 | ((uint64_t)w3 << 32);
+}
+
+// One inner-node visit: slab-test the children and push the hits.
+// Returns false on stack overflow.
+template <int N, int PROFILE, int KIND, bool COUNT>
+BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r, float tmax,
+                           uint32_t* stack, int stride, int& sp, int cap, Counters& ctr,
+                           int& depth_out) {
+  using F = NodeFmt<N>;
+  constexpr int NM = F::NM;
+  const uint4 meta = ldgu4(rec + F::META);
+  const uint32_t inner_base = meta.x, leaf_base = meta.y;
+  const uint32_t leaf_mask = meta.z & 0xFFFFu;
+  const int count = (int)((meta.z >> 16) & 0xFFu);
+  depth_out = (int)(meta.z >> 24);
+
+  uint32_t hit = 0;
+#pragma unroll
+  for (int q = 0; q < NM / 4; ++q) {
+    const float4 lx = ldg4(rec + (0 * NM + 4 * q) * 4);
+    const float4 ly = ldg4(rec + (1 * NM + 4 * q) * 4);
+    const float4 lz = ldg4(rec + (2 * NM + 4 * q) * 4);
+    const float4 hx = ldg4(rec + (3 * NM + 4 * q) * 4);
+    const float4 hy = ldg4(rec + (4 * NM + 4 * q) * 4);
+    const float4 hz = ldg4(rec + (5 * NM + 4 * q) * 4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (4 * q + k < N) {
+        bool h = slab(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k), f4get(hy, k),
+                      f4get(hz, k), r, tmax);
+        hit |= (uint32_t)h << (4 * q + k);
+      }
+    }
+  }
+  hit &= (1u << count) - 1u;
+  if (COUNT) {
+    ctr.node_visits++;
+    ctr.box_tests += (uint32_t)count;
+    ctr.box_hits += (uint32_t)__popc(hit);
+  }
+  if (hit == 0) return true;
+
+  uint64_t clo, chi;
+  load_bytes<NM>(rec + F::LCNT, clo, chi);
+  auto entry = [&](int c) -> uint32_t {
+    const uint32_t below = (1u << c) - 1u;
+    if ((leaf_mask >> c) & 1u) {
+      uint32_t cnt = (uint32_t)byte_at(clo, chi, c);
+      return kLeafBit | ((cnt - 1u) << kLeafCountShift) |
+             (leaf_base + (uint32_t)__popc(leaf_mask & below));
+    }
+    return inner_base + (uint32_t)__popc(~leaf_mask & below);
+  };
+  const bool index_order = (PROFILE == BVHGPU_PROFILE_FAST && KIND == BVHGPU_ANY);
+  if (index_order) {
+    for (int c = 0; c < count; ++c) {
+      if ((hit >> c) & 1u) {
+        if (sp >= cap) return false;
+        stack[sp * stride] = entry(c);
+        ++sp;
+      }
+    }
+  } else {
+    uint64_t olo, ohi;
+    load_bytes<NM>(rec + F::ORDER + r.code * NM, olo, ohi);
+    for (int k = 0; k < count; ++k) {
+      const int i = r.reverse ? k : count - 1 - k;
+      const int c = byte_at(olo, ohi, i);
+      if ((hit >> c) & 1u) {
+        if (sp >= cap) return false;
+        stack[sp * stride] = entry(c);
+        ++sp;
+      }
+    }
+  }
+  return true;
+}
+
+// Best closest hit found so far.
+struct Best {
+  uint32_t leaf = 0xFFFFFFFFu;
+  int lane = -1;
+  float u = 0.f, v = 0.f;
+};
+
+// One leaf visit. Closest rays update tmax / best; any-hit rays return true
+// on a hit. With COUNT false, any-hit rays stop at the first hit triangle
+// (the leaf's result is the same); with COUNT true all triangles are tested
+// like the reference.
+template <int PROFILE, int KIND, bool COUNT>
+BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax, Best& best,
+                           Counters& ctr) {
+  const uint32_t leaf = e & kLeafIndexMask;
+  const int cnt = (int)((e >> kLeafCountShift) & 15u) + 1;
+  const int gang = sc.gang;
+  const int stride = ((cnt - 1) / gang + 1) * gang;
+  const float* blk = sc.leaves + (size_t)leaf * 9 * sc.leaf_memory;
+  if (COUNT) {
+    ctr.leaf_visits++;
+    ctr.tri_tests += (uint32_t)cnt;
+  }
+  bool any = false;
+  // Fast profile closest hit: per-gang-lane minima of triIntersect{L}.
+  float leaf_best = 1000000.0f;
+  int winner = -1;
+  uint32_t lanes_at_best = 0;
+  float wu = 0.f, wv = 0.f;
+
+  // Row offsets: instrumented rays read the permuted axes directly.
+  int ax0 = 0, ax1 = 1, ax2 = 2;
+  if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) { ax0 = r.kx; ax1 = r.ky; ax2 = r.code; }
+  for (int g = 0; g < cnt; g += 4) {
+    float4 c[3][3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      c[v][0] = ldg4(blk + (v * 3 + ax0) * stride + g);
+      c[v][1] = ldg4(blk + (v * 3 + ax1) * stride + g);
+      c[v][2] = ldg4(blk + (v * 3 + ax2) * stride + g);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = g + k;
+      if (i >= cnt) break;
+      float p[3][3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[v][a] = f4get(c[v][a], k);
+      float t, b1, b2;
+      bool h;
+      if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED)
+        h = watertight(p, r, tmax, t, b1, b2);
+      else
+        h = moller_trumbore(p, r, tmax, t, b1, b2);
+      if (!h) continue;
+      if (KIND == BVHGPU_ANY) {
+        if (COUNT) ctr.tri_hits++;
+        any = true;
+        if (!COUNT) return true;
+        continue;
+      }
+      if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) {
+        // Each accepted triangle overwrites the hit (triangle.cpp:243).
+        if (COUNT) ctr.tri_hits++;
+        tmax = t;
+        best.leaf = leaf;
+        best.lane = i;
+        best.u = b1;
+        best.v = b2;
+        any = true;
+      } else {
+        // triIntersect{L}: lane i % gang keeps its first minimum below its
+        // running value (initially 1e6); the result is the largest index
+        // among lanes whose minimum equals the leaf minimum
+        // (rayTracerTemplate.ispc:28-101).
+        if (COUNT) ctr.tri_hits++;
+        const uint32_t lane_bit = 1u << (i % gang);
+        if (t < leaf_best) {
+          leaf_best = t;
+          winner = i;
+          lanes_at_best = lane_bit;
+          wu = b1;
+          wv = b2;
+        } else if (winner >= 0 && t == leaf_best && !(lanes_at_best & lane_bit)) {
+          winner = i;
+          lanes_at_best |= lane_bit;
+          wu = b1;
+          wv = b2;
+        }
+      }
+    }
+  }
+  if (KIND == BVHGPU_CLOSEST && PROFILE == BVHGPU_PROFILE_FAST && winner >= 0) {
+    tmax = leaf_best;
+    best.leaf = leaf;
+    best.lane = winner;
+    best.u = wu;
+    best.v = wv;
+    any = true;
+  }
+  return any;
+}
+
+BVHGPU_DEV void record_error(int* status, int code) { atomicCAS(status, 0, code); }
+
+// Rays are 32-byte records read with two 128-bit loads (16-byte aligned buffer).
+BVHGPU_DEV bvhgpu_ray_t load_ray(const bvhgpu_ray_t* rays, uint64_t i) {
+  const float4* p = reinterpret_cast<const float4*>(rays + i);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  bvhgpu_ray_t r;
+  r.ox = a.x; r.oy = a.y; r.oz = a.z; r.tmax = a.w;
+  r.dx = b.x; r.dy = b.y; r.dz = b.z; r.pad = b.w;
+  return r;
+}
+
+template <bool COUNT>
+BVHGPU_DEV void flush_counters(const TraceArgs& a, uint64_t rid, const Counters& c) {
+  if (!COUNT || a.counters == nullptr) return;
+  uint32_t* o = a.counters + rid * BVHGPU_COUNTERS_PER_RAY;
+  o[0] = c.node_visits;
+  o[1] = c.leaf_visits;
+  o[2] = c.box_tests;
+  o[3] = c.box_hits;
+  o[4] = c.tri_tests;
+  o[5] = c.tri_hits;
+  o[6] = c.max_stack;
+  o[7] = 0;
+}
+
+template <int KIND>
+BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t rid, bool hit,
+                             float tmax, const Best& best) {
+  if (KIND == BVHGPU_ANY) {
+    a.occluded[rid] = hit ? 1 : 0;
+    return;
+  }
+  bvhgpu_hit_t h;
+  if (best.lane >= 0) {
+    h.prim = (int32_t)__ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + best.lane);
+    h.t = tmax;
+    h.u = best.u;
+    h.v = best.v;
+  } else {
+    h.prim = -1;
+    h.t = tmax;
+    h.u = 0.f;
+    h.v = 0.f;
+  }
+  reinterpret_cast<float4*>(a.hits)[rid] =
+      make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
+}
+
+// ---------------------------------------------------------------------------
+// Per-ray depth-first traversal: one thread per ray, the traversal stack in
+// shared memory (stack[slot][thread], conflict-free across a warp).
+template <int N, int PROFILE, int KIND, bool COUNT>
+__global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a) {
+  extern __shared__ uint32_t smem[];
+  const int stride = blockDim.x;
+  uint32_t* stack = smem + threadIdx.x;
+  unsigned long long* hist = nullptr;
+  const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (rid >= a.n) return;
+
+  const bvhgpu_ray_t in = load_ray(a.rays, rid);
+  if (isnan(in.ox)) {
+    Best none;
+    write_result<KIND>(sc, a, rid, false, in.tmax, none);
+    Counters c0;
+    flush_counters<COUNT>(a, rid, c0);
+    return;
+  }
+  const Ray r = make_ray<PROFILE>(in);
+  float tmax = r.tmax;
+  Best best;
+  Counters ctr;
+  bool hit = false;
+  int sp = 0;
+  stack[0] = sc.root_entry;
+  sp = 1;
+  const int cap = a.stack_cap;
+  while (sp > 0) {
+    --sp;
+    const uint32_t e = stack[sp * stride];
+    if (e & kLeafBit) {
+      if (COUNT && a.depth_hist)
+        atomicAdd(a.depth_hist + 64 + sc.leaf_depth[e & kLeafIndexMask], 1ull);
+      bool h = visit_leaf<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
+      if (h) {
+        hit = true;
+        if (KIND == BVHGPU_ANY) break;
+      }
+    } else {
+      const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
+      int depth;
+      if (!visit_node<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
+                                               depth)) {
+        record_error(sc.status, kDevErrStackOverflow);
+        hit = false;
+        best = Best();
+        break;
+      }
+      if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + depth, 1ull);
+      if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
+    }
+  }
+  (void)hist;
+  write_result<KIND>(sc, a, rid, hit, tmax, best);
+  flush_counters<COUNT>(a, rid, ctr);
+}
+
+
+// ---------------------------------------------------------------------------
+// Ray-stream traversal (FastNodeManager::intersectWideAlternative,
+// fastNodeManager.h:835-1049, and its instrumented twin compactNode.cpp:357-601).
+// One block holds a packet of blockDim.x rays. Each step, the work list holds
+// the rays whose stack top is an inner node at the front and the rays whose
+// stack top is a leaf at the back; thread t takes list entry t, so after the
+// ballot / popc compaction a warp is (but for one boundary warp) all node
+// visits or all leaf visits. Ray state, stacks and hits live in shared memory
+// because a ray moves between threads from step to step.
+struct StreamRay {
+  float o[3], d[3], inv[3];
+  float tmax;
+  float sx, sy, sz;
+  uint32_t bits;  // code | reverse << 2 | kx << 3 | ky << 5
+};
+
+BVHGPU_DEV void pack_ray(const Ray& r, StreamRay& s) {
+  for (int k = 0; k < 3; ++k) { s.o[k] = r.o[k]; s.d[k] = r.d[k]; s.inv[k] = r.inv[k]; }
+  s.tmax = r.tmax;
+  s.sx = r.sx; s.sy = r.sy; s.sz = r.sz;
+  s.bits = (uint32_t)r.code | ((uint32_t)r.reverse << 2) | ((uint32_t)r.kx << 3) |
+           ((uint32_t)r.ky << 5);
+}
+BVHGPU_DEV Ray unpack_ray(const StreamRay& s) {
+  Ray r;
+  for (int k = 0; k < 3; ++k) { r.o[k] = s.o[k]; r.d[k] = s.d[k]; r.inv[k] = s.inv[k]; }
+  r.tmax = s.tmax;
+  r.sx = s.sx; r.sy = s.sy; r.sz = s.sz;
+  r.code = (int)(s.bits & 3u);
+  r.reverse = ((s.bits >> 2) & 1u) != 0;
+  r.kx = (int)((s.bits >> 3) & 3u);
+  r.ky = (int)((s.bits >> 5) & 3u);
+  return r;
+}
+
+struct StreamShared {
+  int node_rays, leaf_rays, next_node, next_leaf;
+};
+
+// Shared-memory bytes of the stream kernel for a packet of p rays.
+inline size_t stream_smem_bytes(int p, int stack_cap, bool count) {
+  size_t b = sizeof(StreamShared);
+  b = (b + 15) / 16 * 16;
+  b += (size_t)p * sizeof(StreamRay);
+  b += (size_t)p * stack_cap * 4;        // stacks
+  b += (size_t)p * 4 * 4;                // best: leaf, lane|hit|sp, u, v
+  b += (size_t)p * 2 * 2;                // two work lists
+  if (count) b += (size_t)p * 8 * 4;     // counters
+  return b;
+}
+
+template <int N, int PROFILE, int KIND, bool COUNT>
+__global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArgs a) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  const int P = blockDim.x;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  StreamShared* ctl = reinterpret_cast<StreamShared*>(smem_raw);
+  uint8_t* base = smem_raw + 16;
+  StreamRay* rays = reinterpret_cast<StreamRay*>(base);
+  base += (size_t)P * sizeof(StreamRay);
+  uint32_t* stacks = reinterpret_cast<uint32_t*>(base);  // stacks[slot * P + ray]
+  base += (size_t)P * a.stack_cap * 4;
+  uint32_t* best_leaf = reinterpret_cast<uint32_t*>(base);
+  int32_t* best_misc = reinterpret_cast<int32_t*>(best_leaf + P);  // lane | sp << 8 | hit << 31
+  float* best_u = reinterpret_cast<float*>(best_misc + P);
+  float* best_v = best_u + P;
+  base += (size_t)P * 16;
+  uint16_t* work0 = reinterpret_cast<uint16_t*>(base);  // list c at work0 + c * P
+  base += (size_t)P * 4;
+  uint32_t* ctrs = reinterpret_cast<uint32_t*>(base);  // [8][P]
+
+  const uint64_t first = (uint64_t)blockIdx.x * P;
+  const uint64_t rid = first + tid;
+  const int cap = a.stack_cap;
+
+  if (tid == 0) { ctl->node_rays = 0; ctl->leaf_rays = 0; ctl->next_node = 0; ctl->next_leaf = 0; }
+  __syncthreads();
+  // Set-up: active rays go to the node part of list 0 (the root entry is an
+  // inner node unless the whole tree is one leaf).
+  bool active = false;
+  if (rid < a.n) {
+    const bvhgpu_ray_t in = load_ray(a.rays, rid);
+    Ray r = make_ray<PROFILE>(in);
+    pack_ray(r, rays[tid]);
+    best_leaf[tid] = 0xFFFFFFFFu;
+    best_misc[tid] = -1 & 0xFF;
+    best_u[tid] = 0.f;
+    best_v[tid] = 0.f;
+    if (COUNT) for (int k = 0; k < 8; ++k) ctrs[k * P + tid] = 0;
+    active = !isnan(in.ox);
+    if (active) {
+      stacks[tid] = sc.root_entry;
+      best_misc[tid] = 0xFF | (1 << 8);  // lane -1, sp 1
+    }
+  }
+  const bool root_leaf = (sc.root_entry & kLeafBit) != 0;
+  {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, active);
+    int pos = 0;
+    if (m) {
+      int b = 0;
+      if (lane == __ffs(m) - 1) {
+        if (root_leaf) b = atomicAdd(&ctl->leaf_rays, __popc(m));
+        else b = atomicAdd(&ctl->node_rays, __popc(m));
+      }
+      b = __shfl_sync(0xFFFFFFFFu, b, __ffs(m) - 1);
+      pos = b + __popc(m & ((1u << lane) - 1u));
+    }
+    if (active) {
+      if (root_leaf) work0[P - 1 - pos] = (uint16_t)tid;
+      else work0[pos] = (uint16_t)tid;
+    }
+  }
+  __syncthreads();
+
+  int cur = 0;
+  while (true) {
+    const int node_rays = ctl->node_rays, leaf_rays = ctl->leaf_rays;
+    if (node_rays == 0 && leaf_rays == 0) break;
+    int ray = -1;
+    bool is_node = false;
+    const uint16_t* wcur = work0 + cur * P;
+    if (tid < node_rays) { ray = wcur[tid]; is_node = true; }
+    else if (tid >= P - leaf_rays) { ray = wcur[tid]; }
+    bool want_node = false, want_leaf = false;
+    if (ray >= 0) {
+      Ray r = unpack_ray(rays[ray]);
+      float tmax = r.tmax;
+      int32_t misc = best_misc[ray];
+      int sp = (misc >> 8) & 0x7FFF;
+      bool done = false;
+      Counters ctr;
+      --sp;
+      const uint32_t e = stacks[sp * P + ray];
+      if (is_node) {
+        const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
+        int depth;
+        if (!visit_node<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stacks + ray, P, sp, cap, ctr,
+                                                 depth)) {
+          record_error(sc.status, kDevErrStackOverflow);
+          best_leaf[ray] = 0xFFFFFFFFu;
+          misc = 0xFF;
+          done = true;
+          sp = 0;
+        }
+        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + depth, 1ull);
+      } else {
+        if (COUNT && a.depth_hist)
+          atomicAdd(a.depth_hist + 64 + sc.leaf_depth[e & kLeafIndexMask], 1ull);
+        Best best;
+        best.leaf = best_leaf[ray];
+        best.lane = (int)(int8_t)(misc & 0xFF);
+        best.u = best_u[ray];
+        best.v = best_v[ray];
+        bool h = visit_leaf<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
+        if (h) {
+          misc |= (int32_t)0x80000000;
+          if (KIND == BVHGPU_ANY) done = true;
+          else {
+            rays[ray].tmax = tmax;
+            best_leaf[ray] = best.leaf;
+            misc = (misc & ~0xFF) | (best.lane & 0xFF);
+            best_u[ray] = best.u;
+            best_v[ray] = best.v;
+          }
+        }
+      }
+      if (COUNT) {
+        ctrs[0 * P + ray] += ctr.node_visits;
+        ctrs[1 * P + ray] += ctr.leaf_visits;
+        ctrs[2 * P + ray] += ctr.box_tests;
+        ctrs[3 * P + ray] += ctr.box_hits;
+        ctrs[4 * P + ray] += ctr.tri_tests;
+        ctrs[5 * P + ray] += ctr.tri_hits;
+        ctrs[6 * P + ray] = max(ctrs[6 * P + ray], (uint32_t)sp);
+      }
+      if (!done && sp > 0) {
+        const uint32_t top = stacks[(sp - 1) * P + ray];
+        if (top & kLeafBit) want_leaf = true;
+        else want_node = true;
+      }
+      if (done) sp = 0;
+      misc = (misc & ~(0x7FFF << 8)) | (sp << 8);
+      best_misc[ray] = misc;
+    }
+    // Compact into the next list: inner-node rays from the front, leaf rays
+    // from the back.
+    const int nxt = cur ^ 1;
+    {
+      const unsigned mn = __ballot_sync(0xFFFFFFFFu, want_node);
+      const unsigned ml = __ballot_sync(0xFFFFFFFFu, want_leaf);
+      int bn = 0, bl = 0;
+      if (mn && lane == __ffs(mn) - 1) bn = atomicAdd(&ctl->next_node, __popc(mn));
+      if (ml && lane == __ffs(ml) - 1) bl = atomicAdd(&ctl->next_leaf, __popc(ml));
+      if (mn) bn = __shfl_sync(0xFFFFFFFFu, bn, __ffs(mn) - 1);
+      if (ml) bl = __shfl_sync(0xFFFFFFFFu, bl, __ffs(ml) - 1);
+      const unsigned below = (1u << lane) - 1u;
+      uint16_t* wnxt = work0 + nxt * P;
+      if (want_node) wnxt[bn + __popc(mn & below)] = (uint16_t)ray;
+      if (want_leaf) wnxt[P - 1 - (bl + __popc(ml & below))] = (uint16_t)ray;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      ctl->node_rays = ctl->next_node;
+      ctl->leaf_rays = ctl->next_leaf;
+      ctl->next_node = 0;
+      ctl->next_leaf = 0;
+    }
+    cur = nxt;
+    __syncthreads();
+  }
+
+  // Results of this thread's own ray slot.
+  if (rid < a.n) {
+    const int32_t misc = best_misc[tid];
+    const bool hit = (misc & (int32_t)0x80000000) != 0;
+    Best best;
+    best.leaf = best_leaf[tid];
+    best.lane = (int)(int8_t)(misc & 0xFF);
+    best.u = best_u[tid];
+    best.v = best_v[tid];
+    write_result<KIND>(sc, a, rid, hit, rays[tid].tmax, best);
+    if (COUNT && a.counters) {
+      uint32_t* o = a.counters + rid * BVHGPU_COUNTERS_PER_RAY;
+      for (int k = 0; k < 7; ++k) o[k] = ctrs[k * P + tid];
+      o[7] = 0;
+    }
+  }
+}
+
+}  // namespace dev
+}  // namespace bvhgpu

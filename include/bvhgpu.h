@@ -1,0 +1,201 @@
+/*
+ * bvhgpu — GB300 (sm_103a) traversal of N-wide BVHs with L-wide leaves.
+ *
+ * C ABI of the drop-in boundary. All entry points return a status int
+ * (BVHGPU_OK == 0); no C++ exception crosses this boundary. Buffers are
+ * owned by the caller unless a function says otherwise. Calls that take a
+ * `stream` are stream-ordered and do not synchronise unless noted; distinct
+ * streams may call concurrently into distinct scenes.
+ *
+ * What each entry point replaces in the reference (Hengoo/BVHRaytracer):
+ *   bvhgpu_bvh_build          Bvh::Bvh + Bvh::recursiveBvh + Bvh::bvhAnalysis
+ *                             (src/accelerationStructure/bvh.cpp:28-40,
+ *                              src/accelerationStructure/aabb.cpp:71-206,
+ *                              src/rayTracer.cpp:604-623)
+ *   bvhgpu_sah_factor         RayTracer::loadSahFactor (src/rayTracer.cpp:880-925)
+ *   bvhgpu_bvh_export_compact CompactNodeManager<CompactNodeV3> constructor
+ *                             (src/accelerationStructure/compactNode.cpp:11-116)
+ *   bvhgpu_bvh_export_fast    FastNodeManager constructor
+ *                             (src/accelerationStructure/fastNodeManager.h:1495-1688)
+ *   bvhgpu_scene_create       the device-resident copy of the flat BVH (no
+ *                             reference counterpart: the reference is CPU-only)
+ *   bvhgpu_trace              FastNodeManager::intersect / intersectSecondary /
+ *                             intersectWideAlternative / intersectSecondaryWideAlternative
+ *                             (fastNodeManager.h:1328-1493, 835-1230) and the
+ *                             instrumented CompactNodeManager::intersectImmediately /
+ *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
+ *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
+ *   bvhgpu_intersect_fastrays FastNodeManager::intersectWideAlternative on FastRay
+ *                             records (fastNodeManager.h:835-1049; FastRay: src/fastRay.h:14-29)
+ *   bvhgpu_intersect_secondary_fastrays
+ *                             FastNodeManager::intersectSecondaryWideAlternative
+ *                             (fastNodeManager.h:1051-1230)
+ *   bvhgpu_surface_normal_position
+ *                             FastNodeManager::getSurfaceNormalPosition
+ *                             (fastNodeManager.h:1700-1713)
+ */
+#ifndef BVHGPU_H
+#define BVHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define BVHGPU_OK 0
+#define BVHGPU_ERR_BAD_ARG 1        /* null pointer, size or option out of range */
+#define BVHGPU_ERR_OOM 2            /* device or host allocation failed */
+#define BVHGPU_ERR_CUDA 3           /* a CUDA runtime call failed */
+#define BVHGPU_ERR_STACK_OVERFLOW 4 /* a ray needed more stack than the scene holds */
+#define BVHGPU_ERR_TIMEOUT 5        /* a bounded device wait gave up */
+#define BVHGPU_ERR_UNSUPPORTED 6    /* option combination not built */
+#define BVHGPU_ERR_NO_DEVICE 7      /* no CUDA device visible */
+
+/* ---- handles ----------------------------------------------------------- */
+typedef struct bvhgpu_bvh* bvhgpu_bvh_t;     /* host BVH (builder output) */
+typedef struct bvhgpu_scene* bvhgpu_scene_t; /* device-resident scene */
+
+/* ---- host BVH build ---------------------------------------------------- */
+/* Knobs of the reference's config.txt (minBranch..maxLeafSize, sortEachSplit,
+ * leafSplitOption) and its per-(N, L) SAH node factor. */
+typedef struct {
+  int32_t branching;         /* N, 2..16 */
+  int32_t leaf_size;         /* L, 1..16 */
+  int32_t sort_each_split;   /* must be 1 (per-axis child orders) */
+  int32_t leaf_split_option; /* 0, 1 or 2 */
+  float sah_factor;          /* sahNodeFactor; see bvhgpu_sah_factor */
+  int32_t drop_zero_area;    /* 1: skip zero-area triangles like the scene loader */
+} bvhgpu_build_params_t;
+
+typedef struct {
+  uint64_t n_input_tris; /* triangles passed in */
+  uint64_t n_tris;       /* triangles kept (zero-area ones dropped) */
+  uint64_t n_nodes;      /* all nodes, leaves included (reference numbering) */
+  uint64_t n_inner;
+  uint64_t n_leaves;
+  int32_t depth;         /* bvhDepth: deepest leaf depth + 1 */
+  int32_t max_stack;     /* worst-case depth-first stack height */
+  int32_t branching;
+  int32_t leaf_size;
+  float root_lo[3];
+  float root_hi[3];
+} bvhgpu_bvh_info_t;
+
+/* tris: n_tris x 9 floats (p0, p1, p2), world space, in scene-loader order.
+ * Primitive ids reported by traces are indices into this array. */
+int bvhgpu_bvh_build(const float* tris, uint64_t n_tris, const bvhgpu_build_params_t* params,
+                     bvhgpu_bvh_t* out);
+int bvhgpu_bvh_info(bvhgpu_bvh_t bvh, bvhgpu_bvh_info_t* info);
+int bvhgpu_bvh_free(bvhgpu_bvh_t bvh);
+
+/* sahNodeFactor for (N, L) from the reference's SSE table, with N and L
+ * rounded up to the gang size; gang 8 returns 1 like the reference. */
+int bvhgpu_sah_factor(int32_t branching, int32_t leaf_size, int32_t gang, float* out);
+
+/* CompactNodeV3 view, reference node numbering (root = 0, customTreeOrder).
+ * Arrays sized by bvhgpu_bvh_info: n_nodes entries each (lo3/hi3: 3 per node,
+ * order48: 48 int8 per node, order[axis][i] at [axis*16+i]); prim_ids and
+ * prim_tri9 are sized n_tris (prim_tri9: 9 floats each) in sorted order. */
+int bvhgpu_bvh_export_compact(bvhgpu_bvh_t bvh, float* lo3, float* hi3, uint32_t* child_begin,
+                              uint32_t* child_count, uint32_t* prim_begin, uint32_t* prim_count,
+                              int8_t* order48, uint8_t* depth, uint32_t* prim_ids,
+                              float* prim_tri9);
+
+/* FastNode<node_memory> view and trianglePoints of FastNodeManager with the
+ * given gang size (4 for SSE4, 8 for AVX2) and leaf memory. */
+int bvhgpu_bvh_fast_sizes(bvhgpu_bvh_t bvh, int32_t gang, int32_t node_memory,
+                          int32_t leaf_memory, uint64_t* n_nodes, uint64_t* n_tri_floats);
+int bvhgpu_bvh_export_fast(bvhgpu_bvh_t bvh, int32_t gang, int32_t node_memory,
+                           int32_t leaf_memory, float* bounds /* n_nodes*6*node_memory */,
+                           uint32_t* begin /* childIdBegin or primIdBegin */,
+                           int8_t* order /* n_nodes*3*node_memory */,
+                           uint32_t* child_type /* bit j: child j is an inner node */,
+                           float* tri_points);
+
+/* ---- device scene ------------------------------------------------------ */
+#define BVHGPU_NODES_FP32 0 /* float child boxes */
+#define BVHGPU_NODES_Q8 1   /* 8-bit child boxes relative to the parent box */
+
+typedef struct {
+  int32_t gang;        /* 4 (SSE4 gang) or 8: leaf padding and fast-profile tie rule */
+  int32_t leaf_memory; /* 0: L rounded up to the gang */
+  int32_t node_format; /* BVHGPU_NODES_FP32 or BVHGPU_NODES_Q8 */
+  int32_t top_levels;  /* inner levels laid out first, staged in shared memory (0..4) */
+  int32_t device;      /* CUDA device ordinal */
+} bvhgpu_scene_params_t;
+
+int bvhgpu_scene_create(bvhgpu_bvh_t bvh, const bvhgpu_scene_params_t* params,
+                        bvhgpu_scene_t* out);
+int bvhgpu_scene_free(bvhgpu_scene_t scene);
+/* Device bytes of the node array and of the leaf array. */
+int bvhgpu_scene_bytes(bvhgpu_scene_t scene, uint64_t* node_bytes, uint64_t* leaf_bytes,
+                       uint64_t* node_record_bytes, uint64_t* leaf_record_bytes);
+
+/* ---- tracing ----------------------------------------------------------- */
+typedef struct {
+  float ox, oy, oz, tmax; /* origin and ray length limit */
+  float dx, dy, dz, pad;  /* direction (see profiles) */
+} bvhgpu_ray_t;           /* 32 bytes */
+
+typedef struct {
+  int32_t prim; /* input triangle index, -1 on miss */
+  float t;      /* hit distance (profile units) */
+  float u, v;   /* barycentric weights of p1 and p2 */
+} bvhgpu_hit_t; /* 16 bytes */
+
+#define BVHGPU_CLOSEST 0 /* closest hit (primary rays) */
+#define BVHGPU_ANY 1     /* any hit (shadow / ambient-occlusion rays) */
+
+#define BVHGPU_PER_RAY 0 /* depth-first traversal, one thread per ray */
+#define BVHGPU_STREAM 1  /* ray-stream traversal over node / leaf work lists */
+
+/* Instrumented profile: CompactNodeManager + Ray + Triangle::intersect
+ * semantics (direction normalised, watertight leaf test with the per-triangle
+ * box pre-test, child order by the major axis for every ray).
+ * Fast profile: FastNodeManager + FastRay + ISPC semantics (direction used as
+ * given, Moller-Trumbore leaf test with gang-lane tie rule, index child order
+ * for any-hit rays). */
+#define BVHGPU_PROFILE_INSTRUMENTED 0
+#define BVHGPU_PROFILE_FAST 1
+
+typedef struct {
+  int32_t kind;      /* BVHGPU_CLOSEST / BVHGPU_ANY */
+  int32_t scheme;    /* BVHGPU_PER_RAY / BVHGPU_STREAM */
+  int32_t profile;   /* BVHGPU_PROFILE_* */
+  int32_t workgroup; /* stream scheme: packet = workgroup^2 rays (8, 16, 32); 0 = 16 */
+  int32_t block;     /* per-ray scheme: threads per block (0 = default) */
+} bvhgpu_trace_opts_t;
+
+/* Counters per ray when `counters` is non-null (8 uint32 per ray):
+ * node visits, leaf visits, box tests, box hits, triangle tests,
+ * triangle hits, deepest stack, reserved. `depth_hist` (nullable):
+ * 2 x 64 uint64, node visits then leaf visits per tree depth, accumulated. */
+#define BVHGPU_COUNTERS_PER_RAY 8
+
+/* Device pointers. Closest: writes hits[n]. Any: writes occluded[n] (0/1).
+ * Rays whose origin x is NaN are skipped (miss / not occluded), like the
+ * reference's inactive secondary rays. */
+int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
+                 const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                 uint32_t* counters, uint64_t* depth_hist, void* stream);
+
+/* Host pointers: copies rays in, traces, copies results out, synchronises
+ * `stream`. Device staging buffers are owned by the scene and reused. */
+int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
+                      const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                      void* stream);
+
+/* Synchronises `stream` and returns the first device-side error recorded by
+ * this scene's kernels since the last call (and clears it). */
+int bvhgpu_scene_status(bvhgpu_scene_t scene, void* stream);
+
+/* Message for the last non-zero status returned on this thread. */
+const char* bvhgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BVHGPU_H */

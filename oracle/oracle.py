@@ -1,0 +1,128 @@
+"""ctypes wrapper of the CPU oracle (oracle/bvh_oracle.c) — TEST INFRASTRUCTURE.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
+import this module. Parity status: unpinned at the reference level (the
+reference ships no golden vectors for the path and cannot be built here);
+see the header of bvh_oracle.c.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from .build_oracle import build
+
+_P = C.c_void_p
+
+
+class _Compact(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint64)] + [(k, _P) for k in (
+        "lo3", "hi3", "child_begin", "child_count", "prim_begin", "prim_count", "order48",
+        "depth", "prim_ids", "prim_tri9")]
+
+
+class _Fast(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint64), ("gang", C.c_int32), ("node_memory", C.c_int32),
+                ("leaf_memory", C.c_int32)] + [(k, _P) for k in (
+                    "bounds", "begin", "order", "child_type", "tri_points")]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib() -> C.CDLL:
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = C.CDLL(str(build()))
+            L.oracle_trace_instrumented.restype = C.c_int
+            L.oracle_trace_instrumented.argtypes = [C.POINTER(_Compact), _P, C.c_uint64, C.c_int,
+                                                    _P, _P, _P, _P]
+            L.oracle_trace_instrumented_stream.restype = C.c_int
+            L.oracle_trace_instrumented_stream.argtypes = [C.POINTER(_Compact), _P, C.c_uint64,
+                                                           C.c_int, C.c_int, _P, _P, _P, _P]
+            L.oracle_trace_fast.restype = C.c_int
+            L.oracle_trace_fast.argtypes = [C.POINTER(_Fast), C.POINTER(_Compact), _P, C.c_uint64,
+                                            C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P]
+            L.oracle_fp64_pairs.restype = None
+            L.oracle_fp64_pairs.argtypes = [_P, _P, C.c_uint64, C.c_int, _P]
+            _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class CompactView:
+    """Keeps the exported CompactNodeV3 arrays alive next to the C view."""
+
+    def __init__(self, arrays: dict):
+        self.a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        self.c = _Compact(self.a["child_count"].shape[0], *[_p(self.a[k]) for k in (
+            "lo3", "hi3", "child_begin", "child_count", "prim_begin", "prim_count", "order48",
+            "depth", "prim_ids", "prim_tri9")])
+
+
+class FastView:
+    def __init__(self, arrays: dict):
+        self.a = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v)
+                  for k, v in arrays.items()}
+        self.c = _Fast(self.a["begin"].shape[0], self.a["gang"], self.a["node_memory"],
+                       self.a["leaf_memory"], *[_p(self.a[k]) for k in (
+                           "bounds", "begin", "order", "child_type", "tri_points")])
+
+
+def trace_instrumented(view: CompactView, rays: np.ndarray, shadow: bool, packet: int = 0,
+                       counters: bool = True) -> dict:
+    """CompactNodeManager::intersectImmediately (packet == 0) or
+    intersectWideAlternative over packets of ``packet`` rays."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = rays.shape[0]
+    hits = None if shadow else np.zeros((n, 4), np.float32)
+    occ = np.zeros(n, np.uint8) if shadow else None
+    ctr = np.zeros((n, 8), np.uint32) if counters else None
+    hist = np.zeros((2, 64), np.uint64) if counters else None
+    if packet:
+        rc = lib().oracle_trace_instrumented_stream(C.byref(view.c), _p(rays), n, int(shadow),
+                                                     packet, _p(hits), _p(occ), _p(ctr), _p(hist))
+    else:
+        rc = lib().oracle_trace_instrumented(C.byref(view.c), _p(rays), n, int(shadow), _p(hits),
+                                             _p(occ), _p(ctr), _p(hist))
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist}
+
+
+def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: bool,
+               packet: int = 0, threads: int = 0, counters: bool = True,
+               outputs: bool = True) -> dict:
+    """FastNodeManager::intersect / intersectSecondary (packet == 0) or the
+    WideAlternative stream versions, with ISPC gang-lane semantics."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = rays.shape[0]
+    hits = np.zeros((n, 4), np.float32) if (outputs and not any_hit) else None
+    occ = np.zeros(n, np.uint8) if (outputs and any_hit) else None
+    li = np.zeros(n, np.int32) if (outputs and not any_hit) else None
+    ti = np.zeros(n, np.int8) if (outputs and not any_hit) else None
+    ctr = np.zeros((n, 8), np.uint32) if counters else None
+    hist = np.zeros((2, 64), np.uint64) if counters else None
+    rc = lib().oracle_trace_fast(C.byref(fview.c), C.byref(cview.c), _p(rays), n, int(any_hit),
+                                 packet, threads, _p(hits), _p(occ), _p(li), _p(ti), _p(ctr),
+                                 _p(hist))
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return {"hits": hits, "occluded": occ, "leaf_index": li, "tri_index": ti, "counters": ctr,
+            "depth_hist": hist}
+
+
+def fp64_pairs(rays: np.ndarray, tri9: np.ndarray, normalise: bool) -> np.ndarray:
+    """Double-precision (t, b1, b2) of each (ray, triangle) pair."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    tri9 = np.ascontiguousarray(tri9, np.float32)
+    out = np.zeros((rays.shape[0], 3), np.float64)
+    lib().oracle_fp64_pairs(_p(rays), _p(tri9), rays.shape[0], int(normalise), _p(out))
+    return out

@@ -1,0 +1,127 @@
+"""C ABI: the library loads, exports every declared entry point, and rejects
+bad arguments with status codes (no GPU needed)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import bvhraytracer_gb300 as pkg
+from bvhraytracer_gb300 import _native as N
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "bvhgpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\s*\*)\s+(bvhgpu_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert len(names) >= 14
+    assert "bvhgpu_trace" in names and "bvhgpu_bvh_build" in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(N.LIB_PATH))
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} declared in bvhgpu.h but not exported"
+
+
+def test_python_binding_covers_header():
+    assert set(declared_functions()) == set(N.EXPORTED)
+
+
+def test_status_codes_match_header():
+    text = HEADER.read_text()
+    codes = dict(re.findall(r"#define (BVHGPU_(?:OK|ERR_\w+))\s+(\d+)", text))
+    assert int(codes["BVHGPU_OK"]) == N.OK
+    assert int(codes["BVHGPU_ERR_BAD_ARG"]) == N.ERR_BAD_ARG
+    assert int(codes["BVHGPU_ERR_STACK_OVERFLOW"]) == N.ERR_STACK_OVERFLOW
+    assert int(codes["BVHGPU_ERR_UNSUPPORTED"]) == N.ERR_UNSUPPORTED
+    assert int(codes["BVHGPU_ERR_NO_DEVICE"]) == N.ERR_NO_DEVICE
+
+
+def test_struct_sizes_match_header_layout():
+    assert C.sizeof(N.BuildParams) == 24
+    assert C.sizeof(N.SceneParams) == 20
+    assert C.sizeof(N.TraceOpts) == 20
+
+
+def _tri():
+    return np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+
+
+@pytest.mark.parametrize("n,l", [(1, 4), (17, 4), (4, 0), (4, 17)])
+def test_build_rejects_bad_sizes(n, l):
+    with pytest.raises(pkg.BvhgpuError) as e:
+        pkg.Bvh(_tri(), n, l, sah=1.0)
+    assert e.value.code == N.ERR_BAD_ARG
+
+
+def test_build_rejects_null_and_empty():
+    lib = N.lib()
+    p = N.BuildParams(4, 4, 1, 1, 1.0, 1)
+    h = C.c_void_p()
+    assert lib.bvhgpu_bvh_build(None, 1, C.byref(p), C.byref(h)) == N.ERR_BAD_ARG
+    t = _tri()
+    assert lib.bvhgpu_bvh_build(t.ctypes.data, 0, C.byref(p), C.byref(h)) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_bvh_build(t.ctypes.data, 1, None, C.byref(h)) == N.ERR_BAD_ARG
+    assert b"null" in lib.bvhgpu_last_error()
+
+
+def test_build_rejects_non_finite_and_degenerate_only():
+    t = _tri().copy()
+    t[0, 4] = np.nan
+    with pytest.raises(pkg.BvhgpuError):
+        pkg.Bvh(t, 4, 4)
+    deg = np.zeros((3, 9), np.float32)  # all zero-area
+    with pytest.raises(pkg.BvhgpuError):
+        pkg.Bvh(deg, 4, 4)
+
+
+def test_build_rejects_unsorted_splits():
+    with pytest.raises(pkg.BvhgpuError) as e:
+        pkg.Bvh(_tri(), 4, 4, sort_each_split=False)
+    assert e.value.code == N.ERR_UNSUPPORTED
+
+
+def test_trace_rejects_null_scene_and_options():
+    lib = N.lib()
+    o = N.TraceOpts(0, 0, 0, 16, 128)
+    assert lib.bvhgpu_trace(None, None, 1, C.byref(o), None, None, None, None, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_trace_host(None, None, 1, C.byref(o), None, None, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_scene_status(None, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_scene_free(None) == N.OK
+
+
+def test_scene_create_without_device_reports_no_device():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    b = pkg.Bvh(_tri(), 4, 4)
+    with pytest.raises(pkg.BvhgpuError) as e:
+        pkg.Scene(b)
+    assert e.value.code == N.ERR_NO_DEVICE
+
+
+def _stof(text: str) -> float:
+    """Decimal text rounded straight to the nearest float32 (std::stof)."""
+    from fractions import Fraction
+    x = Fraction(text)
+    c = np.float32(float(text))
+    cands = [np.nextafter(c, np.float32(-1)), c, np.nextafter(c, np.float32(2))]
+    return float(min(cands, key=lambda v: abs(Fraction(float(v)) - x)))
+
+
+def test_sah_factor_table():
+    # sahFactorConfigSse.txt rows; N and L rounded up to the gang of 4.
+    assert pkg.sah_factor(4, 4) == _stof("0.9790158394920848")
+    assert pkg.sah_factor(8, 8) == _stof("0.8089449478051558")
+    assert pkg.sah_factor(16, 16) == _stof("0.7655054621988963")
+    assert pkg.sah_factor(12, 4) == _stof("1.5611955563121058")
+    assert pkg.sah_factor(3, 2) == pkg.sah_factor(4, 4)
+    assert pkg.sah_factor(9, 5) == pkg.sah_factor(12, 8)
+    assert pkg.sah_factor(8, 8, gang=8) == 1.0

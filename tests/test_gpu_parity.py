@@ -1,0 +1,227 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle, bit for bit
+(hit primitive, t, barycentrics, per-ray counters, per-depth histograms),
+for both traversal schemes, both profiles and every N, L in {4,8,12,16}."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import bvhraytracer_gb300 as pkg  # noqa: E402
+from bvhraytracer_gb300 import scenes as S  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests import _scenes as TS  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+LIGHT = [2.0, 3.0, 2.0]
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def check_closest(got, ref, counters=True):
+    g = got["hits"].cpu().numpy()
+    assert np.array_equal(bits(g), bits(ref["hits"])), _first_diff(g, ref["hits"])
+    if counters:
+        gc = got["counters"].cpu().numpy().astype(np.uint32)[:, :7]
+        assert np.array_equal(gc, ref["counters"][:, :7])
+        assert np.array_equal(got["depth_hist"].cpu().numpy().astype(np.uint64), ref["depth_hist"])
+
+
+def check_any(got, ref, counters=True):
+    assert np.array_equal(got["occluded"].cpu().numpy(), ref["occluded"])
+    if counters:
+        gc = got["counters"].cpu().numpy().astype(np.uint32)[:, :7]
+        assert np.array_equal(gc, ref["counters"][:, :7])
+        assert np.array_equal(got["depth_hist"].cpu().numpy().astype(np.uint64), ref["depth_hist"])
+
+
+def _first_diff(g, r):
+    d = np.nonzero(np.any(bits(g) != bits(r), axis=1))[0]
+    if d.size == 0:
+        return "equal"
+    i = d[0]
+    return f"{d.size} rays differ; first {i}: gpu {g[i].view(np.int32)[0]} {g[i][1:]} " \
+           f"oracle {r[i].view(np.int32)[0]} {r[i][1:]}"
+
+
+@pytest.fixture(scope="module")
+def terrain():
+    tris, b, cv = TS.bvh("terrain", 4, 4)
+    rays = TS.terrain_case()[1]
+    return tris, b, cv, rays, pkg.Scene(b)
+
+
+@pytest.mark.parametrize("scheme", ["per_ray", "stream"])
+def test_terrain_instrumented_primary_and_shadow(terrain, scheme):
+    tris, b, cv, rays, scene = terrain
+    ref = O.trace_instrumented(cv, rays, shadow=False)
+    got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True)
+    check_closest(got, ref)
+    prims = pkg.hit_prims(ref["hits"])
+    sh, _ = TS.secondary(tris, rays, prims, LIGHT)
+    refs = O.trace_instrumented(cv, sh, shadow=True)
+    gots = scene.trace(dev(sh), kind="any", scheme=scheme, counters=True, depth_hist=True)
+    check_any(gots, refs)
+    # the fast (counter-free) kernels give the same hits
+    check_closest(scene.trace(dev(rays), scheme=scheme), ref, counters=False)
+    check_any(scene.trace(dev(sh), kind="any", scheme=scheme), refs, counters=False)
+    scene.status()
+
+
+@pytest.mark.parametrize("scheme", ["per_ray", "stream"])
+def test_terrain_fast_profile(terrain, scheme):
+    tris, b, cv, rays, scene = terrain
+    fv = O.FastView(b.export_fast())
+    ref = O.trace_fast(fv, cv, rays, any_hit=False)
+    got = scene.trace(dev(rays), scheme=scheme, profile="fast", counters=True, depth_hist=True)
+    check_closest(got, ref)
+    prims = pkg.hit_prims(ref["hits"])
+    sh, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+    for sec in (sh, ao):
+        r = O.trace_fast(fv, cv, sec, any_hit=True)
+        g = scene.trace(dev(sec), kind="any", scheme=scheme, profile="fast", counters=True,
+                        depth_hist=True)
+        check_any(g, r)
+
+
+@pytest.mark.parametrize("n", [4, 8, 12, 16])
+@pytest.mark.parametrize("l", [4, 8, 12, 16])
+def test_sweep_all_widths(n, l):
+    tris, b, cv = TS.bvh("clutter120", n, l)
+    rays = TS.clutter_rays(tris, res=(64, 48))
+    scene = pkg.Scene(b)
+    fv = O.FastView(b.export_fast())
+    for profile in ("instrumented", "fast"):
+        if profile == "instrumented":
+            ref = O.trace_instrumented(cv, rays, shadow=False)
+        else:
+            ref = O.trace_fast(fv, cv, rays, any_hit=False)
+        prims = pkg.hit_prims(ref["hits"])
+        _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+        if profile == "instrumented":
+            refa = O.trace_instrumented(cv, ao, shadow=True)
+        else:
+            refa = O.trace_fast(fv, cv, ao, any_hit=True)
+        for scheme in ("per_ray", "stream"):
+            got = scene.trace(dev(rays), scheme=scheme, profile=profile, counters=True,
+                              depth_hist=True)
+            check_closest(got, ref)
+            g = scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile, counters=True,
+                            depth_hist=True)
+            check_any(g, refa)
+            check_closest(scene.trace(dev(rays), scheme=scheme, profile=profile), ref, False)
+            check_any(scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile), refa, False)
+
+
+@pytest.mark.parametrize("gang,leaf_memory", [(8, 0), (4, 16), (8, 16)])
+def test_gang_and_leaf_memory(gang, leaf_memory):
+    tris, b, cv = TS.bvh("clutter120", 8, 4)
+    rays = TS.clutter_rays(tris, res=(64, 48))
+    scene = pkg.Scene(b, gang=gang, leaf_memory=leaf_memory)
+    fv = O.FastView(b.export_fast(gang=gang, leaf_memory=leaf_memory))
+    ref = O.trace_fast(fv, cv, rays, any_hit=False)
+    for scheme in ("per_ray", "stream"):
+        check_closest(scene.trace(dev(rays), scheme=scheme, profile="fast", counters=True,
+                                  depth_hist=True), ref)
+    ref = O.trace_instrumented(cv, rays, shadow=False)
+    check_closest(scene.trace(dev(rays), counters=True, depth_hist=True), ref)
+
+
+@pytest.mark.parametrize("top_levels", [1, 2, 3])
+def test_top_levels_layout(top_levels):
+    tris, b, cv = TS.bvh("clutter120", 4, 4)
+    rays = TS.clutter_rays(tris, res=(64, 48))
+    ref = O.trace_instrumented(cv, rays, shadow=False)
+    scene = pkg.Scene(b, top_levels=top_levels)
+    for scheme in ("per_ray", "stream"):
+        check_closest(scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True), ref)
+
+
+def test_edge_cases():
+    # single triangle: the root is a leaf
+    t1 = np.array([[0, 0, 5, 1, 0, 5, 0, 1, 5]], np.float32)
+    b = pkg.Bvh(t1, 4, 4)
+    cv = O.CompactView(b.export_compact())
+    scene = pkg.Scene(b)
+    rays = np.array([[0.25, 0.25, 0, 222222, 0, 0, 1, 0],     # hit, zero x/y direction
+                     [0.75, 0.75, 0, 222222, 0, 0, 1, 0],     # miss
+                     [np.nan, 0, 0, 222222, 0, 0, 1, 0],      # inactive
+                     [0.25, 0.25, 0, 4.0, 0, 0, 1, 0],        # tmax too short
+                     [0.25, 0.25, 10, 222222, 0, 0, -3, 0]],  # from behind, long direction
+                    np.float32)
+    for scheme in ("per_ray", "stream"):
+        got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True)
+        ref = O.trace_instrumented(cv, rays, shadow=False)
+        check_closest(got, ref)
+        assert pkg.hit_prims(got["hits"].cpu().numpy()).tolist() == [0, -1, -1, -1, 0]
+        occ = scene.trace(dev(rays), kind="any", scheme=scheme)["occluded"].cpu().numpy()
+        assert occ.tolist() == [1, 0, 0, 0, 1]
+    # empty batch
+    e = scene.trace(dev(np.zeros((0, 8), np.float32)))
+    assert e["hits"].shape == (0, 4)
+
+
+@pytest.mark.parametrize("n", [1, 31, 127, 129, 255, 257, 1000])
+def test_ragged_ray_counts(n, terrain):
+    tris, b, cv, rays, scene = terrain
+    r = rays[40000:40000 + n]
+    ref = O.trace_instrumented(cv, r, shadow=False)
+    for scheme in ("per_ray", "stream"):
+        check_closest(scene.trace(dev(r), scheme=scheme, counters=True, depth_hist=True), ref)
+
+
+def test_host_entry_point_matches_device(terrain):
+    tris, b, cv, rays, scene = terrain
+    ref = O.trace_instrumented(cv, rays, shadow=False)
+    out = scene.trace_host(rays)
+    assert np.array_equal(bits(out), bits(ref["hits"]))
+    prims = pkg.hit_prims(ref["hits"])
+    sh, _ = TS.secondary(tris, rays, prims, LIGHT)
+    occ = scene.trace_host(sh, kind="any", scheme="stream")
+    assert np.array_equal(occ, O.trace_instrumented(cv, sh, shadow=True)["occluded"])
+
+
+def test_wrappers_mirror_reference_names(terrain):
+    tris, b, cv, rays, scene = terrain
+    fm = pkg.FastNodeManager(b)
+    fv = O.FastView(b.export_fast())
+    ref = O.trace_fast(fv, cv, rays, any_hit=False)
+    for fn in (fm.intersect, fm.intersect_wide_alternative):
+        assert np.array_equal(bits(fn(dev(rays)).cpu().numpy()), bits(ref["hits"]))
+    cm = pkg.CompactNodeManager(b)
+    refi = O.trace_instrumented(cv, rays, shadow=False)
+    for fn in (cm.intersect_immediately, cm.intersect_wide_alternative):
+        check_closest(fn(dev(rays)), refi)
+
+
+def test_full_size_clutter_properties():
+    """1M-triangle clutter, N8L8, 1920x1080 primary rays: per-ray and stream
+    kernels agree bit for bit on every ray; a random sample agrees with the
+    oracle; any-hit == (closest hit within tmax) for the AO rays."""
+    tris = TS.clutter_tris(4000, 1)
+    b = pkg.Bvh(tris, 8, 8)
+    scene = pkg.Scene(b)
+    rays = S.clutter_camera(4000, 1920, 1080)
+    d = dev(rays)
+    a = scene.trace(d)["hits"]
+    s = scene.trace(d, scheme="stream")["hits"]
+    assert torch.equal(a.view(torch.int32), s.view(torch.int32))
+    cv = O.CompactView(b.export_compact())
+    idx = np.random.default_rng(0).choice(rays.shape[0], 20000, replace=False)
+    ref = O.trace_instrumented(cv, rays[idx], shadow=False)
+    assert np.array_equal(bits(a.cpu().numpy()[idx]), bits(ref["hits"]))
+    prims = pkg.hit_prims(a.cpu().numpy())
+    _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+    da = dev(ao)
+    occ = scene.trace(da, kind="any")["occluded"]
+    occ_s = scene.trace(da, kind="any", scheme="stream")["occluded"]
+    close = scene.trace(da)["hits"]
+    assert torch.equal(occ, occ_s)
+    assert torch.equal(occ.bool(), close.view(torch.int32)[:, 0] >= 0)
+    scene.status()
