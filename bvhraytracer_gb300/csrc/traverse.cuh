@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
     const uint32_t e = stack[sp * stride];
     if (e & kLeafBit) {
       if (COUNT && a.depth_hist)
-        atomicAdd(a.depth_hist + 64 + sc.leaf_depth[e & kLeafIndexMask], 1ull);
+        atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
       bool h = visit_leaf<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
       if (h) {
         hit = true;
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
         best = Best();
         break;
       }
-      if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + depth, 1ull);
+      if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
       if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
     }
   }
@@ -508,10 +508,10 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
           done = true;
           sp = 0;
         }
-        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + depth, 1ull);
+        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
       } else {
         if (COUNT && a.depth_hist)
-          atomicAdd(a.depth_hist + 64 + sc.leaf_depth[e & kLeafIndexMask], 1ull);
+          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
         Best best;
         best.leaf = best_leaf[ray];
         best.lane = (int)(int8_t)(misc & 0xFF);

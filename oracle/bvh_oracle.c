@@ -273,7 +273,7 @@ static int leaf_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s) {
   uint32_t pb = b->prim_begin[id], pc = b->prim_count[id];
   s->c.leaf_visits++;
   s->c.tri_tests += pc;
-  if (s->hist) s->hist[MAX_DEPTH + b->depth[id]]++;
+  if (s->hist) s->hist[MAX_DEPTH + (b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1)]++;
   int any = 0;
   for (uint32_t k = 0; k < pc; ++k) {
     float t, b1, b2;
@@ -296,7 +296,7 @@ static void node_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s, int3
                        int* sp, int leaf_sign) {
   uint32_t cb = b->child_begin[id], cc = b->child_count[id];
   s->c.node_visits++;
-  if (s->hist) s->hist[b->depth[id]]++;
+  if (s->hist) s->hist[b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1]++;
   const int8_t* ord = b->order48 + (size_t)id * 48 + s->r.code * 16;
   for (uint32_t k = 0; k < cc; ++k) {
     int i = s->r.reverse ? (int)k : (int)(cc - 1 - k);
@@ -576,7 +576,7 @@ static void fast_leaf(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
   int real = (int)b->prim_count[id];
   s->c.leaf_visits++;
   s->c.tri_tests += (uint32_t)real;
-  if (hist) hist[MAX_DEPTH + b->depth[id]]++;
+  if (hist) hist[MAX_DEPTH + (b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1)]++;
   if (s->any) {
     if (tri_any_hit(f, begin, stride, real, &s->r, &s->c)) s->hit = 1;
   } else {
@@ -600,7 +600,7 @@ static void fast_node(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
   s->c.node_visits++;
   s->c.box_tests += cc;
   s->c.box_hits += (uint32_t)__builtin_popcount(mask);
-  if (hist) hist[b->depth[id]]++;
+  if (hist) hist[b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1]++;
   if (!mask) return;
   if (s->any) {
     for (uint32_t j = 0; j < cc; ++j)
