@@ -8,6 +8,8 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
+#include <algorithm>
 
 #include "bvh_builder.hpp"
 #include "bvh_export.hpp"
@@ -42,6 +44,7 @@ struct bvhgpu_scene {
   int device = 0;
   DeviceLayout layout;  // host copy of the uploaded arrays (sizes and ids)
   int max_stack = 0;
+  std::vector<uint32_t> prim_slot;  // input triangle id -> leaf * leaf_memory + lane
   uint8_t* d_nodes = nullptr;
   float* d_leaves = nullptr;
   uint32_t* d_leaf_prim = nullptr;
@@ -287,6 +290,14 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
     delete s;
     return cuda_error(e, "status word");
   }
+  {
+    uint32_t max_id = 0;
+    for (uint32_t id : s->layout.leaf_prim)
+      if (id != 0xFFFFFFFFu) max_id = std::max(max_id, id);
+    s->prim_slot.assign((size_t)max_id + 1, 0xFFFFFFFFu);
+    for (size_t k = 0; k < s->layout.leaf_prim.size(); ++k)
+      if (s->layout.leaf_prim[k] != 0xFFFFFFFFu) s->prim_slot[s->layout.leaf_prim[k]] = (uint32_t)k;
+  }
   // The host copy of the big arrays is not needed after the upload.
   s->layout.nodes.clear();
   s->layout.nodes.shrink_to_fit();
@@ -393,6 +404,62 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   if (e != cudaSuccess) return cuda_error(e, "copy results out");
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_error(e, "synchronise");
+  return BVHGPU_OK;
+}
+
+// FastRay: tMax, pos[3], invDirection[3], direction[3] (src/fastRay.h:14-29).
+static void fastrays_to_rays(const float* fr, uint64_t n, std::vector<bvhgpu_ray_t>& rays) {
+  rays.resize(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* f = fr + i * 10;
+    rays[i] = bvhgpu_ray_t{f[1], f[2], f[3], f[0], f[7], f[8], f[9], 0.0f};
+  }
+}
+
+int bvhgpu_intersect_fastrays(bvhgpu_scene_t s, float* fastrays, uint64_t n, int32_t scheme,
+                              uint32_t* leaf_index, int8_t* tri_index, void* stream) {
+  if (!s || (n && (!fastrays || !leaf_index || !tri_index)))
+    return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  if (n == 0) return BVHGPU_OK;
+  std::vector<bvhgpu_ray_t> rays;
+  std::vector<bvhgpu_hit_t> hits(n);
+  try {
+    fastrays_to_rays(fastrays, n, rays);
+  } catch (const std::bad_alloc&) {
+    return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  }
+  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128};
+  int rc = bvhgpu_trace_host(s, rays.data(), n, &o, hits.data(), nullptr, stream);
+  if (rc) return rc;
+  const uint32_t lm = (uint32_t)s->layout.leaf_memory;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (hits[i].prim < 0) {
+      tri_index[i] = -1;
+      continue;
+    }
+    const uint32_t slot = s->prim_slot[(uint32_t)hits[i].prim];
+    leaf_index[i] = (slot / lm) * 9 * lm;
+    tri_index[i] = (int8_t)(slot % lm);
+    fastrays[i * 10] = hits[i].t;
+  }
+  return BVHGPU_OK;
+}
+
+int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t s, const float* fastrays, uint64_t n,
+                                        int32_t scheme, uint16_t* result, void* stream) {
+  if (!s || (n && (!fastrays || !result))) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  if (n == 0) return BVHGPU_OK;
+  std::vector<bvhgpu_ray_t> rays;
+  std::vector<uint8_t> occ(n);
+  try {
+    fastrays_to_rays(fastrays, n, rays);
+  } catch (const std::bad_alloc&) {
+    return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  }
+  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128};
+  int rc = bvhgpu_trace_host(s, rays.data(), n, &o, nullptr, occ.data(), stream);
+  if (rc) return rc;
+  for (uint64_t i = 0; i < n; ++i) result[i] = (uint16_t)(result[i] + occ[i]);
   return BVHGPU_OK;
 }
 

@@ -30,9 +30,6 @@
  *   bvhgpu_intersect_secondary_fastrays
  *                             FastNodeManager::intersectSecondaryWideAlternative
  *                             (fastNodeManager.h:1051-1230)
- *   bvhgpu_surface_normal_position
- *                             FastNodeManager::getSurfaceNormalPosition
- *                             (fastNodeManager.h:1700-1713)
  */
 #ifndef BVHGPU_H
 #define BVHGPU_H
@@ -187,6 +184,22 @@ int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
 int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                       const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                       void* stream);
+
+/* ---- FastRay drop-in -------------------------------------------------- */
+/* Host arrays of the reference's FastRay records (40 bytes each: tMax,
+ * pos[3], invDirection[3], direction[3]; src/fastRay.h:14-29), fast profile.
+ * Closest hit (intersect / intersectWideAlternative): for each hit ray, sets
+ * tMax to the hit distance, leaf_index[i] to the leaf's primIdBegin (float
+ * offset of its triangle block) and tri_index[i] to the in-leaf index; misses
+ * keep tMax and get tri_index -1 (leaf_index untouched), like
+ * fastNodeManager.h:1010-1015 after triIndex.fill(-1) (cameraFast.h:483).
+ * Any hit (intersectSecondary[Wide]): result[i] += 1 for each occluded ray;
+ * rays whose pos.x is NaN are skipped (fastNodeManager.h:1075-1082).
+ * scheme: BVHGPU_PER_RAY or BVHGPU_STREAM (workgroup 16). Synchronises. */
+int bvhgpu_intersect_fastrays(bvhgpu_scene_t scene, float* fastrays, uint64_t n, int32_t scheme,
+                              uint32_t* leaf_index, int8_t* tri_index, void* stream);
+int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t scene, const float* fastrays, uint64_t n,
+                                        int32_t scheme, uint16_t* result, void* stream);
 
 /* Synchronises `stream` and returns the first device-side error recorded by
  * this scene's kernels since the last call (and clears it). */

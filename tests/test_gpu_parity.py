@@ -225,3 +225,46 @@ def test_full_size_clutter_properties():
     assert torch.equal(occ, occ_s)
     assert torch.equal(occ.bool(), close.view(torch.int32)[:, 0] >= 0)
     scene.status()
+
+
+def _fastrays(rays):
+    """FastRay records (tMax, pos, invDirection, direction) like FastRay::FastRay."""
+    fr = np.zeros((rays.shape[0], 10), np.float32)
+    fr[:, 0] = rays[:, 3]
+    fr[:, 1:4] = rays[:, 0:3]
+    d = rays[:, 4:7]
+    with np.errstate(divide="ignore"):
+        inv = np.float32(1.0) / d
+    inv[d == 0] = np.finfo(np.float32).max
+    fr[:, 4:7] = inv
+    fr[:, 7:10] = d
+    return fr
+
+
+@pytest.mark.parametrize("scheme", [pkg.PER_RAY, pkg.STREAM])
+def test_fastray_drop_in(terrain, scheme):
+    """bvhgpu_intersect_fastrays / _secondary_fastrays against the oracle's
+    FastNodeManager restatement: leafIndex, triIndex, tMax and AO counts."""
+    import ctypes as C
+    from bvhraytracer_gb300 import _native as N
+    tris, b, cv, rays, scene = terrain
+    fv = O.FastView(b.export_fast())
+    ref = O.trace_fast(fv, cv, rays, any_hit=False)
+    fr = _fastrays(rays)
+    li = np.full(rays.shape[0], 7, np.uint32)
+    ti = np.zeros(rays.shape[0], np.int8)
+    N.check(N.lib().bvhgpu_intersect_fastrays(scene.handle, fr.ctypes.data, rays.shape[0], scheme,
+                                              li.ctypes.data, ti.ctypes.data, None))
+    hit = ref["tri_index"] >= 0
+    assert np.array_equal(ti, ref["tri_index"])
+    assert np.array_equal(li[hit], ref["leaf_index"][hit].astype(np.uint32))
+    assert np.all(li[~hit] == 7)
+    assert np.array_equal(fr[:, 0].view(np.uint32), ref["hits"][:, 1].view(np.uint32))
+    prims = pkg.hit_prims(ref["hits"])
+    _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+    res = np.full(ao.shape[0], 3, np.uint16)
+    fa = _fastrays(ao)
+    N.check(N.lib().bvhgpu_intersect_secondary_fastrays(scene.handle, fa.ctypes.data, ao.shape[0],
+                                                        scheme, res.ctypes.data, None))
+    occ = O.trace_fast(fv, cv, ao, any_hit=True)["occluded"]
+    assert np.array_equal(res, 3 + occ.astype(np.uint16))
