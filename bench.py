@@ -49,7 +49,11 @@ def parse():
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--ao", type=int, default=8)
-    p.add_argument("--scheme", default="per_ray", choices=["per_ray", "stream"])
+    p.add_argument("--scheme", default="persistent", choices=["per_ray", "stream", "persistent"])
+    p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
+    p.add_argument("--refill", type=int, default=8, help="persistent: idle lanes per refill")
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip timing the other traversal schemes")
     p.add_argument("--profile", default="instrumented", choices=["instrumented", "fast"])
     p.add_argument("--cpu-sample", type=float, default=0.5,
                    help="fraction of the frame traced by the cpu_baseline leg")
@@ -240,7 +244,7 @@ def run_ours(a):
     tris, bvh, primary = make_frame(a)
     scene = pkg.Scene(bvh, device=local)
     d_primary = torch.from_numpy(primary).to(dev)
-    hits0 = scene.trace(d_primary, scheme=a.scheme, profile=a.profile)["hits"]
+    hits0 = scene.trace(d_primary, profile=a.profile)["hits"]
     prims = pkg.hit_prims(hits0.cpu().numpy())
     shadow, ao = secondaries(a, tris, primary, prims)
     d_shadow = torch.from_numpy(shadow).to(dev)
@@ -253,19 +257,34 @@ def run_ours(a):
 
     batches = [(d_primary, "closest", out_h), (d_shadow, "any", out_s), (d_ao, "any", out_a)]
 
-    def step(events=None):
+    opts = {"scheme": a.scheme, "profile": a.profile}
+    if a.scheme == "persistent":
+        opts.update(policy=a.policy, refill=a.refill)
+
+    def step(events=None, o=None):
+        o = o or opts
         for i, (r, kind, out) in enumerate(batches):
             if events is not None:
                 events[i][0].record(stream)
-            scene.trace(r, kind=kind, scheme=a.scheme, profile=a.profile, out=out)
+            scene.trace(r, kind=kind, out=out, **o)
             if events is not None:
                 events[i][1].record(stream)
+
+    def frame_ms(o, reps=3):
+        step(None, o)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            step(None, o)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
 
     # Algorithmic bytes per launch from one counting pass (untimed):
     # node visits x node record bytes + triangle tests x 36 bytes.
     alg = []
     for r, kind, _ in batches:
-        c = scene.trace(r, kind=kind, scheme=a.scheme, profile=a.profile, counters=True)
+        c = scene.trace(r, kind=kind, counters=True, **opts)
         cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
         alg.append({"node_visits": int(cs[0]), "leaf_visits": int(cs[1]), "tri_tests": int(cs[4]),
                     "bytes": int(cs[0]) * scene.node_record_bytes + int(cs[4]) * 36})
@@ -309,8 +328,7 @@ def run_ours(a):
 
     def e2e_step():
         for r, o, kind in zip(h_rays, h_out, kinds):
-            scene.trace_host(r.numpy(), kind=kind, scheme=a.scheme, profile=a.profile,
-                             out=o.numpy(), stream=stream)
+            scene.trace_host(r.numpy(), kind=kind, out=o.numpy(), stream=stream, **opts)
 
     for _ in range(max(1, a.warmup)):
         e2e_step()
@@ -336,6 +354,13 @@ def run_ours(a):
     achieved = alg[dom]["bytes"] / (per_kernel_ms[dom] / 1e3) / 1e9
     names = ["primary (closest)", "shadow (any)", "AO (any)"]
 
+    compare = {}
+    if not a.no_compare:
+        variants = {"per_ray": {"scheme": "per_ray"}, "stream": {"scheme": "stream"},
+                    "persistent_while_while": {"scheme": "persistent", "policy": 0, "refill": 8},
+                    "persistent_if_if": {"scheme": "persistent", "policy": 1, "refill": 8}}
+        for name, o in variants.items():
+            compare[name] = frame_ms(dict(o, profile=a.profile))
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, tris, bvh, primary, shadow, ao, a.cpu_sample)
@@ -347,7 +372,11 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded clutter scene standing in for the reference's glTF scenes)",
             "config": {
-                "workload": workload_name(a), "method": f"plain {a.scheme} kernel, FP32 nodes",
+                "workload": workload_name(a),
+                "method": f"{a.scheme} kernel" + (f" (policy {a.policy}, refill {a.refill})"
+                                                 if a.scheme == "persistent" else "") +
+                          ", FP32 nodes",
+                "ms_per_frame_by_scheme": compare,
                 "profile": a.profile, "triangles": int(bvh.info["n_tris"]),
                 "rays_per_step": n_rays, "primary": int(primary.shape[0]),
                 "shadow": int(shadow.shape[0]), "ao": int(ao.shape[0]),

@@ -27,16 +27,16 @@ import numpy as np
 from . import _native as N
 
 __all__ = ["Bvh", "Scene", "FastNodeManager", "CompactNodeManager", "sah_factor",
-           "BvhgpuError", "CLOSEST", "ANY", "PER_RAY", "STREAM", "PROFILE_INSTRUMENTED",
+           "BvhgpuError", "CLOSEST", "ANY", "PER_RAY", "STREAM", "PERSISTENT", "PROFILE_INSTRUMENTED",
            "PROFILE_FAST"]
 
 BvhgpuError = N.BvhgpuError
 CLOSEST, ANY = N.CLOSEST, N.ANY
-PER_RAY, STREAM = N.PER_RAY, N.STREAM
+PER_RAY, STREAM, PERSISTENT = N.PER_RAY, N.STREAM, N.PERSISTENT
 PROFILE_INSTRUMENTED, PROFILE_FAST = N.PROFILE_INSTRUMENTED, N.PROFILE_FAST
 
 _KIND = {"closest": N.CLOSEST, "any": N.ANY}
-_SCHEME = {"per_ray": N.PER_RAY, "stream": N.STREAM}
+_SCHEME = {"per_ray": N.PER_RAY, "stream": N.STREAM, "persistent": N.PERSISTENT}
 _PROFILE = {"instrumented": N.PROFILE_INSTRUMENTED, "fast": N.PROFILE_FAST}
 _FORMAT = {"fp32": N.NODES_FP32, "q8": N.NODES_Q8}
 
@@ -157,7 +157,8 @@ class Scene:
 
     def trace(self, rays, *, kind: str = "closest", scheme: str = "per_ray",
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
-              counters: bool = False, depth_hist: bool = False, out=None, stream=None) -> dict:
+              policy: int = 0, refill: int = 0, counters: bool = False,
+              depth_hist: bool = False, out=None, stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -187,7 +188,7 @@ class Scene:
         if depth_hist:
             res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
             hh = _ptr(res["depth_hist"])
-        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block)
+        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill)
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
                                      C.c_void_p(s.cuda_stream)))
@@ -195,14 +196,15 @@ class Scene:
 
     def trace_host(self, rays: np.ndarray, *, kind: str = "closest", scheme: str = "per_ray",
                    profile: str = "instrumented", workgroup: int = 16, block: int = 128,
-                   out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+                   policy: int = 0, refill: int = 0, out: Optional[np.ndarray] = None,
+                   stream=None) -> np.ndarray:
         """Host rays in, host results out (copies inside the call)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = rays.shape[0]
         k = _KIND[kind]
         if out is None:
             out = (np.empty((n, 4), np.float32) if k == N.CLOSEST else np.empty(n, np.uint8))
-        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block)
+        o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill)
         sp = 0
         if stream is not None:
             sp = stream.cuda_stream

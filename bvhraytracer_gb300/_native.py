@@ -21,7 +21,7 @@ ERR_UNSUPPORTED = 6
 ERR_NO_DEVICE = 7
 
 CLOSEST, ANY = 0, 1
-PER_RAY, STREAM = 0, 1
+PER_RAY, STREAM, PERSISTENT = 0, 1, 2
 PROFILE_INSTRUMENTED, PROFILE_FAST = 0, 1
 NODES_FP32, NODES_Q8 = 0, 1
 COUNTERS_PER_RAY = 8
@@ -47,7 +47,8 @@ class SceneParams(C.Structure):
 
 class TraceOpts(C.Structure):
     _fields_ = [("kind", C.c_int32), ("scheme", C.c_int32), ("profile", C.c_int32),
-                ("workgroup", C.c_int32), ("block", C.c_int32)]
+                ("workgroup", C.c_int32), ("block", C.c_int32), ("policy", C.c_int32),
+                ("refill", C.c_int32)]
 
 
 class BvhgpuError(RuntimeError):

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 
 #include "bvh_builder.hpp"
 #include "bvh_export.hpp"
@@ -50,6 +51,12 @@ struct bvhgpu_scene {
   uint32_t* d_leaf_prim = nullptr;
   uint8_t* d_leaf_depth = nullptr;
   int* d_status = nullptr;
+  // Queue heads of the persistent scheme: one slot per launch, round robin,
+  // so up to kQueueSlots launches may be in flight on different streams.
+  static constexpr int kQueueSlots = 64;
+  unsigned long long* d_queue = nullptr;
+  std::atomic<unsigned> queue_next{0};
+  int sm_count = 0;
   // Staging for bvhgpu_trace_host (grown on demand).
   std::mutex staging_mu;
   void* d_stage = nullptr;
@@ -74,12 +81,14 @@ struct bvhgpu_scene {
     cudaFree(d_leaf_prim);
     cudaFree(d_leaf_depth);
     cudaFree(d_status);
+    cudaFree(d_queue);
     cudaFree(d_stage);
     d_nodes = nullptr;
     d_leaves = nullptr;
     d_leaf_prim = nullptr;
     d_leaf_depth = nullptr;
     d_status = nullptr;
+    d_queue = nullptr;
     d_stage = nullptr;
   }
 };
@@ -99,8 +108,12 @@ static int upload(T** dst, const std::vector<T>& src) {
 static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (!o) return set_error(BVHGPU_ERR_BAD_ARG, "null options");
   if (o->kind != BVHGPU_CLOSEST && o->kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "kind");
-  if (o->scheme != BVHGPU_PER_RAY && o->scheme != BVHGPU_STREAM)
+  if (o->scheme != BVHGPU_PER_RAY && o->scheme != BVHGPU_STREAM && o->scheme != BVHGPU_PERSISTENT)
     return set_error(BVHGPU_ERR_BAD_ARG, "scheme");
+  if (o->policy != 0 && o->policy != 1) return set_error(BVHGPU_ERR_BAD_ARG, "policy");
+  if (o->refill < 0 || o->refill > 32) return set_error(BVHGPU_ERR_BAD_ARG, "refill");
+  c.policy = o->policy;
+  c.refill_min = o->refill ? o->refill : 8;
   if (o->profile != BVHGPU_PROFILE_INSTRUMENTED && o->profile != BVHGPU_PROFILE_FAST)
     return set_error(BVHGPU_ERR_BAD_ARG, "profile");
   c.kind = o->kind;
@@ -116,9 +129,11 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   return BVHGPU_OK;
 }
 
-static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, const dev::LaunchCfg& cfg,
+static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
                   cudaStream_t st) {
   const dev::SceneDev sc = s->dev_view();
+  cfg.sm_count = s->sm_count;
+  cfg.queue = s->d_queue + (s->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
   cudaError_t e;
   switch (s->layout.node_stride) {
     case 4: e = dev::launch_trace_n4(sc, a, cfg, st); break;
@@ -285,6 +300,10 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   }
   e = cudaMalloc((void**)&s->d_status, 16);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, 16);
+  if (e == cudaSuccess)
+    e = cudaMalloc((void**)&s->d_queue, sizeof(unsigned long long) * bvhgpu_scene::kQueueSlots);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
   if (e != cudaSuccess) {
     s->release();
     delete s;
@@ -351,7 +370,7 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   if (cfg.scheme == BVHGPU_STREAM &&
       dev::stream_smem_bytes(cfg.packet, a.stack_cap, cfg.count) > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet does not fit shared memory for this tree depth");
-  if (cfg.scheme == BVHGPU_PER_RAY && (size_t)a.stack_cap * cfg.block * 4 > 227 * 1024)
+  if (cfg.scheme != BVHGPU_STREAM && (size_t)a.stack_cap * 128 * 4 > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
@@ -428,7 +447,7 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t s, float* fastrays, uint64_t n, int
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128};
+  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, hits.data(), nullptr, stream);
   if (rc) return rc;
   const uint32_t lm = (uint32_t)s->layout.leaf_memory;
@@ -456,7 +475,7 @@ int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t s, const float* fastrays,
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128};
+  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, nullptr, occ.data(), stream);
   if (rc) return rc;
   for (uint64_t i = 0; i < n; ++i) result[i] = (uint16_t)(result[i] + occ[i]);

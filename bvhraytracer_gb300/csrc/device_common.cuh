@@ -55,6 +55,10 @@ struct Ray {
   // which depend on the ray only.
   int kx, ky;
   float sx, sy, sz;
+  // True when a NaN can appear in the box tests (non-finite origin, tMax or
+  // 1/direction). Such rays take the reference's comparison forms exactly;
+  // all others use IEEE min/max (see slab_mm).
+  bool exact;
 };
 
 // Ray::Ray (src/ray.cpp:4-36) for the instrumented profile (normalise), and
@@ -84,6 +88,8 @@ BVHGPU_DEV Ray make_ray(const bvhgpu_ray_t& in) {
   r.sx = -pdx / pdz;
   r.sy = -pdy / pdz;
   r.sz = 1.f / pdz;
+  r.exact = !(isfinite(r.o[0]) && isfinite(r.o[1]) && isfinite(r.o[2]) && isfinite(r.tmax) &&
+              isfinite(r.inv[0]) && isfinite(r.inv[1]) && isfinite(r.inv[2]));
   return r;
 }
 
@@ -107,10 +113,38 @@ BVHGPU_DEV bool slab(float lx, float ly, float lz, float hx, float hy, float hz,
   return t0 <= t1;
 }
 
+// The same slab test with IEEE min / max. When no operand is NaN the two
+// forms return the same boolean: they can differ only in the sign of a zero
+// t0 / t1, and t0 <= t1 does not observe it. Rays that could produce a NaN
+// (Ray::exact) use `slab`.
+BVHGPU_DEV bool slab_mm(float lx, float ly, float lz, float hx, float hy, float hz, const Ray& r,
+                        float tmax) {
+  float tn = (lx - r.o[0]) * r.inv[0], tf = (hx - r.o[0]) * r.inv[0];
+  float t0 = fmaxf(fminf(tn, tf), 0.0f), t1 = fminf(fmaxf(tn, tf), tmax);
+  tn = (ly - r.o[1]) * r.inv[1]; tf = (hy - r.o[1]) * r.inv[1];
+  t0 = fmaxf(fminf(tn, tf), t0);
+  t1 = fminf(fmaxf(tn, tf), t1);
+  tn = (lz - r.o[2]) * r.inv[2]; tf = (hz - r.o[2]) * r.inv[2];
+  t0 = fmaxf(fminf(tn, tf), t0);
+  t1 = fminf(fmaxf(tn, tf), t1);
+  return t0 <= t1;
+}
+
+template <bool MM>
+BVHGPU_DEV bool slab_t(float lx, float ly, float lz, float hx, float hy, float hz, const Ray& r,
+                       float tmax) {
+  return MM ? slab_mm(lx, ly, lz, hx, hy, hz, r, tmax) : slab(lx, ly, lz, hx, hy, hz, r, tmax);
+}
+
+// min / max of the reference (MM false) or IEEE min / max (MM true).
+template <bool MM> BVHGPU_DEV float tmin2(float a, float b) { return MM ? fminf(a, b) : rmin(a, b); }
+template <bool MM> BVHGPU_DEV float tmax2(float a, float b) { return MM ? fmaxf(a, b) : rmax(a, b); }
+
 // Watertight ray-triangle test of Triangle::intersect(Ray&)
 // (src/primitives/triangle.cpp:52-249), on points given in the ray's
 // permuted axes (x' = kx, y' = ky, z' = kz). Returns true on a hit with
 // t <= tmax; b1 / b2 are the weights of p1 / p2.
+template <bool MM>
 BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, float& t_out,
                            float& b1_out, float& b2_out) {
   // Per-triangle box pre-test (triangle.cpp:55-79) in the permuted axes; the
@@ -122,17 +156,18 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
   const float iy = sel3(r.ky, r.inv[0], r.inv[1], r.inv[2]);
   const float iz = sel3(r.code, r.inv[0], r.inv[1], r.inv[2]);
   {
-    float bmnx = rmin(rmin(p[0][0], p[1][0]), p[2][0]);
-    float bmxx = rmax(rmax(p[0][0], p[1][0]), p[2][0]);
-    float bmny = rmin(rmin(p[0][1], p[1][1]), p[2][1]);
-    float bmxy = rmax(rmax(p[0][1], p[1][1]), p[2][1]);
-    float bmnz = rmin(rmin(p[0][2], p[1][2]), p[2][2]);
-    float bmxz = rmax(rmax(p[0][2], p[1][2]), p[2][2]);
+    // Triangle vertices are finite, so the bounds are NaN-free in both forms.
+    float bmnx = fminf(fminf(p[0][0], p[1][0]), p[2][0]);
+    float bmxx = fmaxf(fmaxf(p[0][0], p[1][0]), p[2][0]);
+    float bmny = fminf(fminf(p[0][1], p[1][1]), p[2][1]);
+    float bmxy = fmaxf(fmaxf(p[0][1], p[1][1]), p[2][1]);
+    float bmnz = fminf(fminf(p[0][2], p[1][2]), p[2][2]);
+    float bmxz = fmaxf(fmaxf(p[0][2], p[1][2]), p[2][2]);
     float t1x = (bmnx - ox) * ix, t2x = (bmxx - ox) * ix;
     float t1y = (bmny - oy) * iy, t2y = (bmxy - oy) * iy;
     float t1z = (bmnz - oz) * iz, t2z = (bmxz - oz) * iz;
-    float tmin = rmax(rmax(rmin(t1x, t2x), rmin(t1y, t2y)), rmin(t1z, t2z));
-    float tmx = rmin(rmin(rmax(t1x, t2x), rmax(t1y, t2y)), rmax(t1z, t2z));
+    float tmin = tmax2<MM>(tmax2<MM>(tmin2<MM>(t1x, t2x), tmin2<MM>(t1y, t2y)), tmin2<MM>(t1z, t2z));
+    float tmx = tmin2<MM>(tmin2<MM>(tmax2<MM>(t1x, t2x), tmax2<MM>(t1y, t2y)), tmax2<MM>(t1z, t2z));
     if (tmx < 0) return false;
     if (tmin > tmx) return false;
     if (tmax < tmin) return false;
@@ -171,14 +206,14 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
   float b2 = e2 * inv_det;
   float t = t_scaled * inv_det;
   // Conservative t > 0 check (triangle.cpp:172-196).
-  float max_zt = rmax(rmax(fabsf(p0z), fabsf(p1z)), fabsf(p2z));
+  float max_zt = tmax2<MM>(tmax2<MM>(fabsf(p0z), fabsf(p1z)), fabsf(p2z));
   float delta_z = kGamma3 * max_zt;
-  float max_xt = rmax(rmax(fabsf(p0x), fabsf(p1x)), fabsf(p2x));
-  float max_yt = rmax(rmax(fabsf(p0y), fabsf(p1y)), fabsf(p2y));
+  float max_xt = tmax2<MM>(tmax2<MM>(fabsf(p0x), fabsf(p1x)), fabsf(p2x));
+  float max_yt = tmax2<MM>(tmax2<MM>(fabsf(p0y), fabsf(p1y)), fabsf(p2y));
   float delta_x = kGamma5 * (max_xt + max_zt);
   float delta_y = kGamma5 * (max_yt + max_zt);
   float delta_e = 2 * (kGamma2 * max_xt * max_yt + delta_y * max_xt + delta_x * max_yt);
-  float max_e = rmax(rmax(fabsf(e0), fabsf(e1)), fabsf(e2));
+  float max_e = tmax2<MM>(tmax2<MM>(fabsf(e0), fabsf(e1)), fabsf(e2));
   float delta_t =
       3 * (kGamma3 * max_e * max_zt + delta_e * max_zt + delta_z * max_e) * fabsf(inv_det);
   if (t <= delta_t) return false;

@@ -14,6 +14,10 @@ struct LaunchCfg {
   bool count = false;
   int block = 128;      // per-ray scheme threads per block
   int packet = 256;     // stream scheme rays per block
+  int policy = 0;       // persistent scheme: 0 while-while, 1 if-if
+  int refill_min = 8;   // persistent scheme: idle lanes that trigger a refill
+  unsigned long long* queue = nullptr;  // persistent scheme: zeroed queue head
+  int sm_count = 152;
 };
 
 template <typename K>
@@ -34,6 +38,24 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     if (e != cudaSuccess) return e;
     const uint64_t grid = (a.n + bs - 1) / bs;
     k<<<(unsigned)grid, bs, smem, s>>>(sc, a);
+  } else if (cfg.scheme == BVHGPU_PERSISTENT) {
+    const int bs = 128;
+    const size_t smem = (size_t)a.stack_cap * bs * 4;
+    auto k = cfg.policy == 0 ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 0>
+                             : trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 1>;
+    cudaError_t e = set_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, bs, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    uint64_t grid = (uint64_t)per_sm * cfg.sm_count;
+    const uint64_t need = (a.n + bs - 1) / bs;
+    if (grid > need) grid = need;
+    QueueArgs q{cfg.queue, cfg.refill_min};
+    e = cudaMemsetAsync(cfg.queue, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)grid, bs, smem, s>>>(sc, a, q);
   } else {
     const int p = cfg.packet;
     const size_t smem = stream_smem_bytes(p, a.stack_cap, COUNT);

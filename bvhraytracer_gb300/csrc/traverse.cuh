@@ -74,7 +74,7 @@ BVHGPU_DEV void load_bytes(const uint8_t* p, uint64_t& lo, uint64_t& hi) {
 
 // One inner-node visit: slab-test the children and push the hits.
 // Returns false on stack overflow.
-template <int N, int PROFILE, int KIND, bool COUNT>
+template <int N, int PROFILE, int KIND, bool COUNT, bool MM>
 BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r, float tmax,
                            uint32_t* stack, int stride, int& sp, int cap, Counters& ctr,
                            int& depth_out) {
@@ -98,8 +98,8 @@ BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r,
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (4 * q + k < N) {
-        bool h = slab(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k), f4get(hy, k),
-                      f4get(hz, k), r, tmax);
+        bool h = slab_t<MM>(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k),
+                            f4get(hy, k), f4get(hz, k), r, tmax);
         hit |= (uint32_t)h << (4 * q + k);
       }
     }
@@ -159,7 +159,7 @@ struct Best {
 // on a hit. With COUNT false, any-hit rays stop at the first hit triangle
 // (the leaf's result is the same); with COUNT true all triangles are tested
 // like the reference.
-template <int PROFILE, int KIND, bool COUNT>
+template <int PROFILE, int KIND, bool COUNT, bool MM>
 BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax, Best& best,
                            Counters& ctr) {
   const uint32_t leaf = e & kLeafIndexMask;
@@ -201,7 +201,7 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
       float t, b1, b2;
       bool h;
       if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED)
-        h = watertight(p, r, tmax, t, b1, b2);
+        h = watertight<MM>(p, r, tmax, t, b1, b2);
       else
         h = moller_trumbore(p, r, tmax, t, b1, b2);
       if (!h) continue;
@@ -251,6 +251,25 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
     any = true;
   }
   return any;
+}
+
+// Visits with the IEEE min / max forms unless the ray can produce a NaN.
+template <int N, int PROFILE, int KIND, bool COUNT>
+BVHGPU_DEV bool node_step(const SceneDev& sc, const uint8_t* rec, const Ray& r, float tmax,
+                          uint32_t* stack, int stride, int& sp, int cap, Counters& ctr,
+                          int& depth) {
+  if (r.exact)
+    return visit_node<N, PROFILE, KIND, COUNT, false>(sc, rec, r, tmax, stack, stride, sp, cap,
+                                                      ctr, depth);
+  return visit_node<N, PROFILE, KIND, COUNT, true>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
+                                                   depth);
+}
+
+template <int PROFILE, int KIND, bool COUNT>
+BVHGPU_DEV bool leaf_step(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax, Best& best,
+                          Counters& ctr) {
+  if (r.exact) return visit_leaf<PROFILE, KIND, COUNT, false>(sc, e, r, tmax, best, ctr);
+  return visit_leaf<PROFILE, KIND, COUNT, true>(sc, e, r, tmax, best, ctr);
 }
 
 BVHGPU_DEV void record_error(int* status, int code) { atomicCAS(status, 0, code); }
@@ -337,7 +356,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
     if (e & kLeafBit) {
       if (COUNT && a.depth_hist)
         atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
-      bool h = visit_leaf<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
+      bool h = leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
       if (h) {
         hit = true;
         if (KIND == BVHGPU_ANY) break;
@@ -345,8 +364,8 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
     } else {
       const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
       int depth;
-      if (!visit_node<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
-                                               depth)) {
+      if (!node_step<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
+                                              depth)) {
         record_error(sc.status, kDevErrStackOverflow);
         hit = false;
         best = Best();
@@ -383,7 +402,7 @@ BVHGPU_DEV void pack_ray(const Ray& r, StreamRay& s) {
   s.tmax = r.tmax;
   s.sx = r.sx; s.sy = r.sy; s.sz = r.sz;
   s.bits = (uint32_t)r.code | ((uint32_t)r.reverse << 2) | ((uint32_t)r.kx << 3) |
-           ((uint32_t)r.ky << 5);
+           ((uint32_t)r.ky << 5) | ((uint32_t)r.exact << 7);
 }
 BVHGPU_DEV Ray unpack_ray(const StreamRay& s) {
   Ray r;
@@ -394,6 +413,7 @@ BVHGPU_DEV Ray unpack_ray(const StreamRay& s) {
   r.reverse = ((s.bits >> 2) & 1u) != 0;
   r.kx = (int)((s.bits >> 3) & 3u);
   r.ky = (int)((s.bits >> 5) & 3u);
+  r.exact = ((s.bits >> 7) & 1u) != 0;
   return r;
 }
 
@@ -500,8 +520,8 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       if (is_node) {
         const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
         int depth;
-        if (!visit_node<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stacks + ray, P, sp, cap, ctr,
-                                                 depth)) {
+        if (!node_step<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stacks + ray, P, sp, cap, ctr,
+                                                depth)) {
           record_error(sc.status, kDevErrStackOverflow);
           best_leaf[ray] = 0xFFFFFFFFu;
           misc = 0xFF;
@@ -517,7 +537,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
         best.lane = (int)(int8_t)(misc & 0xFF);
         best.u = best_u[ray];
         best.v = best_v[ray];
-        bool h = visit_leaf<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
+        bool h = leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
         if (h) {
           misc |= (int32_t)0x80000000;
           if (KIND == BVHGPU_ANY) done = true;
@@ -589,6 +609,145 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       uint32_t* o = a.counters + rid * BVHGPU_COUNTERS_PER_RAY;
       for (int k = 0; k < 7; ++k) o[k] = ctrs[k * P + tid];
       o[7] = 0;
+    }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// Persistent depth-first traversal. A grid sized to fill the GPU once loops
+// until a global ray queue is drained; each warp refills its finished lanes
+// with the next rays (one atomicAdd per refill) so warps stay full on
+// incoherent rays, the GPU form of the reference's refill structure
+// (RefillStructure, fastNodeManager.h:92-156, 277-450). Lanes keep the
+// per-ray depth-first order, so every ray's visits and results are those of
+// the plain kernel; only the interleaving between lanes changes.
+//
+// POLICY 0 ("while-while"): each round, lanes whose stack top is an inner node
+// visit nodes until every active lane has a leaf on top, then all of them
+// visit their leaf together. POLICY 1 ("if-if"): one node or leaf visit per
+// lane per round.
+struct QueueArgs {
+  unsigned long long* head;  // next unclaimed ray (zeroed before the launch)
+  int refill_min;            // refill when at least this many lanes are idle
+};
+
+template <int N, int PROFILE, int KIND, bool COUNT, int POLICY>
+__global__ void __launch_bounds__(128) trace_persistent_kernel(SceneDev sc, TraceArgs a,
+                                                               QueueArgs q) {
+  extern __shared__ uint32_t smem[];
+  const int stride = blockDim.x;
+  uint32_t* stack = smem + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  const int cap = a.stack_cap;
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+
+  Ray r;
+  float tmax = 0.f;
+  Best best;
+  Counters ctr;
+  bool active = false, hit = false;
+  int sp = 0;
+  uint64_t rid = 0;
+  bool drained = false;
+
+  while (true) {
+    const unsigned idle = __ballot_sync(FULL, !active);
+    if (!drained && idle != 0 && ((int)__popc(idle) >= q.refill_min || idle == FULL)) {
+      const int leader = __ffs(idle) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(q.head, (unsigned long long)__popc(idle));
+      base = __shfl_sync(FULL, base, leader);
+      if (base + __popc(idle) >= a.n) drained = true;
+      if (!active) {
+        const uint64_t my = base + __popc(idle & below);
+        if (my < a.n) {
+          rid = my;
+          const bvhgpu_ray_t in = load_ray(a.rays, rid);
+          if (isnan(in.ox)) {
+            Best none;
+            write_result<KIND>(sc, a, rid, false, in.tmax, none);
+            Counters c0;
+            flush_counters<COUNT>(a, rid, c0);
+          } else {
+            r = make_ray<PROFILE>(in);
+            tmax = r.tmax;
+            best = Best();
+            ctr = Counters();
+            hit = false;
+            stack[0] = sc.root_entry;
+            sp = 1;
+            active = true;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(FULL, active) == 0) {
+      if (drained) break;
+      continue;
+    }
+
+    if (POLICY == 0) {
+      // Node visits until every active lane has a leaf on top (or is done).
+      while (true) {
+        const bool want =
+            active && sp > 0 && (stack[(sp - 1) * stride] & kLeafBit) == 0u;
+        if (__ballot_sync(FULL, want) == 0) break;
+        if (want) {
+          --sp;
+          const uint32_t e = stack[sp * stride];
+          int depth;
+          if (!node_step<N, PROFILE, KIND, COUNT>(sc, sc.nodes + (size_t)e * NodeFmt<N>::REC, r,
+                                                  tmax, stack, stride, sp, cap, ctr, depth)) {
+            record_error(sc.status, kDevErrStackOverflow);
+            hit = false;
+            best = Best();
+            sp = 0;
+          }
+          if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+          if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
+        }
+      }
+      if (active && sp > 0) {
+        --sp;
+        const uint32_t e = stack[sp * stride];
+        if (COUNT && a.depth_hist)
+          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+        if (leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr)) {
+          hit = true;
+          if (KIND == BVHGPU_ANY) sp = 0;
+        }
+      }
+    } else {
+      if (active && sp > 0) {
+        --sp;
+        const uint32_t e = stack[sp * stride];
+        if (e & kLeafBit) {
+          if (COUNT && a.depth_hist)
+            atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+          if (leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr)) {
+            hit = true;
+            if (KIND == BVHGPU_ANY) sp = 0;
+          }
+        } else {
+          int depth;
+          if (!node_step<N, PROFILE, KIND, COUNT>(sc, sc.nodes + (size_t)e * NodeFmt<N>::REC, r,
+                                                  tmax, stack, stride, sp, cap, ctr, depth)) {
+            record_error(sc.status, kDevErrStackOverflow);
+            hit = false;
+            best = Best();
+            sp = 0;
+          }
+          if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+          if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
+        }
+      }
+    }
+    if (active && sp == 0) {
+      write_result<KIND>(sc, a, rid, hit, tmax, best);
+      flush_counters<COUNT>(a, rid, ctr);
+      active = false;
     }
   }
 }

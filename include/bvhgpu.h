@@ -148,6 +148,9 @@ typedef struct {
 
 #define BVHGPU_PER_RAY 0 /* depth-first traversal, one thread per ray */
 #define BVHGPU_STREAM 1  /* ray-stream traversal over node / leaf work lists */
+/* depth-first per ray, by persistent warps that refill finished lanes from a
+ * global ray queue (same per-ray results as BVHGPU_PER_RAY) */
+#define BVHGPU_PERSISTENT 2
 
 /* Instrumented profile: CompactNodeManager + Ray + Triangle::intersect
  * semantics (direction normalised, watertight leaf test with the per-triangle
@@ -162,8 +165,11 @@ typedef struct {
   int32_t kind;      /* BVHGPU_CLOSEST / BVHGPU_ANY */
   int32_t scheme;    /* BVHGPU_PER_RAY / BVHGPU_STREAM */
   int32_t profile;   /* BVHGPU_PROFILE_* */
-  int32_t workgroup; /* stream scheme: packet = workgroup^2 rays (8, 16, 32); 0 = 16 */
-  int32_t block;     /* per-ray scheme: threads per block (0 = default) */
+  int32_t workgroup; /* stream scheme: packet = workgroup^2 rays (8, 16); 0 = 16 */
+  int32_t block;     /* per-ray scheme: threads per block (32, 64, 128; 0 = 128) */
+  int32_t policy;    /* persistent scheme: 0 while-while, 1 if-if */
+  int32_t refill;    /* persistent scheme: idle lanes of a warp that trigger a refill
+                        (1..32; 0 = 8) */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):

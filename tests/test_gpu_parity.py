@@ -14,6 +14,10 @@ from tests import _scenes as TS  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 LIGHT = [2.0, 3.0, 2.0]
+# (scheme, extra trace options): every traversal scheme and persistent policy
+SCHEMES = [("per_ray", {}), ("stream", {}), ("persistent", {"policy": 0}),
+           ("persistent", {"policy": 1, "refill": 1})]
+SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1"]
 
 
 def dev(a):
@@ -57,36 +61,37 @@ def terrain():
     return tris, b, cv, rays, pkg.Scene(b)
 
 
-@pytest.mark.parametrize("scheme", ["per_ray", "stream"])
-def test_terrain_instrumented_primary_and_shadow(terrain, scheme):
+@pytest.mark.parametrize("scheme,kw", SCHEMES, ids=SCHEME_IDS)
+def test_terrain_instrumented_primary_and_shadow(terrain, scheme, kw):
     tris, b, cv, rays, scene = terrain
     ref = O.trace_instrumented(cv, rays, shadow=False)
-    got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True)
+    got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True, **kw)
     check_closest(got, ref)
     prims = pkg.hit_prims(ref["hits"])
     sh, _ = TS.secondary(tris, rays, prims, LIGHT)
     refs = O.trace_instrumented(cv, sh, shadow=True)
-    gots = scene.trace(dev(sh), kind="any", scheme=scheme, counters=True, depth_hist=True)
+    gots = scene.trace(dev(sh), kind="any", scheme=scheme, counters=True, depth_hist=True, **kw)
     check_any(gots, refs)
     # the fast (counter-free) kernels give the same hits
-    check_closest(scene.trace(dev(rays), scheme=scheme), ref, counters=False)
-    check_any(scene.trace(dev(sh), kind="any", scheme=scheme), refs, counters=False)
+    check_closest(scene.trace(dev(rays), scheme=scheme, **kw), ref, counters=False)
+    check_any(scene.trace(dev(sh), kind="any", scheme=scheme, **kw), refs, counters=False)
     scene.status()
 
 
-@pytest.mark.parametrize("scheme", ["per_ray", "stream"])
-def test_terrain_fast_profile(terrain, scheme):
+@pytest.mark.parametrize("scheme,kw", SCHEMES, ids=SCHEME_IDS)
+def test_terrain_fast_profile(terrain, scheme, kw):
     tris, b, cv, rays, scene = terrain
     fv = O.FastView(b.export_fast())
     ref = O.trace_fast(fv, cv, rays, any_hit=False)
-    got = scene.trace(dev(rays), scheme=scheme, profile="fast", counters=True, depth_hist=True)
+    got = scene.trace(dev(rays), scheme=scheme, profile="fast", counters=True, depth_hist=True,
+                      **kw)
     check_closest(got, ref)
     prims = pkg.hit_prims(ref["hits"])
     sh, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
     for sec in (sh, ao):
         r = O.trace_fast(fv, cv, sec, any_hit=True)
         g = scene.trace(dev(sec), kind="any", scheme=scheme, profile="fast", counters=True,
-                        depth_hist=True)
+                        depth_hist=True, **kw)
         check_any(g, r)
 
 
@@ -108,15 +113,16 @@ def test_sweep_all_widths(n, l):
             refa = O.trace_instrumented(cv, ao, shadow=True)
         else:
             refa = O.trace_fast(fv, cv, ao, any_hit=True)
-        for scheme in ("per_ray", "stream"):
+        for scheme, kw in SCHEMES:
             got = scene.trace(dev(rays), scheme=scheme, profile=profile, counters=True,
-                              depth_hist=True)
+                              depth_hist=True, **kw)
             check_closest(got, ref)
             g = scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile, counters=True,
-                            depth_hist=True)
+                            depth_hist=True, **kw)
             check_any(g, refa)
-            check_closest(scene.trace(dev(rays), scheme=scheme, profile=profile), ref, False)
-            check_any(scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile), refa, False)
+            check_closest(scene.trace(dev(rays), scheme=scheme, profile=profile, **kw), ref, False)
+            check_any(scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile, **kw),
+                      refa, False)
 
 
 @pytest.mark.parametrize("gang,leaf_memory", [(8, 0), (4, 16), (8, 16)])
@@ -126,9 +132,9 @@ def test_gang_and_leaf_memory(gang, leaf_memory):
     scene = pkg.Scene(b, gang=gang, leaf_memory=leaf_memory)
     fv = O.FastView(b.export_fast(gang=gang, leaf_memory=leaf_memory))
     ref = O.trace_fast(fv, cv, rays, any_hit=False)
-    for scheme in ("per_ray", "stream"):
+    for scheme, kw in SCHEMES:
         check_closest(scene.trace(dev(rays), scheme=scheme, profile="fast", counters=True,
-                                  depth_hist=True), ref)
+                                  depth_hist=True, **kw), ref)
     ref = O.trace_instrumented(cv, rays, shadow=False)
     check_closest(scene.trace(dev(rays), counters=True, depth_hist=True), ref)
 
@@ -139,8 +145,9 @@ def test_top_levels_layout(top_levels):
     rays = TS.clutter_rays(tris, res=(64, 48))
     ref = O.trace_instrumented(cv, rays, shadow=False)
     scene = pkg.Scene(b, top_levels=top_levels)
-    for scheme in ("per_ray", "stream"):
-        check_closest(scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True), ref)
+    for scheme, kw in SCHEMES:
+        check_closest(scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True, **kw),
+                      ref)
 
 
 def test_edge_cases():
@@ -155,12 +162,12 @@ def test_edge_cases():
                      [0.25, 0.25, 0, 4.0, 0, 0, 1, 0],        # tmax too short
                      [0.25, 0.25, 10, 222222, 0, 0, -3, 0]],  # from behind, long direction
                     np.float32)
-    for scheme in ("per_ray", "stream"):
-        got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True)
+    for scheme, kw in SCHEMES:
+        got = scene.trace(dev(rays), scheme=scheme, counters=True, depth_hist=True, **kw)
         ref = O.trace_instrumented(cv, rays, shadow=False)
         check_closest(got, ref)
         assert pkg.hit_prims(got["hits"].cpu().numpy()).tolist() == [0, -1, -1, -1, 0]
-        occ = scene.trace(dev(rays), kind="any", scheme=scheme)["occluded"].cpu().numpy()
+        occ = scene.trace(dev(rays), kind="any", scheme=scheme, **kw)["occluded"].cpu().numpy()
         assert occ.tolist() == [1, 0, 0, 0, 1]
     # empty batch
     e = scene.trace(dev(np.zeros((0, 8), np.float32)))
@@ -172,8 +179,9 @@ def test_ragged_ray_counts(n, terrain):
     tris, b, cv, rays, scene = terrain
     r = rays[40000:40000 + n]
     ref = O.trace_instrumented(cv, r, shadow=False)
-    for scheme in ("per_ray", "stream"):
-        check_closest(scene.trace(dev(r), scheme=scheme, counters=True, depth_hist=True), ref)
+    for scheme, kw in SCHEMES:
+        check_closest(scene.trace(dev(r), scheme=scheme, counters=True, depth_hist=True, **kw),
+                      ref)
 
 
 def test_host_entry_point_matches_device(terrain):
@@ -210,8 +218,9 @@ def test_full_size_clutter_properties():
     rays = S.clutter_camera(4000, 1920, 1080)
     d = dev(rays)
     a = scene.trace(d)["hits"]
-    s = scene.trace(d, scheme="stream")["hits"]
-    assert torch.equal(a.view(torch.int32), s.view(torch.int32))
+    for scheme, kw in SCHEMES[1:]:
+        s = scene.trace(d, scheme=scheme, **kw)["hits"]
+        assert torch.equal(a.view(torch.int32), s.view(torch.int32)), scheme
     cv = O.CompactView(b.export_compact())
     idx = np.random.default_rng(0).choice(rays.shape[0], 20000, replace=False)
     ref = O.trace_instrumented(cv, rays[idx], shadow=False)
@@ -220,9 +229,9 @@ def test_full_size_clutter_properties():
     _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
     da = dev(ao)
     occ = scene.trace(da, kind="any")["occluded"]
-    occ_s = scene.trace(da, kind="any", scheme="stream")["occluded"]
+    for scheme, kw in SCHEMES[1:]:
+        assert torch.equal(occ, scene.trace(da, kind="any", scheme=scheme, **kw)["occluded"])
     close = scene.trace(da)["hits"]
-    assert torch.equal(occ, occ_s)
     assert torch.equal(occ.bool(), close.view(torch.int32)[:, 0] >= 0)
     scene.status()
 
