@@ -34,7 +34,6 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mrays/s"
-LIGHT = (10.0, 3.8, 5.0)
 
 
 def parse():
@@ -87,7 +86,8 @@ def make_frame(a, scene_trace=None):
 def secondaries(a, tris, primary, prims):
     from bvhraytracer_gb300 import scenes as S
     m, p, n = S.surface(tris, primary, prims)
-    shadow = S.shadow_rays(p, n, np.array(LIGHT) * (a.objects / 4000.0) ** (1 / 3))
+    _, _, light = S.clutter_viewpoints(a.objects, seed=1)
+    shadow = S.shadow_rays(p, n, light)
     ao = S.ao_rays(p, n, a.ao, 0.1 * S.scene_diagonal(tris), seed=11)
     return shadow, ao
 

@@ -79,8 +79,9 @@ def _uv_sphere(center, radius, seg: int = 16, rings: int = 8) -> np.ndarray:
     return np.concatenate(tris).reshape(-1, 9)
 
 
-def _box(center, half, sub: int = 4) -> np.ndarray:
-    """Axis-aligned box with each face subdivided ``sub x sub``."""
+def _box(center, half, sub: int = 4, outward: bool = True) -> np.ndarray:
+    """Axis-aligned box with each face subdivided ``sub x sub``; faces wound
+    so their geometric normals point out of the box (or into it)."""
     s = np.linspace(-1.0, 1.0, sub + 1)
     u, v = np.meshgrid(s, s, indexing="ij")
     faces = []
@@ -94,12 +95,15 @@ def _box(center, half, sub: int = 4) -> np.ndarray:
             else:
                 p[..., a1], p[..., a2] = v, u
             faces.append(_grid_tris(center + half * p))
-    return np.concatenate(faces)
+    tris = np.concatenate(faces)
+    if outward:  # swap p1 and p2 to flip the winding
+        tris = tris.reshape(-1, 3, 3)[:, [0, 2, 1]].reshape(-1, 9)
+    return tris
 
 
-def clutter(n_objects: int = 4000, seed: int = 1, sphere_fraction: float = 0.9,
-            blobs: int = 30) -> np.ndarray:
-    """Cluttered room; about 250 triangles per object."""
+def clutter_objects(n_objects: int = 4000, seed: int = 1, sphere_fraction: float = 0.9,
+                    blobs: int = 30):
+    """Object placement of :func:`clutter`: (room, centres, sizes, is_sphere, aspect)."""
     rng = np.random.default_rng(seed)
     scale = (n_objects / 4000.0) ** (1.0 / 3.0)
     room = np.array([20.0, 4.0, 10.0]) * scale
@@ -111,15 +115,48 @@ def clutter(n_objects: int = 4000, seed: int = 1, sphere_fraction: float = 0.9,
     size = np.exp(rng.uniform(math.log(0.05), math.log(1.0), n_objects))
     is_sphere = rng.uniform(size=n_objects) < sphere_fraction
     aspect = rng.uniform(0.5, 1.0, (n_objects, 3))
+    return room, pos, size, is_sphere, aspect
+
+
+def clutter(n_objects: int = 4000, seed: int = 1, sphere_fraction: float = 0.9,
+            blobs: int = 30) -> np.ndarray:
+    """Cluttered room; about 250 triangles per object."""
+    room, pos, size, is_sphere, aspect = clutter_objects(n_objects, seed, sphere_fraction, blobs)
     parts = []
-    # Room walls (floor, ceiling, four walls), 8 x 8 quads each.
-    parts.append(_box(room / 2, room / 2, sub=8))
+    # Room walls (floor, ceiling, four walls), 8 x 8 quads each, facing inward.
+    parts.append(_box(room / 2, room / 2, sub=8, outward=False))
     for i in range(n_objects):
         if is_sphere[i]:
             parts.append(_uv_sphere(pos[i], size[i] / 2))
         else:
             parts.append(_box(pos[i], size[i] / 2 * aspect[i]))
     return np.concatenate(parts).astype(np.float32)
+
+
+def _clearest(candidates: np.ndarray, pos: np.ndarray, size: np.ndarray) -> np.ndarray:
+    """The candidate point farthest from every object's bounding sphere."""
+    best, best_c = -np.inf, candidates[0]
+    for c in candidates:
+        clear = np.min(np.linalg.norm(pos - c, axis=1) - size * 0.5 * math.sqrt(3.0))
+        if clear > best:
+            best, best_c = clear, c
+    return best_c
+
+
+def clutter_viewpoints(n_objects: int = 4000, seed: int = 1):
+    """Camera position, camera target and point-light position for the
+    clutter scene, placed in free space (largest clearance to any object):
+    the camera near the x = 0 wall at mid height looking down the room, the
+    light under the ceiling near the room centre."""
+    room, pos, size, _, _ = clutter_objects(n_objects, seed)
+    g = np.stack(np.meshgrid(np.linspace(0.03, 0.2, 6), np.linspace(0.35, 0.65, 5),
+                             np.linspace(0.3, 0.7, 9), indexing="ij"), -1).reshape(-1, 3)
+    cam = _clearest(g * room, pos, size)
+    target = np.array([0.95, 0.4, 0.5]) * room
+    gl = np.stack(np.meshgrid(np.linspace(0.35, 0.65, 7), np.linspace(0.8, 0.95, 4),
+                              np.linspace(0.3, 0.7, 7), indexing="ij"), -1).reshape(-1, 3)
+    light = _clearest(gl * room, pos, size)
+    return cam, target, light.astype(np.float32)
 
 
 def scene_diagonal(tris: np.ndarray) -> float:
@@ -226,8 +263,7 @@ def terrain_workload(n: int = 128, res: int = 512, seed: int = 0):
     return tris, rays, np.array([2.0, 3.0, 2.0], np.float32)
 
 
-def clutter_camera(n_objects: int = 4000, width: int = 1920, height: int = 1080):
-    scale = (n_objects / 4000.0) ** (1.0 / 3.0)
-    pos = np.array([0.6, 2.0, 5.0]) * scale
-    target = np.array([19.0, 1.5, 5.0]) * scale
-    return camera_rays(pos, target, width, height)
+def clutter_camera(n_objects: int = 4000, width: int = 1920, height: int = 1080, seed: int = 1):
+    """Primary rays of the clutter scene from :func:`clutter_viewpoints`."""
+    cam, target, _ = clutter_viewpoints(n_objects, seed)
+    return camera_rays(cam, target, width, height)

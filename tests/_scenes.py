@@ -34,7 +34,7 @@ def bvh(kind: str, n: int, l: int, **kw):
 
 
 def clutter_rays(tris: np.ndarray, n_objects: int = 120, res=(96, 64)):
-    return S.clutter_camera(n_objects, *res)
+    return S.clutter_camera(n_objects, *res, seed=3)
 
 
 def secondary(tris, rays, prims, light, ao_samples=2, length=None, seed=7):
