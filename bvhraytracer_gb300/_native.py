@@ -9,7 +9,11 @@ import ctypes as C
 import threading
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "_build" / "libbvhgpu.so"
+import os
+
+# BVHGPU_LIBRARY may point at another build of the same library (tuning runs).
+LIB_PATH = Path(os.environ.get("BVHGPU_LIBRARY",
+                               Path(__file__).resolve().parent / "_build" / "libbvhgpu.so"))
 
 OK = 0
 ERR_BAD_ARG = 1

@@ -56,35 +56,42 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
-def build(verbose: bool = False) -> Path:
-    """Compiles every translation unit and links libbvhgpu.so; returns its path."""
-    BUILD.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, defines: tuple = (), out_dir: Path | None = None) -> Path:
+    """Compiles every translation unit and links libbvhgpu.so; returns its path.
+
+    ``defines`` (e.g. ``("BVHGPU_PERSIST_MIN_BLOCKS=6",)``) and ``out_dir``
+    build a variant of the library elsewhere, for tuning experiments.
+    """
+    build_dir = Path(out_dir) if out_dir else BUILD
+    lib_path = build_dir / "libbvhgpu.so"
+    build_dir.mkdir(parents=True, exist_ok=True)
+    extra = [f"-D{d}" for d in defines]
     headers = list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "bvhgpu.h"]
     nvcc = _nvcc()
     jobs = []
     objs = []
     for src in sorted(CSRC.glob("*.cu")):
-        obj = BUILD / (src.stem + ".cu.o")
+        obj = build_dir / (src.stem + ".cu.o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc] + NVCC_FLAGS + extra + ["-c", str(src), "-o", str(obj)])
     cxx = os.environ.get("CXX", "g++")
     for src in sorted(CSRC.glob("*.cpp")):
-        obj = BUILD / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
             jobs.append([cxx] + CXX_FLAGS + [f"-I{_cuda_include()}", "-c", str(src), "-o", str(obj)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(_run, jobs))
-    if jobs or _stale(LIB, objs):
-        tmp = BUILD / "libbvhgpu.so.tmp"
+    if jobs or _stale(lib_path, objs):
+        tmp = build_dir / "libbvhgpu.so.tmp"
         _run([nvcc] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] +
              ["-Xcompiler", "-pthread"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_path)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib_path}")
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -632,9 +632,12 @@ struct QueueArgs {
   int refill_min;            // refill when at least this many lanes are idle
 };
 
+#ifndef BVHGPU_PERSIST_MIN_BLOCKS
+#define BVHGPU_PERSIST_MIN_BLOCKS 1
+#endif
 template <int N, int PROFILE, int KIND, bool COUNT, int POLICY>
-__global__ void __launch_bounds__(128) trace_persistent_kernel(SceneDev sc, TraceArgs a,
-                                                               QueueArgs q) {
+__global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
+    trace_persistent_kernel(SceneDev sc, TraceArgs a, QueueArgs q) {
   extern __shared__ uint32_t smem[];
   const int stride = blockDim.x;
   uint32_t* stack = smem + threadIdx.x;
