@@ -214,6 +214,28 @@ class Scene:
             C.c_void_p(sp)))
         return out
 
+    def trace_batches_noalloc(self, batches, *, profile: str = "instrumented", policy: int = 0,
+                              refill: int = 0, stream=None) -> None:
+        """Traces up to 64 batches with no GPU allocation in the call.
+
+        ``batches``: list of ``(rays, kind, out)`` with device tensors: rays
+        ``[n, 8]`` float32, kind ``"closest"`` (out ``[n, 4]`` float32) or
+        ``"any"`` (out ``[n]`` uint8). For callers that must not allocate GPU
+        memory while they trace; the scratch is a fixed array inside the
+        library shared by all calls, so calls must not overlap on the GPU.
+        """
+        import torch
+        arr = (N.Batch * max(1, len(batches)))()
+        for i, (rays, kind, out) in enumerate(batches):
+            k = _KIND[kind]
+            arr[i] = N.Batch(_ptr(rays), rays.shape[0], k, 0,
+                             _ptr(out) if k == N.CLOSEST else None,
+                             _ptr(out) if k == N.ANY else None)
+        o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        N.check(N.lib().bvhgpu_trace_batches_noalloc(self._h, arr, len(batches), C.byref(o),
+                                                     C.c_void_p(s.cuda_stream)))
+
     def status(self, stream=None) -> None:
         """Raises if a kernel of this scene recorded a device-side error."""
         sp = stream.cuda_stream if stream is not None else 0

@@ -55,6 +55,11 @@ class TraceOpts(C.Structure):
                 ("refill", C.c_int32)]
 
 
+class Batch(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("n", C.c_uint64), ("kind", C.c_int32), ("pad", C.c_int32),
+                ("hits", C.c_void_p), ("occluded", C.c_void_p)]
+
+
 class BvhgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"bvhgpu error {code}: {msg}")
@@ -82,6 +87,8 @@ _SIGS = {
     "bvhgpu_trace_host": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P]),
     "bvhgpu_intersect_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P, _P]),
     "bvhgpu_intersect_secondary_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P]),
+    "bvhgpu_trace_batches_noalloc": (C.c_int, [_P, C.POINTER(Batch), C.c_int32,
+                                                C.POINTER(TraceOpts), _P]),
     "bvhgpu_scene_status": (C.c_int, [_P, _P]),
 }
 

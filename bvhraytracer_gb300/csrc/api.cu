@@ -499,4 +499,118 @@ int bvhgpu_scene_status(bvhgpu_scene_t s, void* stream) {
   return BVHGPU_OK;
 }
 
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Entry point that allocates nothing.
+//
+// Some callers cannot call cudaMalloc while they trace: a renderer plugin
+// whose host application owns the GPU memory budget and forbids growing it
+// after start-up, or a frame loop that cannot afford the device-wide
+// synchronisation an allocation may cause. bvhgpu_trace_batches_noalloc
+// serves them: it runs the persistent traversal kernel with its only scratch
+// (one ray-queue head per batch) in the fixed array below, so the call itself
+// allocates nothing; the caller passes the rays and the result buffers.
+//
+// The array is a file-scope device variable: every GPU that loads the library
+// holds its kNoAllocQueueSlots * 8 bytes until the process exits. Host code
+// may not use the symbol as an address, so the device address is looked up
+// once per device with cudaGetSymbolAddress (with that device current) on the
+// first call for that device; make that first call before any stream capture.
+// Every call shares the array and leaves its contents behind: each call clears
+// the heads it uses before its launches, and calls that overlap on the GPU
+// (different streams, or devices sharing nothing but the caller) race on the
+// heads, so serialise them.
+namespace {
+
+constexpr int kNoAllocQueueSlots = 64;  // at most 64 batches per call (512 bytes)
+static __device__ __align__(256) unsigned long long g_noalloc_queue[kNoAllocQueueSlots];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_queue on `device` (which must be current).
+int noalloc_scratch(int device, unsigned long long** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "no-alloc trace: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_queue);
+    if (e != cudaSuccess) return cuda_error(e, "no-alloc trace: cudaGetSymbolAddress");
+    g_noalloc_addr[device] = static_cast<unsigned long long*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return BVHGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches,
+                                 int32_t n_batches, const bvhgpu_trace_opts_t* opts,
+                                 void* stream) {
+  if (n_batches < 0 || n_batches > kNoAllocQueueSlots)
+    return set_error(BVHGPU_ERR_BAD_ARG,
+                     "no-alloc trace: at most 64 batches per call (the fixed scratch holds 64 "
+                     "queue heads)");
+  if (!s || (n_batches > 0 && !batches)) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  dev::LaunchCfg cfg;
+  int rc = check_opts(opts, cfg);
+  if (rc) return rc;
+  cfg.scheme = BVHGPU_PERSISTENT;
+  for (int i = 0; i < n_batches; ++i) {
+    const bvhgpu_batch_t& b = batches[i];
+    if (b.kind != BVHGPU_CLOSEST && b.kind != BVHGPU_ANY)
+      return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: batch kind");
+    if (b.n == 0) continue;
+    if (!b.rays || ((uintptr_t)b.rays & 15))
+      return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: rays null or not 16-byte aligned");
+    if (b.kind == BVHGPU_CLOSEST ? (!b.hits || ((uintptr_t)b.hits & 15)) : !b.occluded)
+      return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: result buffer null or misaligned");
+  }
+  if ((size_t)s->max_stack * 128 * 4 > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  if (n_batches == 0) return BVHGPU_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  unsigned long long* heads = nullptr;
+  if ((rc = noalloc_scratch(s->device, &heads))) return rc;
+  // The heads keep the previous call's values: clear the ones this call uses.
+  e = cudaMemsetAsync(heads, 0, sizeof(unsigned long long) * (size_t)n_batches, st);
+  if (e != cudaSuccess) return cuda_error(e, "no-alloc trace: clear queue heads");
+  const dev::SceneDev sc = s->dev_view();
+  for (int i = 0; i < n_batches; ++i) {
+    const bvhgpu_batch_t& b = batches[i];
+    if (b.n == 0) continue;
+    dev::TraceArgs a;
+    a.rays = b.rays;
+    a.n = b.n;
+    a.hits = b.kind == BVHGPU_CLOSEST ? b.hits : nullptr;
+    a.occluded = b.kind == BVHGPU_ANY ? b.occluded : nullptr;
+    a.counters = nullptr;
+    a.depth_hist = nullptr;
+    a.stack_cap = s->max_stack;
+    dev::LaunchCfg c = cfg;
+    c.kind = b.kind;
+    c.count = false;
+    c.sm_count = s->sm_count;
+    c.queue = heads + i;
+    c.queue_cleared = true;
+    switch (s->layout.node_stride) {
+      case 4: e = dev::launch_trace_n4(sc, a, c, st); break;
+      case 8: e = dev::launch_trace_n8(sc, a, c, st); break;
+      case 12: e = dev::launch_trace_n12(sc, a, c, st); break;
+      case 16: e = dev::launch_trace_n16(sc, a, c, st); break;
+      default: return set_error(BVHGPU_ERR_UNSUPPORTED, "node width");
+    }
+    if (e != cudaSuccess) return cuda_error(e, "no-alloc trace launch");
+  }
+  return BVHGPU_OK;
+}
+
 }  // extern "C"

@@ -16,7 +16,8 @@ struct LaunchCfg {
   int packet = 256;     // stream scheme rays per block
   int policy = 0;       // persistent scheme: 0 while-while, 1 if-if
   int refill_min = 8;   // persistent scheme: idle lanes that trigger a refill
-  unsigned long long* queue = nullptr;  // persistent scheme: zeroed queue head
+  unsigned long long* queue = nullptr;  // persistent scheme: queue head
+  bool queue_cleared = false;  // true: the caller zeroed the head already
   int sm_count = 152;
 };
 
@@ -53,8 +54,10 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     const uint64_t need = (a.n + bs - 1) / bs;
     if (grid > need) grid = need;
     QueueArgs q{cfg.queue, cfg.refill_min};
-    e = cudaMemsetAsync(cfg.queue, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
+    if (!cfg.queue_cleared) {
+      e = cudaMemsetAsync(cfg.queue, 0, sizeof(unsigned long long), s);
+      if (e != cudaSuccess) return e;
+    }
     k<<<(unsigned)grid, bs, smem, s>>>(sc, a, q);
   } else {
     const int p = cfg.packet;

@@ -207,6 +207,30 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t scene, float* fastrays, uint64_t n,
 int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t scene, const float* fastrays, uint64_t n,
                                         int32_t scheme, uint16_t* result, void* stream);
 
+/* ---- tracing without allocation --------------------------------------- */
+/* No counterpart in the reference (its renderer allocates nothing on a GPU).
+ * For callers that must not allocate GPU memory while they trace (a plugin
+ * whose host application owns the memory budget, a frame loop that cannot
+ * take the synchronisation an allocation may cause): traces up to 64 ray
+ * batches with the persistent kernel, whose scratch (one ray-queue head per
+ * batch) lives in a fixed 512-byte device array inside the library instead of
+ * being allocated. More than 64 batches -> BVHGPU_ERR_BAD_ARG. The first call
+ * on a device looks up that array's address (make it before any stream
+ * capture). All calls share the array: calls that overlap on the GPU race.
+ * opts: profile, policy and refill are used; scheme is always persistent. */
+typedef struct {
+  const bvhgpu_ray_t* rays; /* device, 16-byte aligned */
+  uint64_t n;
+  int32_t kind;             /* BVHGPU_CLOSEST or BVHGPU_ANY */
+  int32_t pad;
+  bvhgpu_hit_t* hits;       /* closest: device, n records, 16-byte aligned */
+  uint8_t* occluded;        /* any: device, n bytes */
+} bvhgpu_batch_t;
+
+int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t scene, const bvhgpu_batch_t* batches,
+                                 int32_t n_batches, const bvhgpu_trace_opts_t* opts,
+                                 void* stream);
+
 /* Synchronises `stream` and returns the first device-side error recorded by
  * this scene's kernels since the last call (and clears it). */
 int bvhgpu_scene_status(bvhgpu_scene_t scene, void* stream);
