@@ -48,7 +48,10 @@ def parse():
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--ao", type=int, default=8)
-    p.add_argument("--scheme", default="persistent", choices=["per_ray", "stream", "persistent"])
+    p.add_argument("--scheme", default="auto",
+                   choices=["auto", "per_ray", "stream", "persistent"])
+    p.add_argument("--nodes", default="fp32", choices=["fp32", "q8"])
+    p.add_argument("--top-levels", type=int, default=0)
     p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
     p.add_argument("--refill", type=int, default=8, help="persistent: idle lanes per refill")
     p.add_argument("--no-compare", action="store_true",
@@ -238,13 +241,13 @@ def run_ours(a):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     import bvhraytracer_gb300 as pkg
-    from bvhraytracer_gb300 import _native as NAT
+    from bvhraytracer_gb300 import autotune
 
     t_setup = time.time()
     tris, bvh, primary = make_frame(a)
-    scene = pkg.Scene(bvh, device=local)
+    plain = pkg.Scene(bvh, device=local)
     d_primary = torch.from_numpy(primary).to(dev)
-    hits0 = scene.trace(d_primary, profile=a.profile)["hits"]
+    hits0 = plain.trace(d_primary, profile=a.profile)["hits"]
     prims = pkg.hit_prims(hits0.cpu().numpy())
     shadow, ao = secondaries(a, tris, primary, prims)
     d_shadow = torch.from_numpy(shadow).to(dev)
@@ -254,28 +257,43 @@ def run_ours(a):
     out_s = torch.empty(shadow.shape[0], dtype=torch.uint8, device=dev)
     out_a = torch.empty(ao.shape[0], dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-
     batches = [(d_primary, "closest", out_h), (d_shadow, "any", out_s), (d_ao, "any", out_a)]
+    names = ["primary (closest)", "shadow (any)", "AO (any)"]
 
-    opts = {"scheme": a.scheme, "profile": a.profile}
-    if a.scheme == "persistent":
-        opts.update(policy=a.policy, refill=a.refill)
+    # Per-batch configuration: the autotuner's choice, or one fixed scheme.
+    if a.scheme == "auto":
+        plan, scenes = autotune.tune_scene(bvh, [(r, k) for r, k, _ in batches],
+                                           profile=a.profile, reps=2, device=local,
+                                           scenes={("fp32", 0): plain})
+        chosen = [(scenes[lay], dict(opts)) for lay, opts, _ in plan.choices]
+        method = "autotuned per batch: " + "; ".join(
+            f"{n}: {d['layout']} {d['scheme']}" for n, d in zip(names, plan.describe()))
+        plan_desc = plan.describe()
+    else:
+        sc = plain if (a.nodes == "fp32" and a.top_levels == 0) else pkg.Scene(
+            bvh, node_format=a.nodes, top_levels=a.top_levels, device=local)
+        o = {"scheme": a.scheme}
+        if a.scheme == "persistent":
+            o.update(policy=a.policy, refill=a.refill)
+        chosen = [(sc, o)] * 3
+        method = f"{a.scheme} kernel, {a.nodes} nodes, top levels {a.top_levels}"
+        plan_desc = None
 
-    def step(events=None, o=None):
-        o = o or opts
-        for i, (r, kind, out) in enumerate(batches):
+    def step(events=None, cfg=None):
+        cfg = cfg or chosen
+        for i, ((r, kind, out), (sc, o)) in enumerate(zip(batches, cfg)):
             if events is not None:
                 events[i][0].record(stream)
-            scene.trace(r, kind=kind, out=out, **o)
+            sc.trace(r, kind=kind, out=out, profile=a.profile, **o)
             if events is not None:
                 events[i][1].record(stream)
 
-    def frame_ms(o, reps=3):
-        step(None, o)
+    def frame_ms(cfg, reps=3):
+        step(None, cfg)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            step(None, o)
+            step(None, cfg)
         e1.record(stream)
         torch.cuda.synchronize(dev)
         return e0.elapsed_time(e1) / reps
@@ -283,12 +301,13 @@ def run_ours(a):
     # Algorithmic bytes per launch from one counting pass (untimed):
     # node visits x node record bytes + triangle tests x 36 bytes.
     alg = []
-    for r, kind, _ in batches:
-        c = scene.trace(r, kind=kind, counters=True, **opts)
+    for (r, kind, _), (sc, o) in zip(batches, chosen):
+        c = sc.trace(r, kind=kind, counters=True, profile=a.profile, **o)
         cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
         alg.append({"node_visits": int(cs[0]), "leaf_visits": int(cs[1]), "tri_tests": int(cs[4]),
-                    "bytes": int(cs[0]) * scene.node_record_bytes + int(cs[4]) * 36})
-    scene.status()
+                    "bytes": int(cs[0]) * sc.node_record_bytes + int(cs[4]) * 36})
+    for sc, _ in chosen:
+        sc.status()
     setup_s = time.time() - t_setup
 
     for _ in range(a.warmup):
@@ -308,16 +327,17 @@ def run_ours(a):
         torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop)
     clocks = clk.summary()
-    scene.status()
-    t = torch.tensor([ms], dtype=torch.float64)
+    for sc, _ in chosen:
+        sc.status()
     if world > 1:
         import torch.distributed as dist
-        tt = t.to(dev)
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     per_kernel_ms = [statistics.mean(e[i][0].elapsed_time(e[i][1]) for e in ev)
                      for i in range(len(batches))]
     value = n_rays * world * a.steps / (ms / 1e3) / 1e6
+    ok = torch.equal(out_h.view(torch.int32), hits0.view(torch.int32))
 
     # End to end through the C-ABI host entry point, pinned host buffers.
     h_rays = [torch.from_numpy(x).pin_memory() for x in (primary, shadow, ao)]
@@ -327,8 +347,9 @@ def run_ours(a):
     kinds = ["closest", "any", "any"]
 
     def e2e_step():
-        for r, o, kind in zip(h_rays, h_out, kinds):
-            scene.trace_host(r.numpy(), kind=kind, out=o.numpy(), stream=stream, **opts)
+        for r, o_buf, kind, (sc, o) in zip(h_rays, h_out, kinds, chosen):
+            sc.trace_host(r.numpy(), kind=kind, out=o_buf.numpy(), stream=stream,
+                          profile=a.profile, **o)
 
     for _ in range(max(1, a.warmup)):
         e2e_step()
@@ -352,15 +373,15 @@ def run_ours(a):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg[dom]["bytes"] / (per_kernel_ms[dom] / 1e3) / 1e9
-    names = ["primary (closest)", "shadow (any)", "AO (any)"]
 
     compare = {}
     if not a.no_compare:
-        variants = {"per_ray": {"scheme": "per_ray"}, "stream": {"scheme": "stream"},
-                    "persistent_while_while": {"scheme": "persistent", "policy": 0, "refill": 8},
-                    "persistent_if_if": {"scheme": "persistent", "policy": 1, "refill": 8}}
-        for name, o in variants.items():
-            compare[name] = frame_ms(dict(o, profile=a.profile))
+        plain_cfg = [(plain, {"scheme": "per_ray"})] * 3
+        compare["plain_per_ray_fp32"] = frame_ms(plain_cfg)
+        compare["stream_fp32_wg16"] = frame_ms([(plain, {"scheme": "stream"})] * 3)
+        compare["persistent_fp32"] = frame_ms([(plain, {"scheme": "persistent"})] * 3)
+        compare["this_method"] = ms / a.steps
+        compare["speedup_vs_plain_per_ray"] = compare["plain_per_ray_fp32"] / (ms / a.steps)
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, tris, bvh, primary, shadow, ao, a.cpu_sample)
@@ -372,18 +393,16 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded clutter scene standing in for the reference's glTF scenes)",
             "config": {
-                "workload": workload_name(a),
-                "method": f"{a.scheme} kernel" + (f" (policy {a.policy}, refill {a.refill})"
-                                                 if a.scheme == "persistent" else "") +
-                          ", FP32 nodes",
-                "ms_per_frame_by_scheme": compare,
+                "workload": workload_name(a), "method": method, "plan": plan_desc,
                 "profile": a.profile, "triangles": int(bvh.info["n_tris"]),
                 "rays_per_step": n_rays, "primary": int(primary.shape[0]),
                 "shadow": int(shadow.shape[0]), "ao": int(ao.shape[0]),
+                "results_equal_plain_kernel": bool(ok),
                 "l2": "inputs larger than L2 (rays ~%d MB per step); BVH stays L2-resident"
                       % (n_rays * 32 // 2**20),
-                "bvh_bytes": {"nodes": scene.node_bytes, "leaves": scene.leaf_bytes},
+                "bvh_bytes": {"nodes_fp32": plain.node_bytes, "leaves": plain.leaf_bytes},
                 "per_kernel_ms": dict(zip(names, per_kernel_ms)),
+                "ms_per_frame_by_method": compare,
                 "setup_s": round(setup_s, 2),
             },
             "roofline": {

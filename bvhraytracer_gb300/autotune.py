@@ -1,0 +1,95 @@
+"""Autotuner: picks, per scene and per ray batch, the traversal configuration
+with the lowest measured time.
+
+Candidates cover the knobs the reference exposes in config.txt (branching
+factor N and leaf size L: a scene is built per (N, L) pair) plus the GPU
+ones: traversal scheme (per-ray, ray-stream with its workgroup size,
+persistent with its refill threshold and divergence policy), node format
+(FP32 / Q8) and how many top levels are staged in shared memory. Every
+candidate gives the same hits (the kernels are bit-exact with one another and
+Q8 keeps hit sets identical), so the choice only changes speed.
+"""
+from __future__ import annotations
+
+import itertools
+from dataclasses import dataclass, field
+
+from . import Bvh, Scene
+
+DEFAULT_OPTIONS = (
+    {"scheme": "per_ray", "block": 128},
+    {"scheme": "per_ray", "block": 64},
+    {"scheme": "stream", "workgroup": 8},
+    {"scheme": "stream", "workgroup": 16},
+    {"scheme": "persistent", "policy": 0, "refill": 8},
+    {"scheme": "persistent", "policy": 0, "refill": 16},
+    {"scheme": "persistent", "policy": 1, "refill": 8},
+)
+DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
+
+
+@dataclass
+class Plan:
+    """Best configuration per batch: (layout, trace options, ms)."""
+    choices: list = field(default_factory=list)
+    table: dict = field(default_factory=dict)
+
+    def describe(self) -> list:
+        return [{"layout": f"{fmt}/top{top}", **opts, "ms": round(ms, 4)}
+                for (fmt, top), opts, ms in self.choices]
+
+
+def _time(scene, rays, kind, opts, profile, reps):
+    import torch
+    st = torch.cuda.current_stream(rays.device)
+    scene.trace(rays, kind=kind, profile=profile, **opts)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        scene.trace(rays, kind=kind, profile=profile, **opts)
+    e1.record(st)
+    torch.cuda.synchronize(rays.device)
+    return e0.elapsed_time(e1) / reps
+
+
+def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFAULT_LAYOUTS,
+               options=DEFAULT_OPTIONS, reps: int = 3, device: int = 0, scenes=None):
+    """Times every (layout, options) candidate on each ``(rays, kind)`` batch
+    (device tensors) and returns (plan, scenes by layout)."""
+    scenes = dict(scenes or {})
+    plan = Plan()
+    for fmt, top in layouts:
+        if (fmt, top) not in scenes:
+            scenes[(fmt, top)] = Scene(bvh, node_format=fmt, top_levels=top, device=device)
+    for bi, (rays, kind) in enumerate(batches):
+        best = None
+        for (lay, sc), opts in itertools.product(scenes.items(), options):
+            if lay[0] != "fp32" and opts["scheme"] == "stream":
+                continue
+            ms = _time(sc, rays, kind, opts, profile, reps)
+            plan.table[(bi, lay, tuple(sorted(opts.items())))] = ms
+            if best is None or ms < best[2]:
+                best = (lay, opts, ms)
+        plan.choices.append(best)
+    return plan, scenes
+
+
+def tune_branching(tris, batches_fn, *, pairs=((4, 4), (4, 8), (8, 4), (8, 8), (16, 4), (16, 8),
+                                              (16, 16)),
+                   profile: str = "instrumented", reps: int = 2, device: int = 0, **kw):
+    """Also picks N and L: builds a BVH per pair, tunes each, returns the pair
+    with the lowest total time. ``batches_fn(scene)`` returns the batches to
+    time for a scene (secondary rays may depend on the primary hits)."""
+    best = None
+    results = {}
+    for n, l in pairs:
+        bvh = Bvh(tris, n, l)
+        scene = Scene(bvh, device=device)
+        batches = batches_fn(scene)
+        plan, scenes = tune_scene(bvh, batches, profile=profile, reps=reps, device=device,
+                                  scenes={("fp32", 0): scene}, **kw)
+        total = sum(ms for _, _, ms in plan.choices)
+        results[(n, l)] = total
+        if best is None or total < best[0]:
+            best = (total, (n, l), bvh, plan, scenes)
+    return best, results

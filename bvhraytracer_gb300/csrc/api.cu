@@ -129,11 +129,23 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   return BVHGPU_OK;
 }
 
+// Shared memory per block for the persistent kernel's copy of the top levels;
+// small enough to keep six blocks per SM next to the traversal stacks.
+constexpr uint32_t kTopStageBytes = 8192;
+
 static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
                   cudaStream_t st) {
   const dev::SceneDev sc = s->dev_view();
   cfg.sm_count = s->sm_count;
   cfg.queue = s->d_queue + (s->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
+  cfg.fmt = s->layout.node_format;
+  if (cfg.scheme == BVHGPU_PERSISTENT) {
+    // Stage the top levels (up to kTopStageBytes) in shared memory.
+    const uint32_t fit = kTopStageBytes / (uint32_t)s->layout.record_bytes;
+    cfg.top_nodes = std::min(s->layout.top_nodes, fit);
+  }
+  if (cfg.scheme == BVHGPU_STREAM && cfg.fmt != BVHGPU_NODES_FP32)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "the stream scheme traverses FP32 nodes only");
   cudaError_t e;
   switch (s->layout.node_stride) {
     case 4: e = dev::launch_trace_n4(sc, a, cfg, st); break;
@@ -274,8 +286,8 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
     return set_error(BVHGPU_ERR_NO_DEVICE, "no CUDA device");
   if (params->device < 0 || params->device >= ndev)
     return set_error(BVHGPU_ERR_BAD_ARG, "device ordinal out of range");
-  if (params->node_format != BVHGPU_NODES_FP32)
-    return set_error(BVHGPU_ERR_UNSUPPORTED, "node format not built yet");
+  if (params->node_format != BVHGPU_NODES_FP32 && params->node_format != BVHGPU_NODES_Q8)
+    return set_error(BVHGPU_ERR_BAD_ARG, "node format");
   auto* s = new (std::nothrow) bvhgpu_scene();
   if (!s) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   s->device = params->device;
@@ -601,6 +613,7 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
     c.sm_count = s->sm_count;
     c.queue = heads + i;
     c.queue_cleared = true;
+    c.fmt = s->layout.node_format;
     switch (s->layout.node_stride) {
       case 4: e = dev::launch_trace_n4(sc, a, c, st); break;
       case 8: e = dev::launch_trace_n8(sc, a, c, st); break;

@@ -254,6 +254,46 @@ BVHGPU_DEV bool moller_trumbore(const float (&p)[3][3], const Ray& r, float tmax
   return hit;
 }
 
+// ---- mbarrier + bulk copy (TMA) helpers, inline PTX (sm_90 and later) ----
+BVHGPU_DEV uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+BVHGPU_DEV void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+BVHGPU_DEV void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Global -> shared bulk copy completing on `bar`; 16-byte aligned addresses,
+// size a multiple of 16.
+BVHGPU_DEV void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Waits for the phase with the given parity to complete; gives up after
+// `limit` polls and returns false.
+BVHGPU_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Read-only global loads.
 BVHGPU_DEV float4 ldg4(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 BVHGPU_DEV uint4 ldgu4(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }

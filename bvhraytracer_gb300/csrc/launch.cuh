@@ -19,6 +19,8 @@ struct LaunchCfg {
   unsigned long long* queue = nullptr;  // persistent scheme: queue head
   bool queue_cleared = false;  // true: the caller zeroed the head already
   int sm_count = 152;
+  int fmt = BVHGPU_NODES_FP32;  // node record format of the scene
+  uint32_t top_nodes = 0;       // persistent scheme: inner records staged in shared memory
 };
 
 template <typename K>
@@ -27,23 +29,24 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <int NM, int PROFILE, int KIND, bool COUNT>
+template <int NM, int PROFILE, int KIND, bool COUNT, int FMT>
 inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& cfg,
                               cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   if (cfg.scheme == BVHGPU_PER_RAY) {
     const int bs = cfg.block;
     const size_t smem = (size_t)a.stack_cap * bs * 4;
-    auto k = trace_dfs_kernel<NM, PROFILE, KIND, COUNT>;
+    auto k = trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     const uint64_t grid = (a.n + bs - 1) / bs;
     k<<<(unsigned)grid, bs, smem, s>>>(sc, a);
   } else if (cfg.scheme == BVHGPU_PERSISTENT) {
     const int bs = 128;
-    const size_t smem = (size_t)a.stack_cap * bs * 4;
-    auto k = cfg.policy == 0 ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 0>
-                             : trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 1>;
+    const size_t smem =
+        (size_t)a.stack_cap * bs * 4 + (size_t)cfg.top_nodes * NodeFmt<NM, FMT>::REC;
+    auto k = cfg.policy == 0 ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 0, FMT>
+                             : trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 1, FMT>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -53,13 +56,14 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     uint64_t grid = (uint64_t)per_sm * cfg.sm_count;
     const uint64_t need = (a.n + bs - 1) / bs;
     if (grid > need) grid = need;
-    QueueArgs q{cfg.queue, cfg.refill_min};
+    QueueArgs q{cfg.queue, cfg.refill_min, cfg.top_nodes};
     if (!cfg.queue_cleared) {
       e = cudaMemsetAsync(cfg.queue, 0, sizeof(unsigned long long), s);
       if (e != cudaSuccess) return e;
     }
     k<<<(unsigned)grid, bs, smem, s>>>(sc, a, q);
   } else {
+    if (FMT != kFmtFP32) return cudaErrorNotSupported;
     const int p = cfg.packet;
     const size_t smem = stream_smem_bytes(p, a.stack_cap, COUNT);
     auto k = trace_stream_kernel<NM, PROFILE, KIND, COUNT>;
@@ -71,19 +75,26 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
   return cudaGetLastError();
 }
 
+template <int NM, int PROFILE, int KIND, bool COUNT>
+inline cudaError_t launch_fmt(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& c,
+                              cudaStream_t s) {
+  if (c.fmt == kFmtQ8) return launch_one<NM, PROFILE, KIND, COUNT, kFmtQ8>(sc, a, c, s);
+  return launch_one<NM, PROFILE, KIND, COUNT, kFmtFP32>(sc, a, c, s);
+}
+
 template <int NM>
 inline cudaError_t launch_for_width(const SceneDev& sc, const TraceArgs& a, const LaunchCfg& c,
                                     cudaStream_t s) {
   const int code = (c.profile << 2) | (c.kind << 1) | (c.count ? 1 : 0);
   switch (code) {
-    case 0: return launch_one<NM, 0, 0, false>(sc, a, c, s);
-    case 1: return launch_one<NM, 0, 0, true>(sc, a, c, s);
-    case 2: return launch_one<NM, 0, 1, false>(sc, a, c, s);
-    case 3: return launch_one<NM, 0, 1, true>(sc, a, c, s);
-    case 4: return launch_one<NM, 1, 0, false>(sc, a, c, s);
-    case 5: return launch_one<NM, 1, 0, true>(sc, a, c, s);
-    case 6: return launch_one<NM, 1, 1, false>(sc, a, c, s);
-    case 7: return launch_one<NM, 1, 1, true>(sc, a, c, s);
+    case 0: return launch_fmt<NM, 0, 0, false>(sc, a, c, s);
+    case 1: return launch_fmt<NM, 0, 0, true>(sc, a, c, s);
+    case 2: return launch_fmt<NM, 0, 1, false>(sc, a, c, s);
+    case 3: return launch_fmt<NM, 0, 1, true>(sc, a, c, s);
+    case 4: return launch_fmt<NM, 1, 0, false>(sc, a, c, s);
+    case 5: return launch_fmt<NM, 1, 0, true>(sc, a, c, s);
+    case 6: return launch_fmt<NM, 1, 1, false>(sc, a, c, s);
+    case 7: return launch_fmt<NM, 1, 1, true>(sc, a, c, s);
   }
   return cudaErrorInvalidValue;
 }

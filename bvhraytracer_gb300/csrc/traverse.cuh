@@ -48,14 +48,38 @@ struct Counters {
 };
 
 constexpr int round4(int n) { return (n + 3) / 4 * 4; }
-template <int N>
+
+// Node record formats (the byte layouts are written by build_device_layout).
+constexpr int kFmtFP32 = BVHGPU_NODES_FP32;
+constexpr int kFmtQ8 = BVHGPU_NODES_Q8;
+
+template <int N, int FMT = kFmtFP32>
 struct NodeFmt {
   static constexpr int NM = round4(N);
-  static constexpr int REC = ((28 * NM + 12) + 15) / 16 * 16;
-  static constexpr int META = 24 * NM;            // byte offset of the metadata
-  static constexpr int ORDER = META + 12;         // order[3][NM]
-  static constexpr int LCNT = ORDER + 3 * NM;     // leaf_cnt[NM]
+  // FP32: float box[6][NM] | meta (12 B) | order[3][NM] | leaf_cnt[NM]
+  // Q8:   origin (3 f32) + exp (3 i8) | meta | order | leaf_cnt | q[6][NM]
+  static constexpr int META = FMT == kFmtFP32 ? 24 * NM : 16;
+  static constexpr int ORDER = META + 12;
+  static constexpr int LCNT = ORDER + 3 * NM;
+  static constexpr int QBOX = 32 + 4 * NM;
+  static constexpr int REC = FMT == kFmtFP32 ? ((28 * NM + 12) + 15) / 16 * 16
+                                             : ((32 + 10 * NM) + 15) / 16 * 16;
 };
+
+// Loads from a node record, either in global memory (read-only path) or in
+// the block's shared-memory copy of the top levels (generic loads).
+template <bool SH> BVHGPU_DEV uint4 rec_u4(const uint8_t* p) {
+  if (SH) return *reinterpret_cast<const uint4*>(p);
+  return ldgu4(p);
+}
+template <bool SH> BVHGPU_DEV float4 rec_f4(const uint8_t* p) {
+  if (SH) return *reinterpret_cast<const float4*>(p);
+  return ldg4(p);
+}
+template <bool SH> BVHGPU_DEV uint32_t rec_u32(const uint8_t* p) {
+  if (SH) return *reinterpret_cast<const uint32_t*>(p);
+  return ldgu(p);
+}
 
 // Byte i (0 <= i < 16) of a little-endian 16-byte group held as two words.
 BVHGPU_DEV int byte_at(uint64_t lo, uint64_t hi, int i) {
@@ -63,38 +87,78 @@ BVHGPU_DEV int byte_at(uint64_t lo, uint64_t hi, int i) {
   return (int)((w >> ((i & 7) * 8)) & 0xFFu);
 }
 
-template <int NM>
+template <int NM, bool SH>
 BVHGPU_DEV void load_bytes(const uint8_t* p, uint64_t& lo, uint64_t& hi) {
   // NM bytes at a 4-byte aligned address.
-  uint32_t w0 = ldgu(p), w1 = NM > 4 ? ldgu(p + 4) : 0u;
-  uint32_t w2 = NM > 8 ? ldgu(p + 8) : 0u, w3 = NM > 12 ? ldgu(p + 12) : 0u;
+  uint32_t w0 = rec_u32<SH>(p), w1 = NM > 4 ? rec_u32<SH>(p + 4) : 0u;
+  uint32_t w2 = NM > 8 ? rec_u32<SH>(p + 8) : 0u, w3 = NM > 12 ? rec_u32<SH>(p + 12) : 0u;
   lo = (uint64_t)w0 | ((uint64_t)w1 << 32);
   hi = (uint64_t)w2 | ((uint64_t)w3 << 32);
 }
 
+// 2^e for a normal exponent e (-126 <= e <= 127).
+BVHGPU_DEV float exp2i(int e) { return __int_as_float((e + 127) << 23); }
+
+// Four children's Q8 coordinates of one row: origin + q * step, rounded
+// down (lower bounds) or up (upper bounds). q * step is exact (q < 256,
+// step a power of two), so the decoded box contains the original one.
+BVHGPU_DEV float4 q8_row(uint32_t w, float origin, float step, bool up) {
+  float4 v;
+  const float a = (float)(w & 0xFFu) * step, b = (float)((w >> 8) & 0xFFu) * step;
+  const float c = (float)((w >> 16) & 0xFFu) * step, d = (float)(w >> 24) * step;
+  if (up) {
+    v.x = __fadd_ru(origin, a); v.y = __fadd_ru(origin, b);
+    v.z = __fadd_ru(origin, c); v.w = __fadd_ru(origin, d);
+  } else {
+    v.x = __fadd_rd(origin, a); v.y = __fadd_rd(origin, b);
+    v.z = __fadd_rd(origin, c); v.w = __fadd_rd(origin, d);
+  }
+  return v;
+}
+
 // One inner-node visit: slab-test the children and push the hits.
 // Returns false on stack overflow.
-template <int N, int PROFILE, int KIND, bool COUNT, bool MM>
-BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r, float tmax,
-                           uint32_t* stack, int stride, int& sp, int cap, Counters& ctr,
-                           int& depth_out) {
-  using F = NodeFmt<N>;
+template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH>
+BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
+                           int stride, int& sp, int cap, Counters& ctr, int& depth_out) {
+  using F = NodeFmt<N, FMT>;
   constexpr int NM = F::NM;
-  const uint4 meta = ldgu4(rec + F::META);
+  const uint4 meta = rec_u4<SH>(rec + F::META);
   const uint32_t inner_base = meta.x, leaf_base = meta.y;
   const uint32_t leaf_mask = meta.z & 0xFFFFu;
   const int count = (int)((meta.z >> 16) & 0xFFu);
   depth_out = (int)(meta.z >> 24);
 
+  float ox = 0.f, oy = 0.f, oz = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+  if (FMT == kFmtQ8) {
+    const uint4 h = rec_u4<SH>(rec);
+    ox = __uint_as_float(h.x);
+    oy = __uint_as_float(h.y);
+    oz = __uint_as_float(h.z);
+    sx = exp2i((int)(int8_t)(h.w & 0xFFu));
+    sy = exp2i((int)(int8_t)((h.w >> 8) & 0xFFu));
+    sz = exp2i((int)(int8_t)((h.w >> 16) & 0xFFu));
+  }
   uint32_t hit = 0;
 #pragma unroll
   for (int q = 0; q < NM / 4; ++q) {
-    const float4 lx = ldg4(rec + (0 * NM + 4 * q) * 4);
-    const float4 ly = ldg4(rec + (1 * NM + 4 * q) * 4);
-    const float4 lz = ldg4(rec + (2 * NM + 4 * q) * 4);
-    const float4 hx = ldg4(rec + (3 * NM + 4 * q) * 4);
-    const float4 hy = ldg4(rec + (4 * NM + 4 * q) * 4);
-    const float4 hz = ldg4(rec + (5 * NM + 4 * q) * 4);
+    float4 lx, ly, lz, hx, hy, hz;
+    if (FMT == kFmtFP32) {
+      lx = rec_f4<SH>(rec + (0 * NM + 4 * q) * 4);
+      ly = rec_f4<SH>(rec + (1 * NM + 4 * q) * 4);
+      lz = rec_f4<SH>(rec + (2 * NM + 4 * q) * 4);
+      hx = rec_f4<SH>(rec + (3 * NM + 4 * q) * 4);
+      hy = rec_f4<SH>(rec + (4 * NM + 4 * q) * 4);
+      hz = rec_f4<SH>(rec + (5 * NM + 4 * q) * 4);
+    } else {
+      const uint8_t* qb = rec + F::QBOX + 4 * q;
+      lx = q8_row(rec_u32<SH>(qb + 0 * NM), ox, sx, false);
+      ly = q8_row(rec_u32<SH>(qb + 1 * NM), oy, sy, false);
+      lz = q8_row(rec_u32<SH>(qb + 2 * NM), oz, sz, false);
+      hx = q8_row(rec_u32<SH>(qb + 3 * NM), ox, sx, true);
+      hy = q8_row(rec_u32<SH>(qb + 4 * NM), oy, sy, true);
+      hz = q8_row(rec_u32<SH>(qb + 5 * NM), oz, sz, true);
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (4 * q + k < N) {
@@ -113,7 +177,7 @@ BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r,
   if (hit == 0) return true;
 
   uint64_t clo, chi;
-  load_bytes<NM>(rec + F::LCNT, clo, chi);
+  load_bytes<NM, SH>(rec + F::LCNT, clo, chi);
   auto entry = [&](int c) -> uint32_t {
     const uint32_t below = (1u << c) - 1u;
     if ((leaf_mask >> c) & 1u) {
@@ -134,7 +198,7 @@ BVHGPU_DEV bool visit_node(const SceneDev& sc, const uint8_t* rec, const Ray& r,
     }
   } else {
     uint64_t olo, ohi;
-    load_bytes<NM>(rec + F::ORDER + r.code * NM, olo, ohi);
+    load_bytes<NM, SH>(rec + F::ORDER + r.code * NM, olo, ohi);
     for (int k = 0; k < count; ++k) {
       const int i = r.reverse ? k : count - 1 - k;
       const int c = byte_at(olo, ohi, i);
@@ -254,15 +318,27 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
 }
 
 // Visits with the IEEE min / max forms unless the ray can produce a NaN.
-template <int N, int PROFILE, int KIND, bool COUNT>
-BVHGPU_DEV bool node_step(const SceneDev& sc, const uint8_t* rec, const Ray& r, float tmax,
-                          uint32_t* stack, int stride, int& sp, int cap, Counters& ctr,
-                          int& depth) {
+// Node e is read from the block's shared copy of the top levels when e <
+// top (top == 0: all nodes from global memory).
+template <int N, int PROFILE, int KIND, bool COUNT, int FMT>
+BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_smem, uint32_t top,
+                          const Ray& r, float tmax, uint32_t* stack, int stride, int& sp, int cap,
+                          Counters& ctr, int& depth) {
+  constexpr int REC = NodeFmt<N, FMT>::REC;
+  if (e < top) {
+    const uint8_t* rec = top_smem + (size_t)e * REC;
+    if (r.exact)
+      return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true>(rec, r, tmax, stack, stride,
+                                                                   sp, cap, ctr, depth);
+    return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true>(rec, r, tmax, stack, stride, sp,
+                                                                cap, ctr, depth);
+  }
+  const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
-    return visit_node<N, PROFILE, KIND, COUNT, false>(sc, rec, r, tmax, stack, stride, sp, cap,
-                                                      ctr, depth);
-  return visit_node<N, PROFILE, KIND, COUNT, true>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
-                                                   depth);
+    return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false>(rec, r, tmax, stack, stride, sp,
+                                                                  cap, ctr, depth);
+  return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false>(rec, r, tmax, stack, stride, sp,
+                                                               cap, ctr, depth);
 }
 
 template <int PROFILE, int KIND, bool COUNT>
@@ -324,7 +400,7 @@ BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t ri
 // ---------------------------------------------------------------------------
 // Per-ray depth-first traversal: one thread per ray, the traversal stack in
 // shared memory (stack[slot][thread], conflict-free across a warp).
-template <int N, int PROFILE, int KIND, bool COUNT>
+template <int N, int PROFILE, int KIND, bool COUNT, int FMT>
 __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a) {
   extern __shared__ uint32_t smem[];
   const int stride = blockDim.x;
@@ -362,10 +438,9 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
         if (KIND == BVHGPU_ANY) break;
       }
     } else {
-      const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
       int depth;
-      if (!node_step<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stack, stride, sp, cap, ctr,
-                                              depth)) {
+      if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, nullptr, 0u, r, tmax, stack, stride, sp,
+                                                   cap, ctr, depth)) {
         record_error(sc.status, kDevErrStackOverflow);
         hit = false;
         best = Best();
@@ -518,10 +593,9 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       --sp;
       const uint32_t e = stacks[sp * P + ray];
       if (is_node) {
-        const uint8_t* rec = sc.nodes + (size_t)e * NodeFmt<N>::REC;
         int depth;
-        if (!node_step<N, PROFILE, KIND, COUNT>(sc, rec, r, tmax, stacks + ray, P, sp, cap, ctr,
-                                                depth)) {
+        if (!node_step<N, PROFILE, KIND, COUNT, kFmtFP32>(sc, e, nullptr, 0u, r, tmax, stacks + ray,
+                                                          P, sp, cap, ctr, depth)) {
           record_error(sc.status, kDevErrStackOverflow);
           best_leaf[ray] = 0xFFFFFFFFu;
           misc = 0xFF;
@@ -630,17 +704,38 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
 struct QueueArgs {
   unsigned long long* head;  // next unclaimed ray (zeroed before the launch)
   int refill_min;            // refill when at least this many lanes are idle
+  uint32_t top_nodes;        // inner records staged in shared memory (0: none)
 };
 
 #ifndef BVHGPU_PERSIST_MIN_BLOCKS
-#define BVHGPU_PERSIST_MIN_BLOCKS 1
+#define BVHGPU_PERSIST_MIN_BLOCKS 6
 #endif
-template <int N, int PROFILE, int KIND, bool COUNT, int POLICY>
+template <int N, int PROFILE, int KIND, bool COUNT, int POLICY, int FMT>
 __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
     trace_persistent_kernel(SceneDev sc, TraceArgs a, QueueArgs q) {
-  extern __shared__ uint32_t smem[];
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint64_t top_bar;
   const int stride = blockDim.x;
   uint32_t* stack = smem + threadIdx.x;
+  // The first q.top_nodes inner records (the top levels, laid out first) are
+  // copied into shared memory once per block with one bulk (TMA) copy.
+  uint8_t* top_smem = reinterpret_cast<uint8_t*>(smem + (size_t)a.stack_cap * stride);
+  const uint32_t top = q.top_nodes;
+  if (top > 0) {
+    const uint32_t bytes = top * (uint32_t)NodeFmt<N, FMT>::REC;
+    if (threadIdx.x == 0) mbar_init(&top_bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(&top_bar, bytes);
+      for (uint32_t off = 0; off < bytes; off += 32768u)
+        bulk_copy_g2s(top_smem + off, sc.nodes + off, min(32768u, bytes - off), &top_bar);
+    }
+    if (!mbar_wait(&top_bar, 0, 1u << 24)) {
+      record_error(sc.status, kDevErrTimeout);
+      mbar_wait(&top_bar, 0, 1u << 24);  // let the copy land before the block exits
+      return;
+    }
+  }
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   const int cap = a.stack_cap;
@@ -701,8 +796,8 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
           --sp;
           const uint32_t e = stack[sp * stride];
           int depth;
-          if (!node_step<N, PROFILE, KIND, COUNT>(sc, sc.nodes + (size_t)e * NodeFmt<N>::REC, r,
-                                                  tmax, stack, stride, sp, cap, ctr, depth)) {
+          if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, top_smem, top, r, tmax, stack,
+                                                       stride, sp, cap, ctr, depth)) {
             record_error(sc.status, kDevErrStackOverflow);
             hit = false;
             best = Best();
@@ -735,8 +830,8 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
           }
         } else {
           int depth;
-          if (!node_step<N, PROFILE, KIND, COUNT>(sc, sc.nodes + (size_t)e * NodeFmt<N>::REC, r,
-                                                  tmax, stack, stride, sp, cap, ctr, depth)) {
+          if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, top_smem, top, r, tmax, stack,
+                                                       stride, sp, cap, ctr, depth)) {
             record_error(sc.status, kDevErrStackOverflow);
             hit = false;
             best = Best();

@@ -234,6 +234,12 @@ def test_full_size_clutter_properties():
     close = scene.trace(da)["hits"]
     assert torch.equal(occ.bool(), close.view(torch.int32)[:, 0] >= 0)
     scene.status()
+    # Q8 nodes with the top levels staged in shared memory: identical hits.
+    q8 = pkg.Scene(b, node_format="q8", top_levels=2)
+    assert torch.equal(q8.trace(d, scheme="persistent")["hits"].view(torch.int32),
+                       a.view(torch.int32))
+    assert torch.equal(q8.trace(da, kind="any", scheme="persistent")["occluded"], occ)
+    q8.status()
 
 
 def _fastrays(rays):
@@ -277,3 +283,33 @@ def test_fastray_drop_in(terrain, scheme):
                                                         scheme, res.ctypes.data, None))
     occ = O.trace_fast(fv, cv, ao, any_hit=True)["occluded"]
     assert np.array_equal(res, 3 + occ.astype(np.uint16))
+
+
+@pytest.mark.parametrize("n,l", [(4, 4), (8, 8), (16, 16), (8, 4), (12, 8)])
+def test_q8_nodes_keep_hits_identical(n, l):
+    """8-bit child boxes relative to the parent box, rounded outward: the
+    hit sets (and every closest-hit record) equal the FP32 nodes' and the
+    oracle's; node bytes shrink."""
+    tris, b, cv = TS.bvh("clutter120", n, l)
+    rays = TS.clutter_rays(tris, res=(96, 64))
+    s32 = pkg.Scene(b)
+    s8 = pkg.Scene(b, node_format="q8", top_levels=2)
+    assert s8.node_bytes < s32.node_bytes
+    for profile in ("instrumented", "fast"):
+        ref = s32.trace(dev(rays), profile=profile)["hits"].cpu().numpy()
+        prims = pkg.hit_prims(ref)
+        sh, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+        ref_a = s32.trace(dev(ao), kind="any", profile=profile)["occluded"].cpu().numpy()
+        for scheme, kw in (("per_ray", {}), ("persistent", {"policy": 0}),
+                           ("persistent", {"policy": 1})):
+            got = s8.trace(dev(rays), scheme=scheme, profile=profile, **kw)["hits"].cpu().numpy()
+            assert np.array_equal(bits(got), bits(ref)), (profile, scheme, _first_diff(got, ref))
+            occ = s8.trace(dev(ao), kind="any", scheme=scheme, profile=profile, **kw)["occluded"]
+            assert np.array_equal(occ.cpu().numpy(), ref_a), (profile, scheme)
+    # counters run on Q8 too (visits may grow: boxes are conservative)
+    c8 = s8.trace(dev(rays), counters=True)["counters"].cpu().numpy()
+    c32 = s32.trace(dev(rays), counters=True)["counters"].cpu().numpy()
+    assert c8[:, 0].sum() >= c32[:, 0].sum()
+    s8.status()
+    with pytest.raises(pkg.BvhgpuError):
+        s8.trace(dev(rays), scheme="stream")
