@@ -297,6 +297,21 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
     delete s;
     return set_error(rc, "device layout failed (gang 4/8, leaf_memory >= L and a gang multiple <= 16)");
   }
+  {
+    // The host layout and the kernels must agree on the record size.
+    const int nm = s->layout.node_stride, fmt = s->layout.node_format;
+    int expect = 0;
+    if (fmt == BVHGPU_NODES_FP32)
+      expect = nm == 4 ? dev::NodeFmt<4, 0>::REC : nm == 8 ? dev::NodeFmt<8, 0>::REC
+             : nm == 12 ? dev::NodeFmt<12, 0>::REC : dev::NodeFmt<16, 0>::REC;
+    else
+      expect = nm == 4 ? dev::NodeFmt<4, 1>::REC : nm == 8 ? dev::NodeFmt<8, 1>::REC
+             : nm == 12 ? dev::NodeFmt<12, 1>::REC : dev::NodeFmt<16, 1>::REC;
+    if (expect != s->layout.record_bytes) {
+      delete s;
+      return set_error(BVHGPU_ERR_UNSUPPORTED, "internal: node record size mismatch");
+    }
+  }
   s->max_stack = h->bvh.max_stack;
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) {

@@ -238,7 +238,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
       rec[12] = (uint8_t)ex[0];
       rec[13] = (uint8_t)ex[1];
       rec[14] = (uint8_t)ex[2];
-      uint8_t* q = rec + 32 + 4 * nm;
+      uint8_t* q = rec + q8_box_offset(nm);
       for (uint32_t j = 0; j < c.child_count; ++j) {
         const CompactNode& ch = bvh.nodes[c.child_begin + j];
         for (int k = 0; k < 3; ++k) {
@@ -265,10 +265,20 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
     std::memcpy(meta + 8, &leaf_mask, 2);
     meta[10] = (uint8_t)c.child_count;
     meta[11] = c.depth;
-    uint8_t* order = meta + 12;
-    for (int a = 0; a < 3; ++a)
-      for (size_t i = 0; i < bn->order[a].size(); ++i) order[a * nm + i] = (uint8_t)bn->order[a][i];
-    uint8_t* lcnt = meta + 12 + 3 * nm;
+    // Push sequences per axis and direction, one child per nibble.
+    const int wb = perm_word_bytes(nm);
+    uint8_t* perm = meta + 12;
+    for (int a = 0; a < 3; ++a) {
+      const size_t c_n = bn->order[a].size();
+      uint64_t up = 0, down = 0;
+      for (size_t k = 0; k < c_n; ++k) {
+        up |= (uint64_t)(uint8_t)bn->order[a][k] << (4 * k);
+        down |= (uint64_t)(uint8_t)bn->order[a][c_n - 1 - k] << (4 * k);
+      }
+      std::memcpy(perm + (a * 2 + 0) * wb, &up, wb);
+      std::memcpy(perm + (a * 2 + 1) * wb, &down, wb);
+    }
+    uint8_t* lcnt = meta + 12 + 6 * wb;
     for (uint32_t j = 0; j < c.child_count; ++j) {
       const CompactNode& ch = bvh.nodes[c.child_begin + j];
       lcnt[j] = ch.child_count == 0 ? (uint8_t)ch.prim_count : 0;

@@ -28,7 +28,12 @@ int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, Fast
 //   uint16   leaf_mask      bit j: child j is a leaf
 //   uint8    count          number of children
 //   uint8    depth          tree depth of this node
-//   uint8    order[3][Nm]   traverseOrderEachAxis
+//   perm[3][2]              traverseOrderEachAxis as push sequences: for axis a,
+//                           perm[a][0] pushes order[a][0], order[a][1], ...
+//                           (direction[a] <= 0) and perm[a][1] pushes
+//                           order[a][count-1], ..., order[a][0]; one child index
+//                           per 4-bit nibble, first push in the low nibble;
+//                           each word is perm_word_bytes(Nm) bytes
 //   uint8    leaf_cnt[Nm]   triangles of leaf child j (0 for inner children)
 // Leaves are not given node records: leaf k is the k-th leaf of the
 // reference's customTreeOrder and its triangle block is exactly the
@@ -39,11 +44,13 @@ int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, Fast
 // Q8 record (branching N, Nm as above), 16-byte aligned:
 //   float    origin[3]      parent box lower corner (the quantisation frame)
 //   int8     exp[3], pad    per-axis power-of-two step: step = 2^exp
-//   uint32   inner_base, leaf_base
-//   uint16   leaf_mask; uint8 count; uint8 depth
-//   uint8    order[3][Nm]; uint8 leaf_cnt[Nm]
-//   uint8    q[6][Nm]       child boxes: lo = origin + q_lo*step (rounded
-//                           down), hi = origin + q_hi*step (rounded up)
+//   uint32   inner_base, leaf_base; uint16 leaf_mask; uint8 count; uint8 depth
+//   perm[3][2]; uint8 leaf_cnt[Nm]  (as above)
+//   uint8    q[6][Nm]       child boxes at q8_box_offset: lo = origin + q_lo*step
+//                           (rounded down), hi = origin + q_hi*step (rounded up)
+inline int perm_word_bytes(int nm) { return nm <= 4 ? 2 : (nm <= 8 ? 4 : 8); }
+inline int fp32_meta_offset(int nm) { return 24 * nm; }
+inline int q8_box_offset(int nm) { return (28 + 6 * perm_word_bytes(nm) + nm + 3) / 4 * 4; }
 struct DeviceLayout {
   int branching = 4, node_stride = 4, leaf_memory = 4, gang = 4;
   int node_format = 0;
@@ -62,8 +69,10 @@ constexpr int kLeafCountShift = 27;
 constexpr uint32_t kLeafIndexMask = (1u << 27) - 1;
 
 inline int round_up(int v, int m) { return ((v + m - 1) / m) * m; }
-inline int fp32_record_bytes(int nm) { return round_up(28 * nm + 12, 16); }
-inline int q8_record_bytes(int nm) { return round_up(32 + 4 * nm + 6 * nm, 16); }
+inline int fp32_record_bytes(int nm) {
+  return round_up(24 * nm + 12 + 6 * perm_word_bytes(nm) + nm, 16);
+}
+inline int q8_record_bytes(int nm) { return round_up(q8_box_offset(nm) + 6 * nm, 16); }
 
 int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_format,
                         int top_levels, DeviceLayout& out);

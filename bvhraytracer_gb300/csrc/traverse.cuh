@@ -56,14 +56,16 @@ constexpr int kFmtQ8 = BVHGPU_NODES_Q8;
 template <int N, int FMT = kFmtFP32>
 struct NodeFmt {
   static constexpr int NM = round4(N);
-  // FP32: float box[6][NM] | meta (12 B) | order[3][NM] | leaf_cnt[NM]
-  // Q8:   origin (3 f32) + exp (3 i8) | meta | order | leaf_cnt | q[6][NM]
+  // Push-sequence word: one nibble per child.
+  static constexpr int PW = NM <= 4 ? 2 : (NM <= 8 ? 4 : 8);
+  // FP32: float box[6][NM] | meta (12 B) | perm[3][2] | leaf_cnt[NM]
+  // Q8:   origin (3 f32) + exp (3 i8) | meta | perm | leaf_cnt | q[6][NM]
   static constexpr int META = FMT == kFmtFP32 ? 24 * NM : 16;
-  static constexpr int ORDER = META + 12;
-  static constexpr int LCNT = ORDER + 3 * NM;
-  static constexpr int QBOX = 32 + 4 * NM;
-  static constexpr int REC = FMT == kFmtFP32 ? ((28 * NM + 12) + 15) / 16 * 16
-                                             : ((32 + 10 * NM) + 15) / 16 * 16;
+  static constexpr int PERM = META + 12;
+  static constexpr int LCNT = PERM + 6 * PW;
+  static constexpr int QBOX = (28 + 6 * PW + NM + 3) / 4 * 4;
+  static constexpr int REC = FMT == kFmtFP32 ? ((24 * NM + 12 + 6 * PW + NM) + 15) / 16 * 16
+                                             : ((QBOX + 6 * NM) + 15) / 16 * 16;
 };
 
 // Loads from a node record, either in global memory (read-only path) or in
@@ -187,27 +189,35 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
     }
     return inner_base + (uint32_t)__popc(~leaf_mask & below);
   };
-  const bool index_order = (PROFILE == BVHGPU_PROFILE_FAST && KIND == BVHGPU_ANY);
-  if (index_order) {
-    for (int c = 0; c < count; ++c) {
-      if ((hit >> c) & 1u) {
-        if (sp >= cap) return false;
-        stack[sp * stride] = entry(c);
-        ++sp;
-      }
-    }
+  // Push sequence: child-index order for fast any-hit rays
+  // (fastNodeManager.h:1481-1488), else traverseOrderEachAxis[code] in the
+  // ray's direction.
+  uint64_t perm;
+  if (PROFILE == BVHGPU_PROFILE_FAST && KIND == BVHGPU_ANY) {
+    perm = 0xFEDCBA9876543210ull;
   } else {
-    uint64_t olo, ohi;
-    load_bytes<NM, SH>(rec + F::ORDER + r.code * NM, olo, ohi);
-    for (int k = 0; k < count; ++k) {
-      const int i = r.reverse ? k : count - 1 - k;
-      const int c = byte_at(olo, ohi, i);
-      if ((hit >> c) & 1u) {
-        if (sp >= cap) return false;
-        stack[sp * stride] = entry(c);
-        ++sp;
-      }
+    const uint8_t* pp = rec + F::PERM + (r.code * 2 + (r.reverse ? 0 : 1)) * F::PW;
+    if (F::PW == 2) {
+      perm = rec_u32<SH>(pp - ((uintptr_t)pp & 2)) >> (((uintptr_t)pp & 2) * 8);
+      perm &= 0xFFFFull;
+    } else if (F::PW == 4) {
+      perm = rec_u32<SH>(pp);
+    } else {
+      perm = (uint64_t)rec_u32<SH>(pp) | ((uint64_t)rec_u32<SH>(pp + 4) << 32);
     }
+  }
+  // Positions in the push sequence whose child was hit.
+  uint32_t pm = 0;
+#pragma unroll
+  for (int k = 0; k < NM; ++k) pm |= ((hit >> (uint32_t)((perm >> (4 * k)) & 15u)) & 1u) << k;
+  pm &= (1u << count) - 1u;
+  while (pm) {
+    const int k = __ffs(pm) - 1;
+    pm &= pm - 1u;
+    const int c = (int)((perm >> (4 * k)) & 15u);
+    if (sp >= cap) return false;
+    stack[sp * stride] = entry(c);
+    ++sp;
   }
   return true;
 }
