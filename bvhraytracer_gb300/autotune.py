@@ -24,6 +24,8 @@ DEFAULT_OPTIONS = (
     {"scheme": "persistent", "policy": 0, "refill": 8},
     {"scheme": "persistent", "policy": 0, "refill": 16},
     {"scheme": "persistent", "policy": 1, "refill": 8},
+    {"scheme": "persistent", "policy": 2, "refill": 8},
+    {"scheme": "persistent", "policy": 2, "refill": 16},
 )
 DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
 

@@ -710,7 +710,8 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
 // POLICY 0 ("while-while"): each round, lanes whose stack top is an inner node
 // visit nodes until every active lane has a leaf on top, then all of them
 // visit their leaf together. POLICY 1 ("if-if"): one node or leaf visit per
-// lane per round.
+// lane per round. POLICY 2: while-while with leaves set aside (speculative
+// traversal) for any-hit rays without counters.
 struct QueueArgs {
   unsigned long long* head;  // next unclaimed ray (zeroed before the launch)
   int refill_min;            // refill when at least this many lanes are idle
@@ -759,6 +760,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
   int sp = 0;
   uint64_t rid = 0;
   bool drained = false;
+  uint32_t postponed = 0xFFFFFFFFu;  // POLICY 2: leaf set aside
 
   while (true) {
     const unsigned idle = __ballot_sync(FULL, !active);
@@ -796,7 +798,44 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
       continue;
     }
 
-    if (POLICY == 0) {
+    if (POLICY == 2) {
+      // Any-hit rays without counters: a lane that reaches a leaf sets it
+      // aside and keeps visiting nodes until every lane holds a leaf (or has
+      // no node left); then all lanes test their leaf together. Whether an
+      // any-hit ray is occluded does not depend on the order in which its
+      // reachable leaves are tested (tMax does not change), so results equal
+      // the depth-first order's.
+      while (true) {
+        if (active && sp > 0 && postponed == 0xFFFFFFFFu &&
+            (stack[(sp - 1) * stride] & kLeafBit) != 0u) {
+          --sp;
+          postponed = stack[sp * stride];
+        }
+        const bool want =
+            active && sp > 0 && (stack[(sp - 1) * stride] & kLeafBit) == 0u;
+        const unsigned holding = __ballot_sync(FULL, !active || postponed != 0xFFFFFFFFu);
+        if (__ballot_sync(FULL, want) == 0 || holding == FULL) break;
+        if (want) {
+          --sp;
+          const uint32_t e = stack[sp * stride];
+          int depth;
+          if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, top_smem, top, r, tmax, stack,
+                                                       stride, sp, cap, ctr, depth)) {
+            record_error(sc.status, kDevErrStackOverflow);
+            hit = false;
+            sp = 0;
+            postponed = 0xFFFFFFFFu;
+          }
+        }
+      }
+      if (active && postponed != 0xFFFFFFFFu) {
+        if (leaf_step<PROFILE, KIND, COUNT>(sc, postponed, r, tmax, best, ctr)) {
+          hit = true;
+          sp = 0;
+        }
+        postponed = 0xFFFFFFFFu;
+      }
+    } else if (POLICY == 0) {
       // Node visits until every active lane has a leaf on top (or is done).
       while (true) {
         const bool want =
@@ -852,7 +891,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
         }
       }
     }
-    if (active && sp == 0) {
+    if (active && sp == 0 && postponed == 0xFFFFFFFFu) {
       write_result<KIND>(sc, a, rid, hit, tmax, best);
       flush_counters<COUNT>(a, rid, ctr);
       active = false;

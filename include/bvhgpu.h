@@ -167,7 +167,8 @@ typedef struct {
   int32_t profile;   /* BVHGPU_PROFILE_* */
   int32_t workgroup; /* stream scheme: packet = workgroup^2 rays (8, 16); 0 = 16 */
   int32_t block;     /* per-ray scheme: threads per block (32, 64, 128; 0 = 128) */
-  int32_t policy;    /* persistent scheme: 0 while-while, 1 if-if */
+  int32_t policy;    /* persistent scheme: 0 while-while, 1 if-if, 2 while-while with
+                        leaves set aside (any-hit rays without counters; else 0) */
   int32_t refill;    /* persistent scheme: idle lanes of a warp that trigger a refill
                         (1..32; 0 = 8) */
 } bvhgpu_trace_opts_t;

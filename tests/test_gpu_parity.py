@@ -16,8 +16,8 @@ pytestmark = pytest.mark.gpu
 LIGHT = [2.0, 3.0, 2.0]
 # (scheme, extra trace options): every traversal scheme and persistent policy
 SCHEMES = [("per_ray", {}), ("stream", {}), ("persistent", {"policy": 0}),
-           ("persistent", {"policy": 1, "refill": 1})]
-SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1"]
+           ("persistent", {"policy": 1, "refill": 1}), ("persistent", {"policy": 2, "refill": 16})]
+SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1", "persistent_spec"]
 
 
 def dev(a):
@@ -301,7 +301,7 @@ def test_q8_nodes_keep_hits_identical(n, l):
         sh, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
         ref_a = s32.trace(dev(ao), kind="any", profile=profile)["occluded"].cpu().numpy()
         for scheme, kw in (("per_ray", {}), ("persistent", {"policy": 0}),
-                           ("persistent", {"policy": 1})):
+                           ("persistent", {"policy": 1}), ("persistent", {"policy": 2})):
             got = s8.trace(dev(rays), scheme=scheme, profile=profile, **kw)["hits"].cpu().numpy()
             assert np.array_equal(bits(got), bits(ref)), (profile, scheme, _first_diff(got, ref))
             occ = s8.trace(dev(ao), kind="any", scheme=scheme, profile=profile, **kw)["occluded"]
