@@ -62,6 +62,11 @@ def parse():
     p.add_argument("--ref-sample", type=float, default=0.1,
                    help="fraction of the frame traced per step by --impl reference")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="clutter", choices=["clutter", "batch64"],
+                   help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch")
+    p.add_argument("--scenes", type=int, default=64)
+    p.add_argument("--tune-nl", action="store_true",
+                   help="batch64: let the autotuner pick N/L per scene")
     return p.parse_args()
 
 
@@ -427,10 +432,151 @@ def run_ours(a):
         torch.distributed.destroy_process_group()
 
 
+def batch_scenes(a, seed=5):
+    """Scene and ray specs of the multi-scene workload: triangle counts
+    log-uniform in 1k..500k, ray counts log-uniform in 4k..2M split 1:1:4
+    between primary, shadow and AO rays; terrain and clutter alternate."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(a.scenes):
+        t = float(np.exp(rng.uniform(np.log(1e3), np.log(5e5))))
+        r = float(np.exp(rng.uniform(np.log(4e3), np.log(2e6))))
+        specs.append(("terrain" if i % 2 == 0 else "clutter", t, r, i))
+    return specs
+
+
+def make_batch_scene(kind, tris_target, rays_target, i):
+    from bvhraytracer_gb300 import scenes as S
+    n_primary = max(64, int(rays_target / 6))
+    w = max(8, int(round(np.sqrt(n_primary * 16 / 9))))
+    h = max(8, n_primary // w)
+    if kind == "terrain":
+        n = max(4, int(round(np.sqrt(tris_target / 2))))
+        tris = S.terrain(n, seed=100 + i)
+        c = np.array([0.5, 0.0, 0.5])
+        primary = S.camera_rays(c + [0.0, 0.7, 0.9], c, w, h)
+        light = np.array([2.0, 3.0, 2.0], np.float32)
+    else:
+        n_obj = max(1, int(round(tris_target / 250)))
+        tris = S.clutter(n_obj, seed=100 + i)
+        cam, target, light = S.clutter_viewpoints(n_obj, seed=100 + i)
+        primary = S.camera_rays(cam, target, w, h)
+    return tris, primary, light
+
+
+def run_batch(a):
+    """Many scenes of uneven size and ray count in one persistent launch
+    (recorded in a CUDA graph) against one plain per-ray launch per batch."""
+    import torch
+    import bvhraytracer_gb300 as pkg
+    from bvhraytracer_gb300 import autotune
+    from bvhraytracer_gb300 import scenes as S
+    dev = torch.device("cuda", 0)
+    t_setup = time.time()
+    scenes, jobs_plain, chosen = [], [], []
+    n_tris = n_rays = 0
+    for kind, tt, rr, i in batch_scenes(a):
+        tris, primary, light = make_batch_scene(kind, tt, rr, i)
+        d_p = torch.from_numpy(primary).to(dev)
+        if a.tune_nl:
+            def batches_fn(scene, d_p=d_p, tris=tris, primary=primary, light=light):
+                h = scene.trace(d_p)["hits"]
+                m, p, n = S.surface(tris, primary, pkg.hit_prims(h.cpu().numpy()))
+                ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris))).to(dev)
+                return [(d_p, "closest"), (ao, "any")]
+            best, _ = autotune.tune_branching(
+                tris, batches_fn, pairs=tuple((n, l) for n in (4, 8, 16) for l in (4, 8, 16)),
+                layouts=(("fp32", 0),), options=({"scheme": "per_ray", "block": 32},
+                                                 {"scheme": "per_ray", "block": 64},
+                                                 {"scheme": "per_ray", "block": 128}),
+                reps=1)
+            _, (bn, bl), bvh, plan, tuned = best
+            scene = tuned[("fp32", 0)]
+            block = plan.choices[0][1]["block"]
+        else:
+            bn, bl, block = a.branching, a.leaf, 128
+            bvh = pkg.Bvh(tris, bn, bl)
+            scene = pkg.Scene(bvh)
+        h = scene.trace(d_p)["hits"]
+        m, p, n = S.surface(tris, primary, pkg.hit_prims(h.cpu().numpy()))
+        sh = torch.from_numpy(S.shadow_rays(p, n, light)).to(dev)
+        ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris), seed=i)).to(dev)
+        for rays, k in ((d_p, "closest"), (sh, "any"), (ao, "any")):
+            out = (torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+                   if k == "closest" else torch.empty(rays.shape[0], dtype=torch.uint8, device=dev))
+            jobs_plain.append((scene, rays, k, out))
+            n_rays += rays.shape[0]
+        scenes.append({"kind": kind, "triangles": int(bvh.info["n_tris"]), "N": bn, "L": bl,
+                       "block": block, "rays": int(d_p.shape[0] + sh.shape[0] + ao.shape[0])})
+        chosen.append(block)
+        n_tris += int(bvh.info["n_tris"])
+    setup_s = time.time() - t_setup
+    stream = torch.cuda.current_stream(dev)
+    blocks = [b for b in chosen for _ in range(3)]
+
+    def sequential():
+        for (scene, rays, k, out), b in zip(jobs_plain, blocks):
+            scene.trace(rays, kind=k, scheme="per_ray", block=b, out=out)
+
+    def batched():
+        pkg.trace_jobs(jobs_plain, policy=2, refill=16)
+
+    def timed(fn, steps):
+        for _ in range(a.warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / steps
+
+    # Reference results of the sequential plain launches, then the batch.
+    sequential()
+    refs = [out.clone() for (_, _, _, out) in jobs_plain]
+    batched()
+    torch.cuda.synchronize(dev)
+    same = all(torch.equal(o.view(torch.uint8), r.view(torch.uint8))
+               for (_, _, _, o), r in zip(jobs_plain, refs))
+    # The batched launch recorded in a CUDA graph.
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        batched()
+    with ClockSampler(0) as clk:
+        ms_graph = timed(g.replay, a.steps)
+    clocks = clk.summary()
+    ms_batched = timed(batched, a.steps)
+    ms_seq = timed(sequential, a.steps)
+    for s_ in {id(j[0]): j[0] for j in jobs_plain}.values():
+        s_.status()
+    line = {
+        "metric": METRIC, "value": n_rays / (ms_graph / 1e3) / 1e6, "unit": METRIC, "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_graph, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded terrain and clutter scenes)",
+        "config": {
+            "workload": f"{a.scenes} scenes in one persistent launch, triangles log-uniform "
+                        f"1k-500k, rays log-uniform 4k-2M (primary:shadow:AO 1:1:4)",
+            "triangles_total": n_tris, "rays_per_step": n_rays, "jobs": len(jobs_plain),
+            "method": "bvhgpu_trace_jobs (speculative any-hit policy) in a CUDA graph",
+            "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,
+            "ms_sequential_plain_launches": ms_seq,
+            "speedup_vs_sequential": ms_seq / ms_graph, "results_identical": bool(same),
+            "autotuned_nl": bool(a.tune_nl), "scenes": scenes, "setup_s": round(setup_s, 1),
+        },
+        "clocks": clocks, "gpu_launches": a.steps,
+    }
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batch64":
+        run_batch(a)
     else:
         run_ours(a)
 

@@ -26,7 +26,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["Bvh", "Scene", "FastNodeManager", "CompactNodeManager", "sah_factor",
+__all__ = ["Bvh", "Scene", "FastNodeManager", "CompactNodeManager", "sah_factor", "trace_jobs",
            "BvhgpuError", "CLOSEST", "ANY", "PER_RAY", "STREAM", "PERSISTENT", "PROFILE_INSTRUMENTED",
            "PROFILE_FAST"]
 
@@ -251,6 +251,30 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+
+def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: int = 16,
+               stream=None) -> None:
+    """Traces many (scene, rays) jobs in one persistent launch.
+
+    ``jobs``: list of ``(scene, rays, kind, out)`` with device tensors (rays
+    ``[n, 8]`` float32; ``out`` ``[n, 4]`` float32 for ``"closest"``, ``[n]``
+    uint8 for ``"any"``); up to 192 jobs, scenes of any N, L and node format.
+    Per-ray results equal :meth:`Scene.trace`'s. Stream-ordered (default:
+    torch's current stream); allocates nothing, so it can be recorded in a
+    CUDA graph.
+    """
+    import torch
+    arr = (N.Job * max(1, len(jobs)))()
+    dev = None
+    for i, (scene, rays, kind, out) in enumerate(jobs):
+        k = _KIND[kind]
+        arr[i] = N.Job(scene.handle, _ptr(rays), rays.shape[0], k, 0,
+                       _ptr(out) if k == N.CLOSEST else None, _ptr(out) if k == N.ANY else None)
+        dev = rays.device
+    o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    N.check(N.lib().bvhgpu_trace_jobs(arr, len(jobs), C.byref(o), C.c_void_p(s.cuda_stream)))
 
 
 def hit_prims(hits) -> "np.ndarray":

@@ -60,6 +60,15 @@ class Batch(C.Structure):
                 ("hits", C.c_void_p), ("occluded", C.c_void_p)]
 
 
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("n", C.c_uint64),
+                ("kind", C.c_int32), ("pad", C.c_int32), ("hits", C.c_void_p),
+                ("occluded", C.c_void_p)]
+
+
+MAX_JOBS = 192
+
+
 class BvhgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"bvhgpu error {code}: {msg}")
@@ -85,6 +94,7 @@ _SIGS = {
     "bvhgpu_scene_bytes": (C.c_int, [_P] + [C.POINTER(C.c_uint64)] * 4),
     "bvhgpu_trace": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P, _P, _P]),
     "bvhgpu_trace_host": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P]),
+    "bvhgpu_trace_jobs": (C.c_int, [C.POINTER(Job), C.c_int32, C.POINTER(TraceOpts), _P]),
     "bvhgpu_intersect_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P, _P]),
     "bvhgpu_intersect_secondary_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P]),
     "bvhgpu_trace_batches_noalloc": (C.c_int, [_P, C.POINTER(Batch), C.c_int32,

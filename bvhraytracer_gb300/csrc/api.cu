@@ -17,6 +17,7 @@
 #include "bvhgpu.h"
 #include "bvhgpu_status.hpp"
 #include "launch.cuh"
+#include "batched.cuh"
 
 namespace bvhgpu {
 
@@ -450,6 +451,80 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   if (e != cudaSuccess) return cuda_error(e, "copy results out");
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_error(e, "synchronise");
+  return BVHGPU_OK;
+}
+
+}  // extern "C"
+
+namespace bvhgpu {
+namespace dev {
+cudaError_t launch_batched(const JobTable& t, int profile, int sm_count, cudaStream_t s);
+}  // namespace dev
+}  // namespace bvhgpu
+
+extern "C" {
+
+int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_trace_opts_t* opts,
+                      void* stream) {
+  if (n_jobs < 0 || n_jobs > dev::kMaxJobs)
+    return set_error(BVHGPU_ERR_BAD_ARG, "at most BVHGPU_MAX_JOBS (192) jobs per launch");
+  if (n_jobs > 0 && !jobs) return set_error(BVHGPU_ERR_BAD_ARG, "null jobs");
+  dev::LaunchCfg cfg;
+  int rc = check_opts(opts, cfg);
+  if (rc) return rc;
+  if (cfg.policy == 1) return set_error(BVHGPU_ERR_UNSUPPORTED, "jobs: policy 0 or 2");
+  static_assert(BVHGPU_MAX_JOBS == dev::kMaxJobs, "job limit");
+  std::unique_ptr<dev::JobTable> t(new (std::nothrow) dev::JobTable());
+  if (!t) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  uint64_t total = 0;
+  int device = -1, stack = 1, sms = 0;
+  bvhgpu_scene_t first = nullptr;
+  int nj = 0;
+  for (int i = 0; i < n_jobs; ++i) {
+    const bvhgpu_job_t& j = jobs[i];
+    if (!j.scene) return set_error(BVHGPU_ERR_BAD_ARG, "job without a scene");
+    if (j.kind != BVHGPU_CLOSEST && j.kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "job kind");
+    if (j.n >= (1ull << 32)) return set_error(BVHGPU_ERR_BAD_ARG, "job with 2^32 rays or more");
+    if (device >= 0 && j.scene->device != device)
+      return set_error(BVHGPU_ERR_BAD_ARG, "jobs on different devices");
+    device = j.scene->device;
+    if (j.n == 0) continue;
+    if (!j.rays || ((uintptr_t)j.rays & 15)) return set_error(BVHGPU_ERR_BAD_ARG, "job rays");
+    if (j.kind == BVHGPU_CLOSEST ? (!j.hits || ((uintptr_t)j.hits & 15)) : !j.occluded)
+      return set_error(BVHGPU_ERR_BAD_ARG, "job result buffer");
+    if (!first) first = j.scene;
+    dev::JobDev& d = t->jobs[nj++];
+    d.nodes = j.scene->d_nodes;
+    d.leaves = j.scene->d_leaves;
+    d.leaf_prim = j.scene->d_leaf_prim;
+    d.rays = j.rays;
+    d.out = j.kind == BVHGPU_CLOSEST ? (void*)j.hits : (void*)j.occluded;
+    d.status = j.scene->d_status;
+    d.ray_begin = total;
+    d.n = (uint32_t)j.n;
+    d.root_entry = j.scene->layout.root_entry;
+    d.leaf_memory = j.scene->layout.leaf_memory;
+    d.gang = (int16_t)j.scene->layout.gang;
+    d.nm = (int8_t)j.scene->layout.node_stride;
+    d.fmt = (int8_t)j.scene->layout.node_format;
+    d.kind = (int8_t)j.kind;
+    total += j.n;
+    stack = std::max(stack, j.scene->max_stack);
+    sms = j.scene->sm_count;
+  }
+  if (nj == 0) return BVHGPU_OK;
+  if ((size_t)stack * 128 * 4 > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for these trees");
+  t->n_jobs = nj;
+  t->total = total;
+  t->head = first->d_queue + (first->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
+  t->refill_min = cfg.refill_min;
+  t->stack_cap = stack;
+  t->policy = cfg.policy;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  e = dev::launch_batched(*t, cfg.profile, sms, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "batched launch");
   return BVHGPU_OK;
 }
 

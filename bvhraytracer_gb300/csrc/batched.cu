@@ -1,0 +1,35 @@
+// Instantiation and launch of the batched (multi-scene) persistent kernel.
+#include <cuda_runtime.h>
+
+#include "batched.cuh"
+
+namespace bvhgpu {
+namespace dev {
+
+size_t batched_param_bytes() { return sizeof(JobTable); }
+
+cudaError_t launch_batched(const JobTable& t, int profile, int sm_count, cudaStream_t s) {
+  const int bs = 128;
+  const size_t smem = (size_t)t.stack_cap * bs * 4;
+  auto k = profile == BVHGPU_PROFILE_FAST ? trace_batched_kernel<BVHGPU_PROFILE_FAST>
+                                          : trace_batched_kernel<BVHGPU_PROFILE_INSTRUMENTED>;
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024)
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, bs, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = (uint64_t)per_sm * sm_count;
+  const uint64_t need = (t.total + bs - 1) / bs;
+  if (grid > need) grid = need;
+  if (grid == 0) return cudaSuccess;
+  e = cudaMemsetAsync(t.head, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  k<<<(unsigned)grid, bs, smem, s>>>(t);
+  return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace bvhgpu

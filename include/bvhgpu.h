@@ -25,6 +25,8 @@
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
  *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
+ *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
+ *                             structure, fastNodeManager.h:92-156, across scenes)
  *   bvhgpu_intersect_fastrays FastNodeManager::intersectWideAlternative on FastRay
  *                             records (fastNodeManager.h:835-1049; FastRay: src/fastRay.h:14-29)
  *   bvhgpu_intersect_secondary_fastrays
@@ -190,6 +192,29 @@ int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
  * `stream`. Device staging buffers are owned by the scene and reused. */
 int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                       const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                      void* stream);
+
+/* ---- many scenes in one launch ---------------------------------------- */
+/* A job: one ray batch traced in one scene. bvhgpu_trace_jobs traces up to
+ * BVHGPU_MAX_JOBS jobs (scenes of any N, L and node format, closest or any
+ * hit, uneven sizes) in ONE persistent launch that pulls rays from a global
+ * queue spanning all jobs (the GPU form of the reference's workgroup refill,
+ * fastNodeManager.h:92-156, 277-450, extended across scenes). Results per ray
+ * equal bvhgpu_trace's. All scenes must live on the stream's device; the
+ * options' profile and policy (0 or 2) apply to every job. Stream-ordered, no
+ * allocation, no synchronisation (so it can be recorded in a CUDA graph). */
+#define BVHGPU_MAX_JOBS 192
+typedef struct {
+  bvhgpu_scene_t scene;
+  const bvhgpu_ray_t* rays; /* device, 16-byte aligned */
+  uint64_t n;               /* < 2^32 */
+  int32_t kind;             /* BVHGPU_CLOSEST or BVHGPU_ANY */
+  int32_t pad;
+  bvhgpu_hit_t* hits;       /* closest: device, 16-byte aligned */
+  uint8_t* occluded;        /* any: device */
+} bvhgpu_job_t;
+
+int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_trace_opts_t* opts,
                       void* stream);
 
 /* ---- FastRay drop-in -------------------------------------------------- */
