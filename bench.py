@@ -62,8 +62,9 @@ def parse():
     p.add_argument("--ref-sample", type=float, default=0.1,
                    help="fraction of the frame traced per step by --impl reference")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="clutter", choices=["clutter", "batch64"],
-                   help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch")
+    p.add_argument("--workload", default="clutter", choices=["clutter", "batch64", "adjoint"],
+                   help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch; "
+                        "adjoint: forward + backward of the hit distance")
     p.add_argument("--scenes", type=int, default=64)
     p.add_argument("--tune-nl", action="store_true",
                    help="batch64: let the autotuner pick N/L per scene")
@@ -571,12 +572,125 @@ def run_batch(a):
     print(json.dumps(line))
 
 
+def fd_check(verts, faces, rays, prim, mask, t_tgt, gv, n_coords=512, h=1e-4, seed=3):
+    """Central finite differences in FP64 of the fixed-visibility loss on
+    sampled vertex coordinates; returns (norm-relative error, max relative)."""
+    V = verts.astype(np.float64)
+    R = rays.astype(np.float64)
+    hit = np.nonzero(mask)[0]
+    tri_of = prim[hit]
+    F = faces
+    touched = np.unique(F[tri_of].reshape(-1))
+    rng = np.random.default_rng(seed)
+    vids = rng.choice(touched, n_coords, replace=len(touched) < n_coords)
+    axes = rng.integers(0, 3, n_coords)
+    # rays per vertex through the triangles that use it
+    order = np.argsort(tri_of)
+    sorted_tris = tri_of[order]
+    fd = np.zeros(n_coords)
+    for k, (vid, ax) in enumerate(zip(vids, axes)):
+        tris = np.nonzero(np.any(F == vid, axis=1))[0]
+        lo = np.searchsorted(sorted_tris, tris, "left")
+        hi = np.searchsorted(sorted_tris, tris, "right")
+        rr = hit[np.concatenate([order[a:b] for a, b in zip(lo, hi)])]
+        tt = F[prim[rr]]
+
+        def L(delta):
+            W = V[np.unique(tt)].copy()
+            idx = {g: j for j, g in enumerate(np.unique(tt))}
+            W[idx[vid], ax] += delta
+            p0 = W[[idx[x] for x in tt[:, 0]]]
+            p1 = W[[idx[x] for x in tt[:, 1]]]
+            p2 = W[[idx[x] for x in tt[:, 2]]]
+            o, d = R[rr, 0:3], R[rr, 4:7]
+            e1, e2 = p1 - p0, p2 - p0
+            s1 = np.cross(d, e2)
+            inv = 1.0 / np.sum(s1 * e1, -1)
+            s2 = np.cross(o - p0, e1)
+            t = np.sum(e2 * s2, -1) * inv
+            return np.sum((t - t_tgt[rr]) ** 2)
+        fd[k] = (L(h) - L(-h)) / (2 * h)
+    ad = gv[vids, axes].astype(np.float64)
+    rel = np.linalg.norm(ad - fd) / max(np.linalg.norm(fd), 1e-300)
+    big = np.abs(fd) > 1e-3 * np.max(np.abs(fd))
+    return float(rel), float(np.max(np.abs(ad - fd)[big] / np.abs(fd)[big]))
+
+
+def run_adjoint(a):
+    """Forward + backward of sum over 1M primary rays of (t - t_target)^2,
+    t_target from vertices moved by seeded N(0, 0.01) noise; terrain
+    256 x 256 quads and the 1M-triangle clutter scene."""
+    import torch
+    from bvhraytracer_gb300 import diff as D
+    from bvhraytracer_gb300 import scenes as S
+    dev = torch.device("cuda", 0)
+    results = {}
+    rng = np.random.default_rng(11)
+    for name in ("terrain256", "clutter1M"):
+        if name == "terrain256":
+            verts, faces = S.terrain_mesh(256, seed=0)
+            c = np.array([0.5, 0.0, 0.5])
+            rays = S.camera_rays(c + [0.0, 0.55, 0.65], c, 1024, 1024)
+        else:
+            tris = S.clutter(a.objects, seed=1)
+            verts = tris.reshape(-1, 3)
+            faces = np.arange(verts.shape[0], dtype=np.int64).reshape(-1, 3)
+            cam, target, _ = S.clutter_viewpoints(a.objects, seed=1)
+            rays = S.camera_rays(cam, target, 1024, 1024)
+        v = torch.from_numpy(verts).to(dev).requires_grad_(True)
+        f = torch.from_numpy(faces).to(dev)
+        r = torch.from_numpy(rays).to(dev).requires_grad_(True)
+        scene = D.scene_for(v, f)
+        vt = torch.from_numpy(verts + rng.normal(0, 0.01, verts.shape).astype(np.float32)).to(dev)
+        t_tgt, _, _, p_tgt = D.ray_hit(vt, f, r.detach(), D.scene_for(vt, f))
+
+        def step():
+            t, u, w, prim = D.ray_hit(v, f, r, scene)
+            m = (prim >= 0) & (p_tgt >= 0)
+            loss = ((t - t_tgt)[m] ** 2).sum()
+            gv, gr = torch.autograd.grad(loss, (v, r))
+            return loss, gv, gr, prim, m
+
+        for _ in range(a.warmup):
+            step()
+        torch.cuda.synchronize(dev)
+        stream = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            loss, gv, gr, prim, m = step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / a.steps
+        rel, worst = fd_check(verts, faces, rays, prim.cpu().numpy(), m.cpu().numpy(),
+                              t_tgt.cpu().numpy().astype(np.float64), gv.cpu().numpy())
+        scene.status()
+        results[name] = {"triangles": int(faces.shape[0]), "rays": int(rays.shape[0]),
+                         "hits": int(m.sum().item()), "ms_forward_backward": ms,
+                         "mrays_per_s_forward_backward": rays.shape[0] / (ms / 1e3) / 1e6,
+                         "fd_fp64_rel_error_norm": rel, "fd_fp64_rel_error_max": worst,
+                         "fd": "central, FP64, h=1e-4, 512 sampled vertex coordinates"}
+    line = {
+        "metric": "Mrays/s (forward+backward)",
+        "value": results["clutter1M"]["mrays_per_s_forward_backward"],
+        "unit": "Mrays/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": results["clutter1M"]["ms_forward_backward"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded terrain and clutter scenes)",
+        "config": {"workload": "adjoint: loss sum (t - t_target)^2 over 1M primary rays",
+                   "results": results},
+    }
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "batch64":
         run_batch(a)
+    elif a.workload == "adjoint":
+        run_adjoint(a)
     else:
         run_ours(a)
 

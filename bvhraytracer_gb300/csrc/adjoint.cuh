@@ -1,0 +1,22 @@
+// Arguments and launcher of the adjoint kernel (adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "traverse.cuh"
+
+namespace bvhgpu {
+namespace dev {
+
+struct AdjointArgs {
+  const bvhgpu_ray_t* rays;
+  uint64_t n;
+  const float4* grad_hits;  // per ray: (unused, dL/dt, dL/db1, dL/db2)
+  float* grad_tri9;         // per input triangle: dL/dp0, dL/dp1, dL/dp2 (accumulated)
+  float* grad_rays;         // per ray: dL/do (3), 0, dL/dd (3), 0 (written)
+  int stack_cap;
+};
+
+cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s);
+
+}  // namespace dev
+}  // namespace bvhgpu

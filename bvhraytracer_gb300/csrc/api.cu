@@ -18,6 +18,7 @@
 #include "bvhgpu_status.hpp"
 #include "launch.cuh"
 #include "batched.cuh"
+#include "adjoint.cuh"
 
 namespace bvhgpu {
 
@@ -525,6 +526,30 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   e = dev::launch_batched(*t, cfg.profile, sms, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_error(e, "batched launch");
+  return BVHGPU_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int bvhgpu_adjoint(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n, const float* grad_hits,
+                   float* grad_tri9, float* grad_rays, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  if (n == 0) return BVHGPU_OK;
+  if (!rays || !grad_hits || !grad_tri9 || !grad_rays || ((uintptr_t)rays & 15) ||
+      ((uintptr_t)grad_hits & 15) || ((uintptr_t)grad_rays & 15))
+    return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: null or misaligned buffer");
+  if (s->layout.node_format != BVHGPU_NODES_FP32)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "adjoint: FP32 node scenes only");
+  if ((size_t)s->max_stack * 128 * 4 > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  dev::AdjointArgs a{rays, n, reinterpret_cast<const float4*>(grad_hits), grad_tri9, grad_rays,
+                     s->max_stack};
+  e = dev::launch_adjoint(s->dev_view(), s->layout.node_stride, a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "adjoint launch");
   return BVHGPU_OK;
 }
 

@@ -1,0 +1,83 @@
+"""Differentiable closest-hit distance: a torch.autograd.Function over the
+C ABI's trace (forward) and adjoint (backward) kernels.
+
+The visibility set is fixed: the forward pass finds each ray's closest
+triangle in a BVH built for the current vertex positions, and gradients flow
+through the hit triangle's Moller-Trumbore distance and barycentrics (the
+formulas of the reference's triIntersect{L}, rayTracerTemplate.ispc:35-76),
+not through changes of which triangle is hit. The backward kernel re-traces
+the rays instead of reading stored hits.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import Bvh, Scene
+from . import _native as N
+
+
+class _RayHit(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, verts, rays, faces, scene):
+        res = scene.trace(rays.detach().contiguous(), profile="fast")["hits"]
+        ctx.scene = scene
+        ctx.n_verts = verts.shape[0]
+        ctx.save_for_backward(rays, faces)
+        prim = res.view(torch.int32)[:, 0].clone()
+        ctx.mark_non_differentiable(prim)
+        return res[:, 1].clone(), res[:, 2].clone(), res[:, 3].clone(), prim
+
+    @staticmethod
+    def backward(ctx, gt, gu, gv, _gprim):
+        rays, faces = ctx.saved_tensors
+        n = rays.shape[0]
+        dev = rays.device
+        z = torch.zeros(n, dtype=torch.float32, device=dev)
+
+        def g(x):
+            return z if x is None else x.to(torch.float32)
+
+        grad_hits = torch.stack([z, g(gt), g(gu), g(gv)], dim=1).contiguous()
+        grad_tri9 = torch.zeros((faces.shape[0], 9), dtype=torch.float32, device=dev)
+        grad_rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
+        stream = torch.cuda.current_stream(dev)
+        N.check(N.lib().bvhgpu_adjoint(ctx.scene.handle, rays.data_ptr(), n, grad_hits.data_ptr(),
+                                       grad_tri9.data_ptr(), grad_rays.data_ptr(),
+                                       C.c_void_p(stream.cuda_stream)))
+        grad_verts = torch.zeros((ctx.n_verts, 3), dtype=torch.float32, device=dev)
+        grad_verts.index_add_(0, faces.reshape(-1), grad_tri9.view(-1, 3))
+        return grad_verts, grad_rays, None, None
+
+
+def ray_hit(verts: torch.Tensor, faces: torch.Tensor, rays: torch.Tensor, scene: Scene):
+    """Closest hit of each ray: returns ``(t, u, v, prim)``; ``t``, ``u``, ``v``
+    are differentiable with respect to ``verts`` ``[V, 3]`` and ``rays``
+    ``[n, 8]`` (origin and direction). ``scene`` must be built from
+    ``verts[faces]`` (see :func:`scene_for`). Misses have prim -1, t = tmax and
+    zero gradients."""
+    return _RayHit.apply(verts, rays, faces, scene)
+
+
+def scene_for(verts: torch.Tensor, faces: torch.Tensor, branching: int = 8, leaf_size: int = 8,
+              device: int = 0) -> Scene:
+    """BVH and device scene of the mesh at its current vertex positions."""
+    tris = verts.detach().cpu()[faces.cpu()].reshape(-1, 9).numpy()
+    return Scene(Bvh(tris, branching, leaf_size, drop_zero_area=False), device=device)
+
+
+def moller_trumbore_torch(o, d, p0, p1, p2):
+    """Plain PyTorch Moller-Trumbore (t, b1, b2) of given ray/triangle pairs,
+    in the order of triIntersect{L}; differentiable by autograd."""
+    e1 = p1 - p0
+    e2 = p2 - p0
+    s1 = torch.cross(d, e2, dim=-1)
+    div = (s1 * e1).sum(-1)
+    inv = 1.0 / div
+    s = o - p0
+    b1 = (s * s1).sum(-1) * inv
+    s2 = torch.cross(s, e1, dim=-1)
+    b2 = (d * s2).sum(-1) * inv
+    t = (e2 * s2).sum(-1) * inv
+    return t, b1, b2

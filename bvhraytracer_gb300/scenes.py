@@ -42,8 +42,7 @@ def _grid_tris(verts: np.ndarray) -> np.ndarray:
     return np.stack([t1, t2], axis=2).reshape(-1, 9).astype(np.float32)
 
 
-def terrain(n: int = 128, seed: int = 0) -> np.ndarray:
-    """Height-field terrain with ``2*n*n`` triangles."""
+def _terrain_grid(n: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     xs = np.linspace(0.0, 1.0, n + 1)
     x, z = np.meshgrid(xs, xs, indexing="ij")
@@ -52,8 +51,27 @@ def terrain(n: int = 128, seed: int = 0) -> np.ndarray:
         th = rng.uniform(0, 2 * math.pi)
         ph = rng.uniform(0, 2 * math.pi)
         y += (0.1 / k) * np.sin(2 * math.pi * f * (x * math.cos(th) + z * math.sin(th)) + ph)
-    verts = np.stack([x, y, z], axis=-1)
-    return _grid_tris(verts)
+    return np.stack([x, y, z], axis=-1)
+
+
+def terrain(n: int = 128, seed: int = 0) -> np.ndarray:
+    """Height-field terrain with ``2*n*n`` triangles."""
+    return _grid_tris(_terrain_grid(n, seed))
+
+
+def terrain_mesh(n: int = 128, seed: int = 0):
+    """The same terrain as shared vertices ``[(n+1)^2, 3]`` float32 and faces
+    ``[2 n^2, 3]`` int64, in the triangle order of :func:`terrain`."""
+    verts = _terrain_grid(n, seed).reshape(-1, 3).astype(np.float32)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    a = i * (n + 1) + j
+    b = (i + 1) * (n + 1) + j
+    c = (i + 1) * (n + 1) + j + 1
+    d = i * (n + 1) + j + 1
+    t1 = np.stack([a, c, b], -1)
+    t2 = np.stack([a, d, c], -1)
+    faces = np.stack([t1, t2], axis=2).reshape(-1, 3).astype(np.int64)
+    return verts, faces
 
 
 def _uv_sphere(center, radius, seg: int = 16, rings: int = 8) -> np.ndarray:

@@ -25,6 +25,8 @@
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
  *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
+ *   bvhgpu_adjoint            no reference counterpart: reverse pass of triIntersect{L}'s
+ *                             Moller-Trumbore (rayTracerTemplate.ispc:35-76)
  *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
  *                             structure, fastNodeManager.h:92-156, across scenes)
  *   bvhgpu_intersect_fastrays FastNodeManager::intersectWideAlternative on FastRay
@@ -232,6 +234,19 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t scene, float* fastrays, uint64_t n,
                               uint32_t* leaf_index, int8_t* tri_index, void* stream);
 int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t scene, const float* fastrays, uint64_t n,
                                         int32_t scheme, uint16_t* result, void* stream);
+
+/* ---- adjoint ---------------------------------------------------------- */
+/* Backward pass of the closest-hit leaf intersection through a fixed
+ * visibility set (fast profile: Moller-Trumbore of triIntersect{L},
+ * rayTracerTemplate.ispc:35-76). For each ray the kernel re-traces the closest
+ * hit (no stored hits are read) and, given grad_hits[i] = (unused, dL/dt,
+ * dL/du, dL/dv), adds dL/dp0, dL/dp1, dL/dp2 of the hit triangle into
+ * grad_tri9[prim*9 .. prim*9+8] (atomically: zero it first; sized by the input
+ * triangle count) and writes grad_rays[i*8 ..] = (dL/do, 0, dL/dd, 0). Rays
+ * that miss get zero gradients. FP32 node scenes only. Device pointers,
+ * 16-byte aligned; stream-ordered. */
+int bvhgpu_adjoint(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
+                   const float* grad_hits, float* grad_tri9, float* grad_rays, void* stream);
 
 /* ---- tracing without allocation --------------------------------------- */
 /* No counterpart in the reference (its renderer allocates nothing on a GPU).

@@ -1,0 +1,132 @@
+"""Adjoint of the leaf intersection (bvhgpu_adjoint) behind torch.autograd:
+checked against PyTorch autograd of Moller-Trumbore on the same hit set and
+against central finite differences in FP64 (h = 1e-4)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from bvhraytracer_gb300 import diff as D  # noqa: E402
+from bvhraytracer_gb300 import scenes as S  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(n=64, res=96, seed=0):
+    verts, faces = S.terrain_mesh(n, seed)
+    c = np.array([0.5, 0.0, 0.5])
+    rays = S.camera_rays(c + [0.0, 0.6, 0.7], c, res, res)
+    v = torch.from_numpy(verts).cuda().requires_grad_(True)
+    f = torch.from_numpy(faces).cuda()
+    r = torch.from_numpy(rays).cuda().requires_grad_(True)
+    scene = D.scene_for(v, f)
+    # targets from vertices moved by seeded N(0, 0.01) noise
+    rng = np.random.default_rng(seed + 1)
+    vt = torch.from_numpy(verts + rng.normal(0, 0.01, verts.shape).astype(np.float32)).cuda()
+    t_tgt, _, _, p_tgt = D.ray_hit(vt, f, r.detach(), D.scene_for(vt, f))
+    return v, f, r, scene, t_tgt, p_tgt
+
+
+def _loss_and_grads(v, f, r, scene, t_tgt, p_tgt):
+    t, u, w, prim = D.ray_hit(v, f, r, scene)
+    m = (prim >= 0) & (p_tgt >= 0)
+    loss = ((t - t_tgt)[m] ** 2).sum()
+    gv, gr = torch.autograd.grad(loss, (v, r))
+    return loss, gv, gr, prim, m
+
+
+def test_adjoint_matches_torch_autograd_moller_trumbore():
+    v, f, r, scene, t_tgt, p_tgt = _case()
+    loss, gv, gr, prim, m = _loss_and_grads(v, f, r, scene, t_tgt, p_tgt)
+    # Same loss with PyTorch autograd of Moller-Trumbore on the same hit set.
+    v2 = v.detach().clone().requires_grad_(True)
+    r2 = r.detach().clone().requires_grad_(True)
+    idx = torch.nonzero(m).squeeze(1)
+    tri = f[prim[idx].long()]
+    t2, b1, b2 = D.moller_trumbore_torch(r2[idx, 0:3], r2[idx, 4:7], v2[tri[:, 0]],
+                                         v2[tri[:, 1]], v2[tri[:, 2]])
+    t_fwd, u_fwd, w_fwd, _ = D.ray_hit(v, f, r, scene)
+    # the same forward values (torch may contract to FMA, so not bit for bit)
+    assert torch.allclose(t2.detach(), t_fwd[idx].detach(), rtol=1e-5, atol=0)
+    loss2 = ((t2 - t_tgt[idx]) ** 2).sum()
+    gv2, gr2 = torch.autograd.grad(loss2, (v2, r2))
+    rel_v = (gv - gv2).norm() / gv2.norm()
+    rel_r = (gr[:, [0, 1, 2, 4, 5, 6]] - gr2[:, [0, 1, 2, 4, 5, 6]]).norm() / gr2.norm()
+    assert rel_v < 1e-5 and rel_r < 1e-5, (rel_v.item(), rel_r.item())
+
+
+def test_adjoint_barycentric_gradients():
+    v, f, r, scene, t_tgt, p_tgt = _case(n=32, res=48)
+    t, u, w, prim = D.ray_hit(v, f, r, scene)
+    m = prim >= 0
+    loss = (u[m] * 0.7 - w[m] * 1.3).sum()
+    gv, = torch.autograd.grad(loss, (v,))
+    v2 = v.detach().clone().requires_grad_(True)
+    idx = torch.nonzero(m).squeeze(1)
+    tri = f[prim[idx].long()]
+    _, b1, b2 = D.moller_trumbore_torch(r[idx, 0:3].detach(), r[idx, 4:7].detach(),
+                                        v2[tri[:, 0]], v2[tri[:, 1]], v2[tri[:, 2]])
+    gv2, = torch.autograd.grad((b1 * 0.7 - b2 * 1.3).sum(), (v2,))
+    assert (gv - gv2).norm() / gv2.norm() < 1e-5
+
+
+def _fd_loss(o, d, p0, p1, p2, tgt):
+    """FP64 loss over fixed ray/triangle pairs (numpy)."""
+    e1 = p1 - p0
+    e2 = p2 - p0
+    s1 = np.cross(d, e2)
+    inv = 1.0 / np.sum(s1 * e1, -1)
+    s = o - p0
+    s2 = np.cross(s, e1)
+    t = np.sum(e2 * s2, -1) * inv
+    return np.sum((t - tgt) ** 2)
+
+
+def test_adjoint_against_fp64_finite_differences():
+    v, f, r, scene, t_tgt, p_tgt = _case(n=64, res=128)
+    loss, gv, gr, prim, m = _loss_and_grads(v, f, r, scene, t_tgt, p_tgt)
+    V = v.detach().cpu().numpy().astype(np.float64)
+    F = f.cpu().numpy()
+    R = r.detach().cpu().numpy().astype(np.float64)
+    P = prim.cpu().numpy()
+    M = m.cpu().numpy()
+    T = t_tgt.cpu().numpy().astype(np.float64)
+    rays_hit = np.nonzero(M)[0]
+    tri_of = P[rays_hit]
+    # vertices touched by hits; 512 sampled coordinates
+    touched = np.unique(F[tri_of].reshape(-1))
+    rng = np.random.default_rng(3)
+    vids = rng.choice(touched, 512, replace=True)
+    axes = rng.integers(0, 3, 512)
+    h = 1e-4
+    gad = gv.cpu().numpy().astype(np.float64)
+    fd = np.zeros(512)
+    for k, (vid, ax) in enumerate(zip(vids, axes)):
+        sel = np.any(F[tri_of] == vid, axis=1)
+        rr = rays_hit[sel]
+        tt = F[P[rr]]
+
+        def L(delta):
+            W = V.copy()
+            W[vid, ax] += delta
+            return _fd_loss(R[rr, 0:3], R[rr, 4:7], W[tt[:, 0]], W[tt[:, 1]], W[tt[:, 2]], T[rr])
+        fd[k] = (L(h) - L(-h)) / (2 * h)
+    ad = gad[vids, axes]
+    rel = np.linalg.norm(ad - fd) / np.linalg.norm(fd)
+    assert rel < 1e-4, rel
+    # ray origin / direction gradients on 128 sampled rays
+    pick = rng.choice(rays_hit, 128, replace=False)
+    gR = gr.cpu().numpy().astype(np.float64)
+    fdr, adr = [], []
+    for i in pick:
+        tri = F[P[i]]
+        for comp in (0, 1, 2, 4, 5, 6):
+            def Lr(delta):
+                Q = R[i].copy()
+                Q[comp] += delta
+                return _fd_loss(Q[None, 0:3], Q[None, 4:7], V[tri[0]][None], V[tri[1]][None],
+                                V[tri[2]][None], T[i:i + 1])
+            fdr.append((Lr(h) - Lr(-h)) / (2 * h))
+            adr.append(gR[i, comp])
+    fdr, adr = np.array(fdr), np.array(adr)
+    assert np.linalg.norm(adr - fdr) / np.linalg.norm(fdr) < 1e-4
