@@ -85,6 +85,12 @@ def _fd_loss(o, d, p0, p1, p2, tgt):
 
 
 def test_adjoint_against_fp64_finite_differences():
+    """FP64 central differences on 512 sampled vertex coordinates and on the
+    origin / direction of 128 sampled rays. At h = 1e-4 the differences
+    themselves are off by about 1% on rays that graze steep triangles (t is
+    a rational function of the vertices); they converge to the adjoint as h
+    shrinks, so the check uses h = 1e-6 and a Richardson extrapolation of
+    h = 1e-4 and 5e-5."""
     v, f, r, scene, t_tgt, p_tgt = _case(n=64, res=128)
     loss, gv, gr, prim, m = _loss_and_grads(v, f, r, scene, t_tgt, p_tgt)
     V = v.detach().cpu().numpy().astype(np.float64)
@@ -95,15 +101,13 @@ def test_adjoint_against_fp64_finite_differences():
     T = t_tgt.cpu().numpy().astype(np.float64)
     rays_hit = np.nonzero(M)[0]
     tri_of = P[rays_hit]
-    # vertices touched by hits; 512 sampled coordinates
     touched = np.unique(F[tri_of].reshape(-1))
     rng = np.random.default_rng(3)
     vids = rng.choice(touched, 512, replace=True)
     axes = rng.integers(0, 3, 512)
-    h = 1e-4
     gad = gv.cpu().numpy().astype(np.float64)
-    fd = np.zeros(512)
-    for k, (vid, ax) in enumerate(zip(vids, axes)):
+
+    def fd_vertex(vid, ax, h):
         sel = np.any(F[tri_of] == vid, axis=1)
         rr = rays_hit[sel]
         tt = F[P[rr]]
@@ -112,10 +116,18 @@ def test_adjoint_against_fp64_finite_differences():
             W = V.copy()
             W[vid, ax] += delta
             return _fd_loss(R[rr, 0:3], R[rr, 4:7], W[tt[:, 0]], W[tt[:, 1]], W[tt[:, 2]], T[rr])
-        fd[k] = (L(h) - L(-h)) / (2 * h)
+        return (L(h) - L(-h)) / (2 * h)
+
     ad = gad[vids, axes]
-    rel = np.linalg.norm(ad - fd) / np.linalg.norm(fd)
-    assert rel < 1e-4, rel
+    fd = {h: np.array([fd_vertex(a, b, h) for a, b in zip(vids, axes)])
+          for h in (1e-4, 5e-5, 1e-6)}
+    rich = (4 * fd[5e-5] - fd[1e-4]) / 3
+
+    def rel(x):
+        return np.linalg.norm(ad - x) / np.linalg.norm(x)
+    assert rel(fd[1e-6]) < 1e-4, rel(fd[1e-6])
+    assert rel(rich) < 1e-3, rel(rich)
+    assert rel(fd[1e-4]) < 5e-2  # truncation-limited, reported by the adjoint bench
     # ray origin / direction gradients on 128 sampled rays
     pick = rng.choice(rays_hit, 128, replace=False)
     gR = gr.cpu().numpy().astype(np.float64)
@@ -128,7 +140,7 @@ def test_adjoint_against_fp64_finite_differences():
                 Q[comp] += delta
                 return _fd_loss(Q[None, 0:3], Q[None, 4:7], V[tri[0]][None], V[tri[1]][None],
                                 V[tri[2]][None], T[i:i + 1])
-            fdr.append((Lr(h) - Lr(-h)) / (2 * h))
+            fdr.append((Lr(1e-6) - Lr(-1e-6)) / 2e-6)
             adr.append(gR[i, comp])
     fdr, adr = np.array(fdr), np.array(adr)
     assert np.linalg.norm(adr - fdr) / np.linalg.norm(fdr) < 1e-4
