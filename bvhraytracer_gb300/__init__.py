@@ -236,6 +236,22 @@ class Scene:
         N.check(N.lib().bvhgpu_trace_batches_noalloc(self._h, arr, len(batches), C.byref(o),
                                                      C.c_void_p(s.cuda_stream)))
 
+    def fp64_check(self, rays, hits, *, profile: str = "instrumented", stream=None):
+        """Per closest hit, the FP64 (t, b1, b2) of the same ray / triangle
+        pair and |t - t64| / |t64| (``[n, 4]`` float64 tensor; NaN rows for
+        misses)."""
+        import torch
+        n = rays.shape[0]
+        out = torch.empty((n, 4), dtype=torch.float64, device=rays.device)
+        s = stream if stream is not None else torch.cuda.current_stream(rays.device)
+        N.check(N.lib().bvhgpu_fp64_check(self._h, _ptr(rays), _ptr(hits), n, _PROFILE[profile],
+                                          _ptr(out), C.c_void_p(s.cuda_stream)))
+        return out
+
+    def set_stack_limit(self, entries: int) -> None:
+        """Caps the traversal stack (0 restores the tree's worst case)."""
+        N.check(N.lib().bvhgpu_scene_set_stack_limit(self._h, entries))
+
     def status(self, stream=None) -> None:
         """Raises if a kernel of this scene recorded a device-side error."""
         sp = stream.cuda_stream if stream is not None else 0

@@ -47,12 +47,15 @@ struct bvhgpu_scene {
   int device = 0;
   DeviceLayout layout;  // host copy of the uploaded arrays (sizes and ids)
   int max_stack = 0;
+  int stack_limit = 0;  // 0: max_stack; else traversal stack entries per ray
+  uint32_t stall_bytes = 0;  // failure-detection tests: staging wait never completes
   std::vector<uint32_t> prim_slot;  // input triangle id -> leaf * leaf_memory + lane
   uint8_t* d_nodes = nullptr;
   float* d_leaves = nullptr;
   uint32_t* d_leaf_prim = nullptr;
   uint8_t* d_leaf_depth = nullptr;
   int* d_status = nullptr;
+  uint32_t* d_prim_slot = nullptr;  // uploaded on first FP64 check
   // Queue heads of the persistent scheme: one slot per launch, round robin,
   // so up to kQueueSlots launches may be in flight on different streams.
   static constexpr int kQueueSlots = 64;
@@ -84,6 +87,7 @@ struct bvhgpu_scene {
     cudaFree(d_leaf_depth);
     cudaFree(d_status);
     cudaFree(d_queue);
+    cudaFree(d_prim_slot);
     cudaFree(d_stage);
     d_nodes = nullptr;
     d_leaves = nullptr;
@@ -91,6 +95,7 @@ struct bvhgpu_scene {
     d_leaf_depth = nullptr;
     d_status = nullptr;
     d_queue = nullptr;
+    d_prim_slot = nullptr;
     d_stage = nullptr;
   }
 };
@@ -105,6 +110,12 @@ static int upload(T** dst, const std::vector<T>& src) {
     if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy");
   }
   return BVHGPU_OK;
+}
+
+// Traversal stack entries per ray: the tree's worst case unless a smaller
+// limit was set (then deeper rays fail with BVHGPU_ERR_STACK_OVERFLOW).
+static int stack_cap(const bvhgpu_scene* s) {
+  return (s->stack_limit > 0 && s->stack_limit < s->max_stack) ? s->stack_limit : s->max_stack;
 }
 
 static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
@@ -145,6 +156,7 @@ static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
     // Stage the top levels (up to kTopStageBytes) in shared memory.
     const uint32_t fit = kTopStageBytes / (uint32_t)s->layout.record_bytes;
     cfg.top_nodes = std::min(s->layout.top_nodes, fit);
+    cfg.stall_bytes = s->stall_bytes;
   }
   if (cfg.scheme == BVHGPU_STREAM && cfg.fmt != BVHGPU_NODES_FP32)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "the stream scheme traverses FP32 nodes only");
@@ -395,7 +407,7 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   a.occluded = occluded;
   a.counters = counters;
   a.depth_hist = reinterpret_cast<unsigned long long*>(depth_hist);
-  a.stack_cap = s->max_stack;
+  a.stack_cap = stack_cap(s);
   if (cfg.scheme == BVHGPU_STREAM &&
       dev::stream_smem_bytes(cfg.packet, a.stack_cap, cfg.count) > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet does not fit shared memory for this tree depth");
@@ -444,7 +456,7 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   a.occluded = closest ? nullptr : d_out;
   a.counters = nullptr;
   a.depth_hist = nullptr;
-  a.stack_cap = s->max_stack;
+  a.stack_cap = stack_cap(s);
   rc = launch(s, a, cfg, st);
   if (rc) return rc;
   e = cudaMemcpyAsync(closest ? (void*)hits : (void*)occluded, d_out,
@@ -510,7 +522,7 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.fmt = (int8_t)j.scene->layout.node_format;
     d.kind = (int8_t)j.kind;
     total += j.n;
-    stack = std::max(stack, j.scene->max_stack);
+    stack = std::max(stack, stack_cap(j.scene));
     sms = j.scene->sm_count;
   }
   if (nj == 0) return BVHGPU_OK;
@@ -547,9 +559,65 @@ int bvhgpu_adjoint(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n, const
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   dev::AdjointArgs a{rays, n, reinterpret_cast<const float4*>(grad_hits), grad_tri9, grad_rays,
-                     s->max_stack};
+                     stack_cap(s)};
   e = dev::launch_adjoint(s->dev_view(), s->layout.node_stride, a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_error(e, "adjoint launch");
+  return BVHGPU_OK;
+}
+
+}  // extern "C"
+
+namespace bvhgpu {
+namespace dev {
+struct Fp64Args {
+  const bvhgpu_ray_t* rays;
+  const float4* hits;
+  uint64_t n;
+  const uint32_t* prim_slot;
+  uint32_t n_prims;
+  int profile;
+  double* out;
+};
+cudaError_t launch_fp64_check(const SceneDev& sc, const Fp64Args& a, cudaStream_t s);
+}  // namespace dev
+}  // namespace bvhgpu
+
+extern "C" {
+
+int bvhgpu_fp64_check(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
+                      uint64_t n, int32_t profile, double* out, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  if (n == 0) return BVHGPU_OK;
+  if (!rays || !hits || !out || ((uintptr_t)rays & 15) || ((uintptr_t)hits & 15) ||
+      ((uintptr_t)out & 7))
+    return set_error(BVHGPU_ERR_BAD_ARG, "fp64 check: null or misaligned buffer");
+  if (profile != BVHGPU_PROFILE_INSTRUMENTED && profile != BVHGPU_PROFILE_FAST)
+    return set_error(BVHGPU_ERR_BAD_ARG, "profile");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  {
+    std::lock_guard<std::mutex> lock(s->staging_mu);
+    if (!s->d_prim_slot) {
+      int rc = upload(&s->d_prim_slot, s->prim_slot);
+      if (rc) return rc;
+    }
+  }
+  dev::Fp64Args a{rays, reinterpret_cast<const float4*>(hits), n, s->d_prim_slot,
+                  (uint32_t)s->prim_slot.size(), profile, out};
+  e = dev::launch_fp64_check(s->dev_view(), a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "fp64 check launch");
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_inject_stall(bvhgpu_scene_t s, int32_t on) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  s->stall_bytes = on ? 16u : 0u;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_set_stack_limit(bvhgpu_scene_t s, int32_t entries) {
+  if (!s || entries < 0) return set_error(BVHGPU_ERR_BAD_ARG, "stack limit");
+  s->stack_limit = entries;
   return BVHGPU_OK;
 }
 
@@ -721,7 +789,7 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
     a.occluded = b.kind == BVHGPU_ANY ? b.occluded : nullptr;
     a.counters = nullptr;
     a.depth_hist = nullptr;
-    a.stack_cap = s->max_stack;
+    a.stack_cap = stack_cap(s);
     dev::LaunchCfg c = cfg;
     c.kind = b.kind;
     c.count = false;

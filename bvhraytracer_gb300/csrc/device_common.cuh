@@ -277,11 +277,19 @@ BVHGPU_DEV void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// Nanoseconds of the global timer.
+BVHGPU_DEV uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // Waits for the phase with the given parity to complete; gives up after
-// `limit` polls and returns false.
-BVHGPU_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+// `limit_ns` nanoseconds and returns false.
+BVHGPU_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
   const uint32_t a = smem_addr(bar);
-  for (uint32_t i = 0; i < limit; ++i) {
+  const uint64_t t0 = global_ns();
+  while (true) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -290,8 +298,8 @@ BVHGPU_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
   }
-  return false;
 }
 
 // Read-only global loads.

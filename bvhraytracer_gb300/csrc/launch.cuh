@@ -21,6 +21,7 @@ struct LaunchCfg {
   int sm_count = 152;
   int fmt = BVHGPU_NODES_FP32;  // node record format of the scene
   uint32_t top_nodes = 0;       // persistent scheme: inner records staged in shared memory
+  uint32_t stall_bytes = 0;     // failure-detection tests (see bvhgpu_scene_inject_stall)
 };
 
 template <typename K>
@@ -61,7 +62,7 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     uint64_t grid = (uint64_t)per_sm * cfg.sm_count;
     const uint64_t need = (a.n + bs - 1) / bs;
     if (grid > need) grid = need;
-    QueueArgs q{cfg.queue, cfg.refill_min, cfg.top_nodes};
+    QueueArgs q{cfg.queue, cfg.refill_min, cfg.top_nodes, cfg.top_nodes ? cfg.stall_bytes : 0u};
     if (!cfg.queue_cleared) {
       e = cudaMemsetAsync(cfg.queue, 0, sizeof(unsigned long long), s);
       if (e != cudaSuccess) return e;

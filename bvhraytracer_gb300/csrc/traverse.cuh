@@ -716,6 +716,7 @@ struct QueueArgs {
   unsigned long long* head;  // next unclaimed ray (zeroed before the launch)
   int refill_min;            // refill when at least this many lanes are idle
   uint32_t top_nodes;        // inner records staged in shared memory (0: none)
+  uint32_t stall_bytes;      // failure-detection tests: bytes the staging wait expects extra
 };
 
 #ifndef BVHGPU_PERSIST_MIN_BLOCKS
@@ -737,13 +738,15 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
     if (threadIdx.x == 0) mbar_init(&top_bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-      mbar_arrive_expect_tx(&top_bar, bytes);
+      // q.stall_bytes (failure-detection tests only) makes the barrier wait
+      // for bytes no copy delivers, so the bounded wait below runs out.
+      mbar_arrive_expect_tx(&top_bar, bytes + q.stall_bytes);
       for (uint32_t off = 0; off < bytes; off += 32768u)
         bulk_copy_g2s(top_smem + off, sc.nodes + off, min(32768u, bytes - off), &top_bar);
     }
-    if (!mbar_wait(&top_bar, 0, 1u << 24)) {
+    if (!mbar_wait(&top_bar, 0, 500000000ull)) {  // 0.5 s
       record_error(sc.status, kDevErrTimeout);
-      mbar_wait(&top_bar, 0, 1u << 24);  // let the copy land before the block exits
+      mbar_wait(&top_bar, 0, 500000000ull);  // let a late copy land before the block exits
       return;
     }
   }

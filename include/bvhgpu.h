@@ -272,6 +272,30 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t scene, const bvhgpu_batch_t* bat
                                  int32_t n_batches, const bvhgpu_trace_opts_t* opts,
                                  void* stream);
 
+/* ---- FP64 check ------------------------------------------------------- */
+/* For each ray with a closest hit (hits[i].prim >= 0), recomputes the hit
+ * record of the same ray / triangle pair in double precision (Moller-Trumbore
+ * on the FP32 ray the kernels traced: normalised in the instrumented
+ * profile) and writes out[i*4 ..] = (t64, b1_64, b2_64, |t - t64| / |t64|);
+ * misses get NaN. The only kernel that computes in FP64. Device pointers
+ * (rays, hits 16-byte aligned); stream-ordered. */
+int bvhgpu_fp64_check(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
+                      uint64_t n, int32_t profile, double* out, void* stream);
+
+/* Caps the traversal stack at `entries` per ray (0: the tree's worst case,
+ * the default, which never overflows). Rays that need more stop, report a
+ * miss and record BVHGPU_ERR_STACK_OVERFLOW for bvhgpu_scene_status; the
+ * reference's stacks are a fixed 48 entries (fastNodeManager.h:1333). */
+int bvhgpu_scene_set_stack_limit(bvhgpu_scene_t scene, int32_t entries);
+
+/* Failure-detection testing (no reference counterpart). With `on`, the
+ * persistent kernels of this scene that stage top levels in shared memory
+ * (scene top_levels > 0) wait for 16 bytes that no copy delivers; the wait
+ * gives up after 0.5 s, the blocks stop without tracing and
+ * bvhgpu_scene_status reports BVHGPU_ERR_TIMEOUT. No GPU fault is involved.
+ * Call with 0 to restore normal operation. */
+int bvhgpu_scene_inject_stall(bvhgpu_scene_t scene, int32_t on);
+
 /* Synchronises `stream` and returns the first device-side error recorded by
  * this scene's kernels since the last call (and clears it). */
 int bvhgpu_scene_status(bvhgpu_scene_t scene, void* stream);
