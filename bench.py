@@ -35,6 +35,15 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mrays/s"
 
+# DRAM traffic per ray of the AO launch (persistent kernel, policy 2, FP32
+# nodes), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
+# of a 4,147,200-ray AO launch on the 251k-triangle clutter scene; the traffic
+# is the ray stream plus cold misses (the BVH stays in L2), so it grows with
+# the ray count and is scaled by it.
+# Source: profiles/trace_persistent_p2_ao_clutter250k_N8L8.md
+NCU_TRAFFIC_PER_AO_RAY = {"bytes": 140371712 / 4147200, "scheme": "persistent", "policy": 2,
+                          "layout": ("fp32", 0)}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -63,9 +72,12 @@ def parse():
                    help="fraction of the frame traced per step by --impl reference")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="clutter",
-                   choices=["clutter", "batch64", "adjoint", "scale8m"],
+                   choices=["clutter", "batch64", "adjoint", "scale8m", "terrain", "sweep"],
                    help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch; "
-                        "adjoint: forward + backward of the hit distance")
+                        "adjoint: forward + backward of the hit distance; scale8m: 8M "
+                        "triangles FP32 vs Q8 nodes; terrain: the 32k-triangle terrain, N4L4, "
+                        "512x512 + shadow rays; sweep: the clutter frame for every N, L in "
+                        "{4,8,12,16}^2, per-ray vs ray-stream")
     p.add_argument("--scenes", type=int, default=64)
     p.add_argument("--tune-nl", action="store_true",
                    help="batch64: let the autotuner pick N/L per scene")
@@ -380,6 +392,12 @@ def run_ours(a):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg[dom]["bytes"] / (per_kernel_ms[dom] / 1e3) / 1e9
+    traffic = None
+    dom_opts = chosen[dom][1]
+    if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
+            and dom_opts.get("policy") == NCU_TRAFFIC_PER_AO_RAY["policy"]
+            and chosen[dom][0].node_format == "fp32"):
+        traffic = NCU_TRAFFIC_PER_AO_RAY["bytes"] * int(batches[dom][0].shape[0])
 
     compare = {}
     if not a.no_compare:
@@ -417,7 +435,9 @@ def run_ours(a):
                 "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks
                 else "fallback",
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": ("ncu DRAM bytes per AO ray of a 4.1M-ray capture on the "
+                                   "251k-triangle scene, scaled by rays" if traffic else None),
                 "algorithmic_bytes_per_launch": alg[dom]["bytes"],
                 "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
             },
@@ -576,8 +596,11 @@ def run_batch(a):
 def fd_check(verts, faces, rays, prim, mask, t_tgt, gv, n_coords=512, seed=3):
     """Central finite differences in FP64 of the fixed-visibility loss on
     sampled vertex coordinates, at h = 1e-4 (truncation-limited on grazing
-    rays), h = 1e-6, and Richardson-extrapolated from h = 1e-4 and 5e-5.
-    Returns the norm-relative error of the adjoint against each."""
+    rays), 1e-6 and 1e-7, and Richardson-extrapolated from h = 1e-4 and 5e-5;
+    and the exact FP64 gradient of the same loss (PyTorch float64 autograd of
+    Moller-Trumbore on the CPU, same hit set). Returns the norm-relative error
+    of the FP32 adjoint against each, and of each difference quotient against
+    the exact FP64 gradient (the truncation error of the differences)."""
     V = verts.astype(np.float64)
     R = rays.astype(np.float64)
     hit = np.nonzero(mask)[0]
@@ -589,7 +612,7 @@ def fd_check(verts, faces, rays, prim, mask, t_tgt, gv, n_coords=512, seed=3):
     axes = rng.integers(0, 3, n_coords)
     order = np.argsort(tri_of)
     sorted_tris = tri_of[order]
-    fd = {h: np.zeros(n_coords) for h in (1e-4, 5e-5, 1e-6)}
+    fd = {h: np.zeros(n_coords) for h in (1e-4, 5e-5, 1e-6, 1e-7)}
     for k, (vid, ax) in enumerate(zip(vids, axes)):
         tris = np.nonzero(np.any(F == vid, axis=1))[0]
         lo = np.searchsorted(sorted_tris, tris, "left")
@@ -613,11 +636,25 @@ def fd_check(verts, faces, rays, prim, mask, t_tgt, gv, n_coords=512, seed=3):
         for h in fd:
             fd[h][k] = (L(h) - L(-h)) / (2 * h)
     ad = gv[vids, axes].astype(np.float64)
+    import torch
+    from bvhraytracer_gb300 import diff as D
+    Vt = torch.from_numpy(V).requires_grad_(True)
+    Rt = torch.from_numpy(R[hit])
+    Ft = torch.from_numpy(F[tri_of].astype(np.int64))
+    t64, _, _ = D.moller_trumbore_torch(Rt[:, 0:3], Rt[:, 4:7], Vt[Ft[:, 0]], Vt[Ft[:, 1]],
+                                        Vt[Ft[:, 2]])
+    g64, = torch.autograd.grad(((t64 - torch.from_numpy(t_tgt[hit])) ** 2).sum(), (Vt,))
+    exact = g64.numpy()[vids, axes]
 
-    def rel(x):
-        return float(np.linalg.norm(ad - x) / max(np.linalg.norm(x), 1e-300))
-    return {"h=1e-4": rel(fd[1e-4]), "h=1e-6": rel(fd[1e-6]),
-            "richardson(1e-4, 5e-5)": rel((4 * fd[5e-5] - fd[1e-4]) / 3)}
+    def rel(x, ref=None):
+        y = ad if ref is None else ref
+        return float(np.linalg.norm(y - x) / max(np.linalg.norm(x), 1e-300))
+    rich = (4 * fd[5e-5] - fd[1e-4]) / 3
+    return {"h=1e-4": rel(fd[1e-4]), "h=1e-6": rel(fd[1e-6]), "h=1e-7": rel(fd[1e-7]),
+            "richardson(1e-4, 5e-5)": rel(rich), "fp64_autograd": rel(exact),
+            "fd_truncation_vs_fp64_autograd": {
+                "h=1e-4": rel(exact, fd[1e-4]), "h=1e-6": rel(exact, fd[1e-6]),
+                "h=1e-7": rel(exact, fd[1e-7]), "richardson(1e-4, 5e-5)": rel(exact, rich)}}
 
 
 def run_adjoint(a):
@@ -774,6 +811,136 @@ def run_scale(a):
     print(json.dumps(line))
 
 
+def _time_trace(sc, rays, kind, opts, reps, stream):
+    import torch
+    sc.trace(rays, kind=kind, **opts)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        out = sc.trace(rays, kind=kind, **opts)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def run_terrain(a):
+    """The 128 x 128-quad terrain (32,768 triangles), N4L4, 512 x 512 primary
+    rays + 1 shadow ray per hit toward (2, 3, 2): per-ray, ray-stream and
+    persistent kernels, results checked against the oracle, and the oracle's
+    restatement of the ISPC path on every host core on the whole frame."""
+    import torch
+    import bvhraytracer_gb300 as pkg
+    from bvhraytracer_gb300 import scenes as S
+    from oracle import oracle as O
+    dev = torch.device("cuda", 0)
+    tris, rays, light = S.terrain_workload()
+    bvh = pkg.Bvh(tris, 4, 4)
+    sc = pkg.Scene(bvh)
+    d_p = torch.from_numpy(rays).to(dev)
+    cv = O.CompactView(bvh.export_compact())
+    ref = O.trace_instrumented(cv, rays, False, counters=False)
+    prims = ref["hits"].view(np.int32)[:, 0]
+    m, p, n = S.surface(tris, rays, prims)
+    shadow = S.shadow_rays(p, n, light)
+    d_s = torch.from_numpy(shadow).to(dev)
+    ref_s = O.trace_instrumented(cv, shadow, True, counters=False)["occluded"]
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for name, o in (("per_ray", {"scheme": "per_ray"}), ("stream_wg16", {"scheme": "stream"}),
+                    ("persistent", {"scheme": "persistent", "policy": 0, "refill": 16})):
+        ms_p, hp = _time_trace(sc, d_p, "closest", o, a.steps, stream)
+        ms_s, hs = _time_trace(sc, d_s, "any", o, a.steps, stream)
+        ok = (np.array_equal(hp["hits"].cpu().numpy().view(np.uint32), ref["hits"].view(np.uint32))
+              and np.array_equal(hs["occluded"].cpu().numpy(), ref_s))
+        res[name] = {"ms_primary": ms_p, "ms_shadow": ms_s,
+                     "mrays_per_s": (rays.shape[0] + shadow.shape[0]) / ((ms_p + ms_s) / 1e3) / 1e6,
+                     "equal_to_oracle": bool(ok)}
+    sc.status()
+    fv = O.FastView(bvh.export_fast(gang=4))
+    cores = os.cpu_count() or 1
+
+    def cpu_once():
+        t0 = time.perf_counter()
+        O.trace_fast(fv, cv, rays, False, packet=256, threads=cores, counters=False)
+        O.trace_fast(fv, cv, shadow, True, packet=256, threads=cores, counters=False)
+        return time.perf_counter() - t0
+    cpu_once()
+    cpu_s = statistics.median([cpu_once() for _ in range(3)])
+    best = max(res, key=lambda k: res[k]["mrays_per_s"])
+    total = rays.shape[0] + shadow.shape[0]
+    line = {
+        "metric": METRIC, "value": res[best]["mrays_per_s"], "unit": METRIC, "n_gpus": 1,
+        "steps": a.steps, "warmup": 1,
+        "ms_per_step": res[best]["ms_primary"] + res[best]["ms_shadow"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded sine-octave terrain)",
+        "config": {"workload": "terrain 128x128 quads (32,768 triangles) N4L4, 512x512 primary "
+                               "+ 1 shadow per hit", "rays_per_step": int(total),
+                   "by_scheme": res, "best": best,
+                   "l2": "scene and rays (10 MB) fit in L2: a small, cache-resident case"},
+        "cpu_baseline": {"value": total / cpu_s / 1e6, "unit": METRIC, "cores": cores,
+                         "kind": "port", "sample": "the whole frame, fast profile, ray-stream "
+                         "16x16 packets, median of 3 after 1 warm-up"},
+    }
+    print(json.dumps(line))
+
+
+def run_sweep(a):
+    """The 1M-triangle clutter frame for every N, L in {4, 8, 12, 16}^2:
+    plain per-ray against ray-stream traversal (and the persistent kernel),
+    Mrays/s of the whole frame (primary + shadow + 8 AO per hit)."""
+    import torch
+    import bvhraytracer_gb300 as pkg
+    dev = torch.device("cuda", 0)
+    tris, bvh0, primary = make_frame(a)
+    sc0 = pkg.Scene(bvh0)
+    d_p = torch.from_numpy(primary).to(dev)
+    prims = pkg.hit_prims(sc0.trace(d_p)["hits"].cpu().numpy())
+    shadow, ao = secondaries(a, tris, primary, prims)
+    batches = [(d_p, "closest"), (torch.from_numpy(shadow).to(dev), "any"),
+               (torch.from_numpy(ao).to(dev), "any")]
+    n_rays = sum(int(r.shape[0]) for r, _ in batches)
+    stream = torch.cuda.current_stream(dev)
+    table = {}
+    for n in (4, 8, 12, 16):
+        for l in (4, 8, 12, 16):
+            bvh = pkg.Bvh(tris, n, l)
+            sc = pkg.Scene(bvh)
+            row = {}
+            ref = None
+            for name, o in (("per_ray", {"scheme": "per_ray"}),
+                            ("stream_wg16", {"scheme": "stream"}),
+                            ("persistent", {"scheme": "persistent", "policy": 2, "refill": 16})):
+                ms = 0.0
+                outs = []
+                try:
+                    for r, k in batches:
+                        t, out = _time_trace(sc, r, k, o, max(1, a.steps // 2), stream)
+                        ms += t
+                        outs.append(out["hits" if k == "closest" else "occluded"].view(torch.uint8))
+                except pkg.BvhgpuError as e:
+                    row[name] = {"unsupported": str(e)}
+                    continue
+                if ref is None:
+                    ref = outs
+                same = all(torch.equal(x, y) for x, y in zip(outs, ref))
+                row[name] = {"ms": round(ms, 3), "mrays_per_s": round(n_rays / ms / 1e3, 1),
+                             "equal_to_per_ray": bool(same)}
+            sc.status()
+            table[f"N{n}L{l}"] = row
+            del sc, bvh
+    best = max(table, key=lambda k: table[k]["persistent"]["mrays_per_s"])
+    line = {
+        "metric": METRIC, "value": table[best]["persistent"]["mrays_per_s"], "unit": METRIC,
+        "n_gpus": 1, "steps": a.steps, "warmup": 1, "ms_per_step": table[best]["persistent"]["ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded clutter scene standing in for the reference's glTF scenes)",
+        "config": {"workload": workload_name(a).replace(f"N{a.branching}L{a.leaf}", "N,L sweep"),
+                   "rays_per_step": n_rays, "best": best, "by_nl": table},
+    }
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -784,6 +951,10 @@ def main():
         run_adjoint(a)
     elif a.workload == "scale8m":
         run_scale(a)
+    elif a.workload == "terrain":
+        run_terrain(a)
+    elif a.workload == "sweep":
+        run_sweep(a)
     else:
         run_ours(a)
 

@@ -139,6 +139,9 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (wg != 8 && wg != 16)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stream workgroup must be 8 or 16 (64 or 256 rays)");
   c.packet = wg * wg;
+  if (o->save_distance && o->scheme != BVHGPU_PER_RAY)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "save_distance needs the per-ray scheme");
+  c.save_distance = o->save_distance != 0;
   return BVHGPU_OK;
 }
 
@@ -411,7 +414,8 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   if (cfg.scheme == BVHGPU_STREAM &&
       dev::stream_smem_bytes(cfg.packet, a.stack_cap, cfg.count) > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet does not fit shared memory for this tree depth");
-  if (cfg.scheme != BVHGPU_STREAM && (size_t)a.stack_cap * 128 * 4 > 227 * 1024)
+  if (cfg.scheme != BVHGPU_STREAM &&
+      (size_t)a.stack_cap * 128 * 4 * (cfg.save_distance ? 2 : 1) > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
@@ -642,7 +646,7 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t s, float* fastrays, uint64_t n, int
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, hits.data(), nullptr, stream);
   if (rc) return rc;
   const uint32_t lm = (uint32_t)s->layout.leaf_memory;
@@ -670,7 +674,7 @@ int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t s, const float* fastrays,
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, nullptr, occ.data(), stream);
   if (rc) return rc;
   for (uint64_t i = 0; i < n; ++i) result[i] = (uint16_t)(result[i] + occ[i]);

@@ -136,6 +136,45 @@ BVHGPU_DEV bool slab_t(float lx, float ly, float lz, float hx, float hy, float h
   return MM ? slab_mm(lx, ly, lz, hx, hy, hz, r, tmax) : slab(lx, ly, lz, hx, hy, hz, r, tmax);
 }
 
+// The slab test that also returns the box's entry distance t0: the
+// `distance` of aabbCheck(ray, id, distance) (compactNode.h:280-313) and the
+// distances[] of aabbIntersect{N}, kept on the stack by the save-distance
+// traversals. For NaN-free rays the IEEE form gives the same t0 up to the
+// sign of a zero, which the later `t0 > tMax` test does not observe.
+template <bool MM>
+BVHGPU_DEV bool slab_dist(float lx, float ly, float lz, float hx, float hy, float hz,
+                          const Ray& r, float tmax, float& t0_out) {
+  float t0, t1;
+  if (MM) {
+    float tn = (lx - r.o[0]) * r.inv[0], tf = (hx - r.o[0]) * r.inv[0];
+    t0 = fmaxf(fminf(tn, tf), 0.0f);
+    t1 = fminf(fmaxf(tn, tf), tmax);
+    tn = (ly - r.o[1]) * r.inv[1]; tf = (hy - r.o[1]) * r.inv[1];
+    t0 = fmaxf(fminf(tn, tf), t0);
+    t1 = fminf(fmaxf(tn, tf), t1);
+    tn = (lz - r.o[2]) * r.inv[2]; tf = (hz - r.o[2]) * r.inv[2];
+    t0 = fmaxf(fminf(tn, tf), t0);
+    t1 = fminf(fmaxf(tn, tf), t1);
+  } else {
+    t0 = 0.0f;
+    t1 = tmax;
+    float tn = (lx - r.o[0]) * r.inv[0], tf = (hx - r.o[0]) * r.inv[0];
+    if (tn > tf) { float t = tn; tn = tf; tf = t; }
+    t0 = rmax(tn, t0);
+    t1 = rmin(tf, t1);
+    tn = (ly - r.o[1]) * r.inv[1]; tf = (hy - r.o[1]) * r.inv[1];
+    if (tn > tf) { float t = tn; tn = tf; tf = t; }
+    t0 = rmax(tn, t0);
+    t1 = rmin(tf, t1);
+    tn = (lz - r.o[2]) * r.inv[2]; tf = (hz - r.o[2]) * r.inv[2];
+    if (tn > tf) { float t = tn; tn = tf; tf = t; }
+    t0 = rmax(tn, t0);
+    t1 = rmin(tf, t1);
+  }
+  t0_out = t0;
+  return t0 <= t1;
+}
+
 // min / max of the reference (MM false) or IEEE min / max (MM true).
 template <bool MM> BVHGPU_DEV float tmin2(float a, float b) { return MM ? fminf(a, b) : rmin(a, b); }
 template <bool MM> BVHGPU_DEV float tmax2(float a, float b) { return MM ? fmaxf(a, b) : rmax(a, b); }

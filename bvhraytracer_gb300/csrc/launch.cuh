@@ -22,6 +22,7 @@ struct LaunchCfg {
   int fmt = BVHGPU_NODES_FP32;  // node record format of the scene
   uint32_t top_nodes = 0;       // persistent scheme: inner records staged in shared memory
   uint32_t stall_bytes = 0;     // failure-detection tests (see bvhgpu_scene_inject_stall)
+  bool save_distance = false;   // per-ray scheme: save-distance traversal (closest hits)
 };
 
 template <typename K>
@@ -36,8 +37,13 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
   if (a.n == 0) return cudaSuccess;
   if (cfg.scheme == BVHGPU_PER_RAY) {
     const int bs = cfg.block;
-    const size_t smem = (size_t)a.stack_cap * bs * 4;
-    auto k = trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT>;
+    // Any-hit rays never lower tMax, so a pushed entry (t0 <= t1 <= tMax) is
+    // never dropped: save-distance any-hit traversal is the plain one.
+    constexpr bool kDist = KIND == BVHGPU_CLOSEST;
+    const bool dist = kDist && cfg.save_distance;
+    const size_t smem = (size_t)a.stack_cap * bs * 4 * (dist ? 2 : 1);
+    auto k = dist ? trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, kDist>
+                  : trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, false>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     const uint64_t grid = (a.n + bs - 1) / bs;

@@ -120,9 +120,12 @@ BVHGPU_DEV float4 q8_row(uint32_t w, float origin, float step, bool up) {
 
 // One inner-node visit: slab-test the children and push the hits.
 // Returns false on stack overflow.
-template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH>
+// DIST: the save-distance traversal; each push also stores the child's entry
+// distance in dstack (same slot layout as stack).
+template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, bool DIST = false>
 BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
-                           int stride, int& sp, int cap, Counters& ctr, int& depth_out) {
+                           int stride, int& sp, int cap, Counters& ctr, int& depth_out,
+                           float* dstack = nullptr) {
   using F = NodeFmt<N, FMT>;
   constexpr int NM = F::NM;
   const uint4 meta = rec_u4<SH>(rec + F::META);
@@ -142,6 +145,7 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
     sz = exp2i((int)(int8_t)((h.w >> 16) & 0xFFu));
   }
   uint32_t hit = 0;
+  float dist[NM];
 #pragma unroll
   for (int q = 0; q < NM / 4; ++q) {
     float4 lx, ly, lz, hx, hy, hz;
@@ -164,8 +168,13 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (4 * q + k < N) {
-        bool h = slab_t<MM>(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k),
-                            f4get(hy, k), f4get(hz, k), r, tmax);
+        bool h;
+        if (DIST)
+          h = slab_dist<MM>(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k),
+                            f4get(hy, k), f4get(hz, k), r, tmax, dist[4 * q + k]);
+        else
+          h = slab_t<MM>(f4get(lx, k), f4get(ly, k), f4get(lz, k), f4get(hx, k),
+                         f4get(hy, k), f4get(hz, k), r, tmax);
         hit |= (uint32_t)h << (4 * q + k);
       }
     }
@@ -217,6 +226,13 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
     const int c = (int)((perm >> (4 * k)) & 15u);
     if (sp >= cap) return false;
     stack[sp * stride] = entry(c);
+    if (DIST) {
+      float tc = 0.f;
+#pragma unroll
+      for (int j = 0; j < NM; ++j)
+        if (j == c) tc = dist[j];
+      dstack[sp * stride] = tc;
+    }
     ++sp;
   }
   return true;
@@ -330,25 +346,25 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
 // Visits with the IEEE min / max forms unless the ray can produce a NaN.
 // Node e is read from the block's shared copy of the top levels when e <
 // top (top == 0: all nodes from global memory).
-template <int N, int PROFILE, int KIND, bool COUNT, int FMT>
+template <int N, int PROFILE, int KIND, bool COUNT, int FMT, bool DIST = false>
 BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_smem, uint32_t top,
                           const Ray& r, float tmax, uint32_t* stack, int stride, int& sp, int cap,
-                          Counters& ctr, int& depth) {
+                          Counters& ctr, int& depth, float* dstack = nullptr) {
   constexpr int REC = NodeFmt<N, FMT>::REC;
   if (e < top) {
     const uint8_t* rec = top_smem + (size_t)e * REC;
     if (r.exact)
-      return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true>(rec, r, tmax, stack, stride,
-                                                                   sp, cap, ctr, depth);
-    return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true>(rec, r, tmax, stack, stride, sp,
-                                                                cap, ctr, depth);
+      return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true, DIST>(
+          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+    return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true, DIST>(
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
   }
   const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
-    return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false>(rec, r, tmax, stack, stride, sp,
-                                                                  cap, ctr, depth);
-  return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false>(rec, r, tmax, stack, stride, sp,
-                                                               cap, ctr, depth);
+    return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false, DIST>(
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+  return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST>(
+      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
 }
 
 template <int PROFILE, int KIND, bool COUNT>
@@ -410,11 +426,18 @@ BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t ri
 // ---------------------------------------------------------------------------
 // Per-ray depth-first traversal: one thread per ray, the traversal stack in
 // shared memory (stack[slot][thread], conflict-free across a warp).
-template <int N, int PROFILE, int KIND, bool COUNT, int FMT>
+// DIST: intersectSaveDistance (fastNodeManager.h:1232-1326) /
+// intersectImmediately(ray, useDistance = true) (compactNode.cpp:623-645):
+// every entry also carries its box's entry distance (in a second shared
+// array after the stack), the root enters with 0, and a pop whose distance
+// exceeds the current tMax is dropped before it is visited or counted.
+template <int N, int PROFILE, int KIND, bool COUNT, int FMT, bool DIST = false>
 __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a) {
   extern __shared__ uint32_t smem[];
   const int stride = blockDim.x;
   uint32_t* stack = smem + threadIdx.x;
+  float* dstack = DIST ? reinterpret_cast<float*>(smem + (size_t)a.stack_cap * stride) + threadIdx.x
+                       : nullptr;
   unsigned long long* hist = nullptr;
   const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (rid >= a.n) return;
@@ -434,11 +457,13 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
   bool hit = false;
   int sp = 0;
   stack[0] = sc.root_entry;
+  if (DIST) dstack[0] = 0.f;
   sp = 1;
   const int cap = a.stack_cap;
   while (sp > 0) {
     --sp;
     const uint32_t e = stack[sp * stride];
+    if (DIST && dstack[sp * stride] > tmax) continue;
     if (e & kLeafBit) {
       if (COUNT && a.depth_hist)
         atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
@@ -449,8 +474,8 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
       }
     } else {
       int depth;
-      if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, nullptr, 0u, r, tmax, stack, stride, sp,
-                                                   cap, ctr, depth)) {
+      if (!node_step<N, PROFILE, KIND, COUNT, FMT, DIST>(sc, e, nullptr, 0u, r, tmax, stack,
+                                                         stride, sp, cap, ctr, depth, dstack)) {
         record_error(sc.status, kDevErrStackOverflow);
         hit = false;
         best = Best();

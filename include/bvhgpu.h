@@ -175,6 +175,13 @@ typedef struct {
                         leaves set aside (any-hit rays without counters; else 0) */
   int32_t refill;    /* persistent scheme: idle lanes of a warp that trigger a refill
                         (1..32; 0 = 8) */
+  int32_t save_distance; /* per-ray scheme, nonzero: the save-distance traversal of
+                        FastNodeManager::intersectSaveDistance (fastNodeManager.h:1232-1326)
+                        and intersectImmediately(ray, useDistance = true)
+                        (compactNode.cpp:604-814): stack entries carry the box entry
+                        distance, pops beyond the current tMax are skipped uncounted.
+                        Any-hit rays are unaffected (their tMax never shrinks). Other
+                        schemes: must be 0. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):

@@ -12,12 +12,15 @@
  *     CompactNodeManager::aabbCheck ....... src/accelerationStructure/compactNode.h:247-278
  *     Triangle::intersect(Ray&) ........... src/primitives/triangle.cpp:52-249
  *     intersectImmediately (per ray) ...... src/accelerationStructure/compactNode.cpp:604-814
+ *       (useDistance: pops whose box entry distance exceeds tMax are
+ *       skipped, compactNode.cpp:623-645)
  *     intersectWideAlternative (stream) ... src/accelerationStructure/compactNode.cpp:357-601
  *   fast profile (the performance renderer, ISPC kernels with gang lanes):
  *     FastRay::FastRay .................... src/fastRay.cpp:3-20
  *     aabbIntersect{N} .................... src/ISPC/rayTracerTemplate.ispc:171-233
  *     triIntersect{L} / triAnyHit{L} ...... src/ISPC/rayTracerTemplate.ispc:26-168
  *     intersect / intersectSecondary ...... src/accelerationStructure/fastNodeManager.h:1328-1493
+ *     intersectSaveDistance ............... fastNodeManager.h:1232-1326
  *     intersectWideAlternative /
  *     intersectSecondaryWideAlternative ... fastNodeManager.h:835-1230
  *
@@ -129,6 +132,22 @@ static int slab(const float lo[3], const float hi[3], const oray_t* r, float tma
     t0 = rmax(tn, t0);
     t1 = rmin(tf, t1);
   }
+  return t0 <= t1;
+}
+
+/* aabbCheck(ray, id, distance) (compactNode.h:280-313) / aabbIntersect's
+ * distances[] output: the same test, also returning the entry distance t0. */
+static int slab_dist(const float lo[3], const float hi[3], const oray_t* r, float tmax,
+                     float* dist) {
+  float t0 = 0, t1 = tmax;
+  for (int a = 0; a < 3; ++a) {
+    float tn = (lo[a] - r->o[a]) * r->inv[a];
+    float tf = (hi[a] - r->o[a]) * r->inv[a];
+    if (tn > tf) { float t = tn; tn = tf; tf = t; }
+    t0 = rmax(tn, t0);
+    t1 = rmin(tf, t1);
+  }
+  *dist = t0;
   return t0 <= t1;
 }
 
@@ -293,7 +312,7 @@ static int leaf_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s) {
 
 /* Inner-node visit: test children in traverseOrderEachAxis order and push. */
 static void node_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s, int32_t* stack,
-                       int* sp, int leaf_sign) {
+                       int* sp, int leaf_sign, float* dstack) {
   uint32_t cb = b->child_begin[id], cc = b->child_count[id];
   s->c.node_visits++;
   if (s->hist) s->hist[b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1]++;
@@ -302,9 +321,11 @@ static void node_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s, int3
     int i = s->r.reverse ? (int)k : (int)(cc - 1 - k);
     uint32_t ch = cb + (uint32_t)ord[i];
     s->c.box_tests++;
-    if (slab(b->lo3 + (size_t)ch * 3, b->hi3 + (size_t)ch * 3, &s->r, s->r.tmax)) {
+    float dist = 0;
+    if (slab_dist(b->lo3 + (size_t)ch * 3, b->hi3 + (size_t)ch * 3, &s->r, s->r.tmax, &dist)) {
       s->c.box_hits++;
       int is_leaf = b->child_count[ch] == 0;
+      if (dstack) dstack[*sp] = dist;
       stack[(*sp)++] = (leaf_sign && is_leaf) ? -(int32_t)ch : (int32_t)ch;
     }
   }
@@ -334,14 +355,19 @@ static int stack_need(const oracle_compact_t* b) {
   return 2048;
 }
 
-/* intersectImmediately(ray, useDistance=false) (compactNode.cpp:604-814). */
+/* intersectImmediately(ray, useDistance) (compactNode.cpp:604-814). With
+ * use_distance each stack entry carries its box's entry distance and a pop
+ * whose distance exceeds the ray's current tMax is skipped uncounted
+ * (compactNode.cpp:637-645); the root enters with distance 0. */
 int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint64_t n, int shadow,
-                              ohit_t* hits, uint8_t* occluded, octr_t* ctrs, uint64_t* hist) {
+                              ohit_t* hits, uint8_t* occluded, octr_t* ctrs, uint64_t* hist,
+                              int use_distance) {
   int cap = stack_need(b);
   int rc = 0;
 #pragma omp parallel
   {
     int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+    float* dstack = use_distance ? (float*)malloc(sizeof(float) * (size_t)cap) : NULL;
     uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 64)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
@@ -353,16 +379,18 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
       make_ray(rays + i * 8, 1, &s.r);
       if (!isnan(rays[i * 8])) {
         int sp = 0;
+        if (dstack) dstack[0] = 0;
         stack[sp++] = 0;
         while (sp > 0) {
           uint32_t id = (uint32_t)stack[--sp];
+          if (dstack && dstack[sp] > s.r.tmax) continue;
           if (b->prim_count[id] != 0) {
             if (leaf_visit(b, id, &s)) {
               s.hit = 1;
               if (shadow) break;
             }
           }
-          if (b->child_count[id] != 0) node_visit(b, id, &s, stack, &sp, 0);
+          if (b->child_count[id] != 0) node_visit(b, id, &s, stack, &sp, 0, dstack);
           if (sp >= cap - 32) { rc = 4; break; }
         }
       }
@@ -374,6 +402,7 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
       for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
       free(h);
     }
+    free(dstack);
     free(stack);
   }
   return rc;
@@ -429,7 +458,7 @@ int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* ray
           ostate_t* s = &st[j];
           int32_t* stk = stacks + (size_t)j * cap;
           int32_t id = stk[--sps[j]];
-          node_visit(b, (uint32_t)id, s, stk, &sps[j], 1);
+          node_visit(b, (uint32_t)id, s, stk, &sps[j], 1, NULL);
           if (sps[j] >= cap - 32) rc = 4;
           if (sps[j] != 0) {
             if (stk[sps[j] - 1] >= 0) nxt[next_node++] = (uint16_t)j;
@@ -544,7 +573,7 @@ static int tri_any_hit(const oracle_fast_t* f, uint32_t begin, int stride, int r
 
 /* aabbIntersect over the node's real children; bit j set if child j is hit. */
 static uint32_t aabb_intersect(const oracle_fast_t* f, const oracle_compact_t* b, uint32_t id,
-                               const oray_t* r) {
+                               const oray_t* r, float* dist) {
   const float* bd = f->bounds + (size_t)id * 6 * f->node_memory;
   int real = f->node_memory;
   if (f->node_memory != f->gang && isnan(bd[f->node_memory * 6 - 1]))
@@ -554,7 +583,11 @@ static uint32_t aabb_intersect(const oracle_fast_t* f, const oracle_compact_t* b
   for (uint32_t j = 0; j < cc; ++j) {
     float lo[3] = {bd[j], bd[j + real], bd[j + real * 2]};
     float hi[3] = {bd[j + real * 3], bd[j + real * 4], bd[j + real * 5]};
-    if (slab(lo, hi, r, r->tmax)) mask |= 1u << j;
+    float t0 = 0;
+    if (slab_dist(lo, hi, r, r->tmax, &t0)) {
+      mask |= 1u << j;
+      if (dist) dist[j] = t0;
+    }
   }
   return mask;
 }
@@ -593,8 +626,10 @@ static void fast_leaf(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
 }
 
 static void fast_node(const oracle_fast_t* f, const oracle_compact_t* b, uint32_t id,
-                      fstate_t* s, int32_t* stack, int* sp, int leaf_sign, uint64_t* hist) {
-  uint32_t mask = aabb_intersect(f, b, id, &s->r);
+                      fstate_t* s, int32_t* stack, int* sp, int leaf_sign, uint64_t* hist,
+                      float* dstack) {
+  float dist[16];
+  uint32_t mask = aabb_intersect(f, b, id, &s->r, dist);
   uint32_t cc = b->child_count[id];
   uint32_t cbeg = f->begin[id];
   s->c.node_visits++;
@@ -606,6 +641,7 @@ static void fast_node(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
     for (uint32_t j = 0; j < cc; ++j)
       if (mask >> j & 1u) {
         int inner = (f->child_type[id] >> j) & 1u;
+        if (dstack) dstack[*sp] = dist[j];
         stack[(*sp)++] = (leaf_sign && !inner) ? -(int32_t)(cbeg + j) : (int32_t)(cbeg + j);
       }
   } else {
@@ -615,6 +651,7 @@ static void fast_node(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
       int j = ord[i];
       if (mask >> j & 1u) {
         int inner = (f->child_type[id] >> j) & 1u;
+        if (dstack) dstack[*sp] = dist[j];
         stack[(*sp)++] = (leaf_sign && !inner) ? -(int32_t)(cbeg + j) : (int32_t)(cbeg + j);
       }
     }
@@ -667,11 +704,14 @@ static uint32_t* leaf_nodes(const oracle_fast_t* f, const oracle_compact_t* b) {
 /* FastNodeManager::intersect / intersectSecondary over n rays
  * (fastNodeManager.h:1328-1493), or, with packet > 0, the stream versions
  * intersectWideAlternative / intersectSecondaryWideAlternative over packets
- * of `packet` consecutive rays. threads <= 0: all available. */
+ * of `packet` consecutive rays. threads <= 0: all available. use_distance
+ * (per ray only): intersectSaveDistance (fastNodeManager.h:1232-1326), whose
+ * stack entries carry aabbIntersect's t0 and whose pops with t0 > tMax are
+ * skipped; the root enters with distance 0. */
 int oracle_trace_fast(const oracle_fast_t* f, const oracle_compact_t* b, const float* rays,
                       uint64_t n, int any, int packet, int threads, ohit_t* hits,
                       uint8_t* occluded, int32_t* leaf_index, int8_t* tri_index, octr_t* ctrs,
-                      uint64_t* hist) {
+                      uint64_t* hist, int use_distance) {
   const int cap = 2048;
   int rc = 0;
   uint32_t* ln = leaf_nodes(f, b);
@@ -685,6 +725,7 @@ int oracle_trace_fast(const oracle_fast_t* f, const oracle_compact_t* b, const f
 #pragma omp parallel num_threads(nt)
     {
       int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * cap);
+      float* dstack = use_distance ? (float*)malloc(sizeof(float) * cap) : NULL;
       uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 64)
       for (int64_t i = 0; i < (int64_t)n; ++i) {
@@ -695,14 +736,16 @@ int oracle_trace_fast(const oracle_fast_t* f, const oracle_compact_t* b, const f
         make_ray(rays + i * 8, 0, &s.r);
         if (!isnan(rays[i * 8])) {
           int sp = 0;
+          if (dstack) dstack[0] = 0;
           stack[sp++] = 0;
           while (sp > 0) {
             uint32_t id = (uint32_t)stack[--sp];
+            if (dstack && dstack[sp] > s.r.tmax) continue;
             if (b->child_count[id] == 0) {
               fast_leaf(f, b, id, &s, h);
               if (any && s.hit) break;
             } else {
-              fast_node(f, b, id, &s, stack, &sp, 0, h);
+              fast_node(f, b, id, &s, stack, &sp, 0, h, dstack);
             }
             if (sp >= cap - 32) { rc = 4; break; }
           }
@@ -716,9 +759,11 @@ int oracle_trace_fast(const oracle_fast_t* f, const oracle_compact_t* b, const f
         for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
         free(h);
       }
+      free(dstack);
       free(stack);
     }
   } else {
+    if (use_distance) { free(ln); return 1; }
     int64_t npk = (int64_t)((n + (uint64_t)packet - 1) / (uint64_t)packet);
 #pragma omp parallel num_threads(nt)
     {
@@ -757,7 +802,7 @@ int oracle_trace_fast(const oracle_fast_t* f, const oracle_compact_t* b, const f
             int j = cur[i];
             int32_t* stk = stacks + (size_t)j * cap;
             int32_t id = stk[--sps[j]];
-            fast_node(f, b, (uint32_t)id, &st[j], stk, &sps[j], 1, h);
+            fast_node(f, b, (uint32_t)id, &st[j], stk, &sps[j], 1, h, NULL);
             if (sps[j] != 0) {
               if (stk[sps[j] - 1] >= 0 && !(stk[sps[j] - 1] == 0 && root_leaf))
                 nxt[next_node++] = (uint16_t)j;

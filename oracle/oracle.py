@@ -40,13 +40,14 @@ def lib() -> C.CDLL:
             L = C.CDLL(str(build()))
             L.oracle_trace_instrumented.restype = C.c_int
             L.oracle_trace_instrumented.argtypes = [C.POINTER(_Compact), _P, C.c_uint64, C.c_int,
-                                                    _P, _P, _P, _P]
+                                                    _P, _P, _P, _P, C.c_int]
             L.oracle_trace_instrumented_stream.restype = C.c_int
             L.oracle_trace_instrumented_stream.argtypes = [C.POINTER(_Compact), _P, C.c_uint64,
                                                            C.c_int, C.c_int, _P, _P, _P, _P]
             L.oracle_trace_fast.restype = C.c_int
             L.oracle_trace_fast.argtypes = [C.POINTER(_Fast), C.POINTER(_Compact), _P, C.c_uint64,
-                                            C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P]
+                                            C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
+                                            C.c_int]
             L.oracle_fp64_pairs.restype = None
             L.oracle_fp64_pairs.argtypes = [_P, _P, C.c_uint64, C.c_int, _P]
             _lib = L
@@ -77,21 +78,23 @@ class FastView:
 
 
 def trace_instrumented(view: CompactView, rays: np.ndarray, shadow: bool, packet: int = 0,
-                       counters: bool = True) -> dict:
-    """CompactNodeManager::intersectImmediately (packet == 0) or
-    intersectWideAlternative over packets of ``packet`` rays."""
+                       counters: bool = True, use_distance: bool = False) -> dict:
+    """CompactNodeManager::intersectImmediately(ray, use_distance) (packet ==
+    0) or intersectWideAlternative over packets of ``packet`` rays."""
     rays = np.ascontiguousarray(rays, np.float32)
     n = rays.shape[0]
     hits = None if shadow else np.zeros((n, 4), np.float32)
     occ = np.zeros(n, np.uint8) if shadow else None
     ctr = np.zeros((n, 8), np.uint32) if counters else None
     hist = np.zeros((2, 64), np.uint64) if counters else None
+    if packet and use_distance:
+        raise ValueError("use_distance is a per-ray traversal")
     if packet:
         rc = lib().oracle_trace_instrumented_stream(C.byref(view.c), _p(rays), n, int(shadow),
                                                      packet, _p(hits), _p(occ), _p(ctr), _p(hist))
     else:
         rc = lib().oracle_trace_instrumented(C.byref(view.c), _p(rays), n, int(shadow), _p(hits),
-                                             _p(occ), _p(ctr), _p(hist))
+                                             _p(occ), _p(ctr), _p(hist), int(use_distance))
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist}
@@ -99,9 +102,10 @@ def trace_instrumented(view: CompactView, rays: np.ndarray, shadow: bool, packet
 
 def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: bool,
                packet: int = 0, threads: int = 0, counters: bool = True,
-               outputs: bool = True) -> dict:
+               outputs: bool = True, use_distance: bool = False) -> dict:
     """FastNodeManager::intersect / intersectSecondary (packet == 0) or the
-    WideAlternative stream versions, with ISPC gang-lane semantics."""
+    WideAlternative stream versions, with ISPC gang-lane semantics;
+    ``use_distance``: intersectSaveDistance (per ray)."""
     rays = np.ascontiguousarray(rays, np.float32)
     n = rays.shape[0]
     hits = np.zeros((n, 4), np.float32) if (outputs and not any_hit) else None
@@ -112,7 +116,7 @@ def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: b
     hist = np.zeros((2, 64), np.uint64) if counters else None
     rc = lib().oracle_trace_fast(C.byref(fview.c), C.byref(cview.c), _p(rays), n, int(any_hit),
                                  packet, threads, _p(hits), _p(occ), _p(li), _p(ti), _p(ctr),
-                                 _p(hist))
+                                 _p(hist), int(use_distance))
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return {"hits": hits, "occluded": occ, "leaf_index": li, "tri_index": ti, "counters": ctr,

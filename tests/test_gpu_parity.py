@@ -313,3 +313,34 @@ def test_q8_nodes_keep_hits_identical(n, l):
     s8.status()
     with pytest.raises(pkg.BvhgpuError):
         s8.trace(dev(rays), scheme="stream")
+
+
+@pytest.mark.parametrize("n,l", [(4, 4), (8, 8), (16, 4)])
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+@pytest.mark.parametrize("fmt", ["fp32", "q8"])
+def test_save_distance_traversal(n, l, profile, fmt):
+    """intersectSaveDistance / intersectImmediately(ray, useDistance=true):
+    hits, counters and depth histograms bit-exact against the oracle; any-hit
+    rays are unaffected."""
+    tris, b, cv = TS.bvh("clutter120", n, l)
+    fv = O.FastView(b.export_fast())
+    rays = TS.clutter_rays(tris)
+    scene = pkg.Scene(b, node_format=fmt)
+    if profile == "instrumented":
+        ref = O.trace_instrumented(cv, rays, False, use_distance=True)
+    else:
+        ref = O.trace_fast(fv, cv, rays, False, use_distance=True)
+    got = scene.trace(dev(rays), profile=profile, save_distance=True, counters=True,
+                      depth_hist=True)
+    if fmt == "fp32":
+        check_closest(got, ref)
+    check_closest(scene.trace(dev(rays), profile=profile, save_distance=True), ref,
+                  counters=False)
+    prims = pkg.hit_prims(ref["hits"])
+    _, ao = TS.secondary(tris, rays, prims, LIGHT)
+    plain = scene.trace(dev(ao), kind="any", profile=profile)["occluded"]
+    dist = scene.trace(dev(ao), kind="any", profile=profile, save_distance=True)["occluded"]
+    assert torch.equal(plain, dist)
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace(dev(rays), scheme="persistent", save_distance=True)
+    scene.status()

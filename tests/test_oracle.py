@@ -241,3 +241,51 @@ def test_scenes_sizes():
     assert TS.terrain_case()[1].shape == (512 * 512, 8)
     assert S._uv_sphere(np.zeros(3), 1.0).shape == (256, 9)
     assert S._box(np.zeros(3), np.ones(3)).shape == (192, 9)
+
+
+# Root with two leaf children on the z axis: a triangle at z = 5 and one at
+# z = 8 behind it.
+NEAR_FAR = [(1, 2, 0, 0, 0), (0, 0, 0, 1, 1), (0, 0, 1, 1, 1)]
+NEAR_FAR_TRIS = [tri_at(0, 5.0), tri_at(0, 8.0)]
+
+
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+def test_kat_save_distance_skips_far_leaf(profile):
+    # A ray along +z pops the near leaf first (hit at t = 5, tMax = 5); the far
+    # leaf was pushed with entry distance 8 > 5, so the save-distance traversal
+    # drops it uncounted (intersectSaveDistance, fastNodeManager.h:1256-1259;
+    # compactNode.cpp:637-645). The plain traversal visits and tests it.
+    cv, fv = views(NEAR_FAR, NEAR_FAR_TRIS)
+    r = ray((0.25, 0.25, 0), (0, 0, 1))
+
+    def run(dist):
+        if profile == "instrumented":
+            return O.trace_instrumented(cv, r, False, use_distance=dist)
+        return O.trace_fast(fv, cv, r, False, use_distance=dist)
+
+    plain, dist = run(False), run(True)
+    for res in (plain, dist):
+        assert res["hits"][0].view(np.int32)[0] == 0 and res["hits"][0][1] == 5.0
+    assert plain["counters"][0].tolist() == [1, 2, 2, 2, 2, 1, 2, 0]
+    assert dist["counters"][0].tolist() == [1, 1, 2, 2, 1, 1, 2, 0]
+    # from the far side the far leaf is near: nothing is skipped
+    back = ray((0.25, 0.25, 10), (0, 0, -1))
+    b = (O.trace_instrumented(cv, back, False, use_distance=True) if profile == "instrumented"
+         else O.trace_fast(fv, cv, back, False, use_distance=True))
+    assert b["hits"][0].view(np.int32)[0] == 1 and b["counters"][0][1] == 1
+
+
+@pytest.mark.parametrize("n,l", [(4, 4), (8, 8)])
+def test_save_distance_same_hits_fewer_visits(n, l):
+    tris, b, cv = TS.bvh("clutter120", n, l)
+    fv = O.FastView(b.export_fast())
+    rays = TS.clutter_rays(tris)
+    for run in (lambda d: O.trace_instrumented(cv, rays, False, use_distance=d),
+                lambda d: O.trace_fast(fv, cv, rays, False, use_distance=d)):
+        p, d = run(False), run(True)
+        assert np.array_equal(p["hits"].view(np.uint32), d["hits"].view(np.uint32))
+        assert np.all(d["counters"][:, 0] <= p["counters"][:, 0])
+        assert np.all(d["counters"][:, 1] <= p["counters"][:, 1])
+        assert d["counters"][:, 1].sum() < p["counters"][:, 1].sum()
+    with pytest.raises(ValueError):
+        O.trace_instrumented(cv, rays, False, packet=64, use_distance=True)
