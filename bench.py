@@ -396,7 +396,7 @@ def run_ours(a):
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
             and dom_opts.get("policy") == NCU_TRAFFIC_PER_AO_RAY["policy"]
-            and chosen[dom][0].node_format == "fp32"):
+            and not dom_opts.get("reorder") and chosen[dom][0].node_format == "fp32"):
         traffic = NCU_TRAFFIC_PER_AO_RAY["bytes"] * int(batches[dom][0].shape[0])
 
     compare = {}
@@ -446,7 +446,9 @@ def run_ours(a):
                     "matches_device_results": bool(e2e_ok)},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": len(batches) * a.steps,
+            # per trace call: one traversal launch, plus four reorder passes
+            # (bin, scan, scan, scatter) when the plan groups the rays first
+            "gpu_launches": sum(1 + (4 if o.get("reorder") else 0) for _, o in chosen) * a.steps,
         }
         print(json.dumps(line))
     if world > 1:

@@ -158,8 +158,8 @@ class Scene:
     def trace(self, rays, *, kind: str = "closest", scheme: str = "per_ray",
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
               policy: int = 0, refill: int = 0, counters: bool = False,
-              depth_hist: bool = False, save_distance: bool = False, out=None,
-              stream=None) -> dict:
+              depth_hist: bool = False, save_distance: bool = False, reorder: int = 0,
+              out=None, stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -167,6 +167,8 @@ class Scene:
         ``[2, 64]`` int64 when requested. Asynchronous on ``stream``
         (default: torch's current stream). ``save_distance`` (per-ray scheme):
         intersectSaveDistance / intersectImmediately(ray, useDistance=true).
+        ``reorder`` = K > 0 traces the rays grouped into 6 K^2 direction bins
+        (results identical, in input order).
         """
         import torch
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
@@ -191,7 +193,7 @@ class Scene:
             res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
             hh = _ptr(res["depth_hist"])
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
-                        int(save_distance))
+                        int(save_distance), int(reorder))
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
                                      C.c_void_p(s.cuda_stream)))
@@ -200,7 +202,8 @@ class Scene:
     def trace_host(self, rays: np.ndarray, *, kind: str = "closest", scheme: str = "per_ray",
                    profile: str = "instrumented", workgroup: int = 16, block: int = 128,
                    policy: int = 0, refill: int = 0, save_distance: bool = False,
-                   out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+                   reorder: int = 0, out: Optional[np.ndarray] = None,
+                   stream=None) -> np.ndarray:
         """Host rays in, host results out (copies inside the call)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = rays.shape[0]
@@ -208,7 +211,7 @@ class Scene:
         if out is None:
             out = (np.empty((n, 4), np.float32) if k == N.CLOSEST else np.empty(n, np.uint8))
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
-                        int(save_distance))
+                        int(save_distance), int(reorder))
         sp = 0
         if stream is not None:
             sp = stream.cuda_stream

@@ -4,8 +4,9 @@ with the lowest measured time.
 Candidates cover the knobs the reference exposes in config.txt (branching
 factor N and leaf size L: a scene is built per (N, L) pair) plus the GPU
 ones: traversal scheme (per-ray, ray-stream with its workgroup size,
-persistent with its refill threshold and divergence policy), node format
-(FP32 / Q8) and how many top levels are staged in shared memory. Every
+persistent with its refill threshold and divergence policy), whether the rays
+are grouped by direction first (reorder), node format (FP32 / Q8) and how many
+top levels are staged in shared memory. Every
 candidate gives the same hits (the kernels are bit-exact with one another and
 Q8 keeps hit sets identical), so the choice only changes speed.
 """
@@ -26,6 +27,9 @@ DEFAULT_OPTIONS = (
     {"scheme": "persistent", "policy": 1, "refill": 8},
     {"scheme": "persistent", "policy": 2, "refill": 8},
     {"scheme": "persistent", "policy": 2, "refill": 16},
+    {"scheme": "per_ray", "block": 128, "reorder": 8},
+    {"scheme": "persistent", "policy": 0, "refill": 16, "reorder": 8},
+    {"scheme": "persistent", "policy": 2, "refill": 16, "reorder": 8},
 )
 DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
 

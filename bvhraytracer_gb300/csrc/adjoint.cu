@@ -9,21 +9,82 @@
 //   e1 = p1 - p0, e2 = p2 - p0, s1 = d x e2, div = s1.e1, inv = 1/div,
 //   s = o - p0, b1 = (s.s1) inv, s2 = s x e1, b2 = (d.s2) inv,
 //   t = (e2.s2) inv.
-// Vertex gradients are accumulated per triangle (9 floats) with atomics; the
-// caller scatters them to shared vertices.
+// The reverse pass runs in double-float arithmetic (pairs of floats, see
+// below), so the FP32 gradients it returns are the correctly rounded values
+// of a ~48-bit evaluation even for grazing rays, where a float evaluation of
+// s1.e1 cancels. Vertex gradients are accumulated per triangle (9 floats)
+// with atomics; the caller scatters them to shared vertices.
 #include "adjoint.cuh"
 
 namespace bvhgpu {
 namespace dev {
 
-BVHGPU_DEV float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-BVHGPU_DEV float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-BVHGPU_DEV float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-BVHGPU_DEV float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
-BVHGPU_DEV float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-BVHGPU_DEV float3 cross3(float3 a, float3 b) {
-  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+// ---- double-float arithmetic -------------------------------------------
+// A value is an unevaluated sum hi + lo of two floats (about 48 significant
+// bits). Error-free transformations: Knuth's TwoSum, Dekker's TwoProduct by
+// fused multiply-add; df_add / df_mul / df_recip follow the double-double
+// algorithms of Hida, Li and Bailey (2001) with float components. The kernels
+// are compiled without FMA contraction, so the compensations are not folded.
+struct df {
+  float hi, lo;
+};
+
+BVHGPU_DEV df df_of(float a) { return df{a, 0.f}; }
+BVHGPU_DEV df quick_two_sum(float a, float b) {
+  const float s = a + b;
+  return df{s, b - (s - a)};
 }
+BVHGPU_DEV df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return df{s, (a - (s - bb)) + (b - bb)};
+}
+BVHGPU_DEV df two_prod(float a, float b) {
+  const float p = a * b;
+  return df{p, __fmaf_rn(a, b, -p)};
+}
+BVHGPU_DEV df df_add(df x, df y) {
+  df s = two_sum(x.hi, y.hi);
+  const df t = two_sum(x.lo, y.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+BVHGPU_DEV df df_neg(df x) { return df{-x.hi, -x.lo}; }
+BVHGPU_DEV df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+BVHGPU_DEV df df_mul(df x, df y) {
+  df p = two_prod(x.hi, y.hi);
+  p.lo += x.hi * y.lo + x.lo * y.hi;
+  return quick_two_sum(p.hi, p.lo);
+}
+BVHGPU_DEV df df_recip(df x) {
+  // One Newton step from the float reciprocal: r + r (1 - x r).
+  const float r = 1.f / x.hi;
+  const df e = df_sub(df_of(1.f), df_mul(x, df_of(r)));
+  return df_add(df_of(r), df_mul(df_of(r), e));
+}
+BVHGPU_DEV float df_float(df x) { return x.hi + x.lo; }
+
+struct df3 {
+  df x, y, z;
+};
+BVHGPU_DEV df3 d3(df x, df y, df z) { return df3{x, y, z}; }
+BVHGPU_DEV df3 d3f(float x, float y, float z) { return df3{df_of(x), df_of(y), df_of(z)}; }
+// a - b of float vectors, exact.
+BVHGPU_DEV df3 sub3f(float3 a, float3 b) {
+  return df3{two_sum(a.x, -b.x), two_sum(a.y, -b.y), two_sum(a.z, -b.z)};
+}
+BVHGPU_DEV df3 add3(df3 a, df3 b) { return d3(df_add(a.x, b.x), df_add(a.y, b.y), df_add(a.z, b.z)); }
+BVHGPU_DEV df3 mul3(df3 a, df s) { return d3(df_mul(a.x, s), df_mul(a.y, s), df_mul(a.z, s)); }
+BVHGPU_DEV df dot3(df3 a, df3 b) {
+  return df_add(df_add(df_mul(a.x, b.x), df_mul(a.y, b.y)), df_mul(a.z, b.z));
+}
+BVHGPU_DEV df3 cross3(df3 a, df3 b) {
+  return d3(df_sub(df_mul(a.y, b.z), df_mul(a.z, b.y)), df_sub(df_mul(a.z, b.x), df_mul(a.x, b.z)),
+            df_sub(df_mul(a.x, b.y), df_mul(a.y, b.x)));
+}
+BVHGPU_DEV float3 to_f3(df3 a) { return make_float3(df_float(a.x), df_float(a.y), df_float(a.z)); }
 
 template <int N>
 __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a) {
@@ -74,36 +135,38 @@ __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a
     if (isnan(last)) stride_l = (int)blk[sc.leaf_memory * 9 - 2];
   }
   const int i = best.lane;
-  const float3 p0 = f3(blk[0 * stride_l + i], blk[1 * stride_l + i], blk[2 * stride_l + i]);
-  const float3 p1 = f3(blk[3 * stride_l + i], blk[4 * stride_l + i], blk[5 * stride_l + i]);
-  const float3 p2 = f3(blk[6 * stride_l + i], blk[7 * stride_l + i], blk[8 * stride_l + i]);
+  const float3 p0 = make_float3(blk[0 * stride_l + i], blk[1 * stride_l + i], blk[2 * stride_l + i]);
+  const float3 p1 = make_float3(blk[3 * stride_l + i], blk[4 * stride_l + i], blk[5 * stride_l + i]);
+  const float3 p2 = make_float3(blk[6 * stride_l + i], blk[7 * stride_l + i], blk[8 * stride_l + i]);
   const uint32_t prim = __ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + i);
-  const float3 o = f3(r.o[0], r.o[1], r.o[2]);
-  const float3 d = f3(r.d[0], r.d[1], r.d[2]);
+  const float3 of = make_float3(r.o[0], r.o[1], r.o[2]);
+  const df3 d = d3f(r.d[0], r.d[1], r.d[2]);
 
-  // Forward intermediates.
-  const float3 e1 = sub3(p1, p0), e2 = sub3(p2, p0);
-  const float3 s1 = cross3(d, e2);
-  const float div = dot3(s1, e1);
-  const float inv = 1.f / div;
-  const float3 s = sub3(o, p0);
-  const float n1 = dot3(s, s1);
-  const float3 s2 = cross3(s, e1);
-  const float n2 = dot3(d, s2);
-  const float n3 = dot3(e2, s2);
+  // Forward intermediates in double-float: the differences of float inputs
+  // are exact, so a grazing ray (small s1.e1) loses no bits to cancellation
+  // before the reverse pass divides by it.
+  const df3 e1 = sub3f(p1, p0), e2 = sub3f(p2, p0);
+  const df3 s1 = cross3(d, e2);
+  const df div = dot3(s1, e1);
+  const df inv = df_recip(div);
+  const df3 s = sub3f(of, p0);
+  const df n1 = dot3(s, s1);
+  const df3 s2 = cross3(s, e1);
+  const df n2 = dot3(d, s2);
+  const df n3 = dot3(e2, s2);
 
   // Reverse pass.
   const float4 g = a.grad_hits[rid];
-  const float gt = g.y, gb1 = g.z, gb2 = g.w;
-  const float g_n1 = gb1 * inv, g_n2 = gb2 * inv, g_n3 = gt * inv;
-  const float g_inv = gb1 * n1 + gb2 * n2 + gt * n3;
-  const float g_div = -g_inv * inv * inv;
-  float3 g_s = mul3(s1, g_n1);
-  float3 g_s1 = add3(mul3(s, g_n1), mul3(e1, g_div));
-  float3 g_d = mul3(s2, g_n2);
-  float3 g_s2 = add3(mul3(d, g_n2), mul3(e2, g_n3));
-  float3 g_e2 = mul3(s2, g_n3);
-  float3 g_e1 = mul3(s1, g_div);
+  const df gt = df_of(g.y), gb1 = df_of(g.z), gb2 = df_of(g.w);
+  const df g_n1 = df_mul(gb1, inv), g_n2 = df_mul(gb2, inv), g_n3 = df_mul(gt, inv);
+  const df g_inv = df_add(df_add(df_mul(gb1, n1), df_mul(gb2, n2)), df_mul(gt, n3));
+  const df g_div = df_neg(df_mul(df_mul(g_inv, inv), inv));
+  df3 g_s = mul3(s1, g_n1);
+  const df3 g_s1 = add3(mul3(s, g_n1), mul3(e1, g_div));
+  df3 g_d = mul3(s2, g_n2);
+  const df3 g_s2 = add3(mul3(d, g_n2), mul3(e2, g_n3));
+  df3 g_e2 = mul3(s2, g_n3);
+  df3 g_e1 = mul3(s1, g_div);
   // s1 = d x e2
   g_d = add3(g_d, cross3(e2, g_s1));
   g_e2 = add3(g_e2, cross3(g_s1, d));
@@ -111,16 +174,18 @@ __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a
   g_s = add3(g_s, cross3(e1, g_s2));
   g_e1 = add3(g_e1, cross3(g_s2, s));
   // s = o - p0, e1 = p1 - p0, e2 = p2 - p0
-  const float3 g_o = g_s;
-  const float3 g_p1 = g_e1, g_p2 = g_e2;
-  const float3 g_p0 = f3(-(g_s.x + g_e1.x + g_e2.x), -(g_s.y + g_e1.y + g_e2.y),
-                         -(g_s.z + g_e1.z + g_e2.z));
+  const float3 g_o = to_f3(g_s);
+  const float3 g_dd = to_f3(g_d);
+  const float3 g_p1 = to_f3(g_e1), g_p2 = to_f3(g_e2);
+  const float3 g_p0 = to_f3(df3{df_neg(df_add(df_add(g_s.x, g_e1.x), g_e2.x)),
+                                df_neg(df_add(df_add(g_s.y, g_e1.y), g_e2.y)),
+                                df_neg(df_add(df_add(g_s.z, g_e1.z), g_e2.z))});
   float* gt9 = a.grad_tri9 + (size_t)prim * 9;
   atomicAdd(gt9 + 0, g_p0.x); atomicAdd(gt9 + 1, g_p0.y); atomicAdd(gt9 + 2, g_p0.z);
   atomicAdd(gt9 + 3, g_p1.x); atomicAdd(gt9 + 4, g_p1.y); atomicAdd(gt9 + 5, g_p1.z);
   atomicAdd(gt9 + 6, g_p2.x); atomicAdd(gt9 + 7, g_p2.y); atomicAdd(gt9 + 8, g_p2.z);
   reinterpret_cast<float4*>(gr)[0] = make_float4(g_o.x, g_o.y, g_o.z, 0.f);
-  reinterpret_cast<float4*>(gr)[1] = make_float4(g_d.x, g_d.y, g_d.z, 0.f);
+  reinterpret_cast<float4*>(gr)[1] = make_float4(g_dd.x, g_dd.y, g_dd.z, 0.f);
 }
 
 cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s) {

@@ -17,6 +17,7 @@
 #include "bvhgpu.h"
 #include "bvhgpu_status.hpp"
 #include "launch.cuh"
+#include "reorder.cuh"
 #include "batched.cuh"
 #include "adjoint.cuh"
 
@@ -142,6 +143,9 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (o->save_distance && o->scheme != BVHGPU_PER_RAY)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "save_distance needs the per-ray scheme");
   c.save_distance = o->save_distance != 0;
+  if (o->reorder < 0 || o->reorder > dev::kReorderMaxK)
+    return set_error(BVHGPU_ERR_BAD_ARG, "reorder must be 0..32 bins per cube face side");
+  c.reorder = o->reorder;
   return BVHGPU_OK;
 }
 
@@ -173,6 +177,40 @@ static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
   }
   if (e != cudaSuccess) return cuda_error(e, "trace launch");
   return BVHGPU_OK;
+}
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// launch() after grouping the rays by direction when cfg.reorder > 0: the
+// rays are copied in bin order to stream-ordered scratch, traced from there,
+// and every result is written to its input slot. The scratch (about 38 bytes
+// per ray) is allocated and freed on the stream.
+static int launch_reordered(bvhgpu_scene_t s, dev::TraceArgs a, const dev::LaunchCfg& cfg,
+                            cudaStream_t st) {
+  if (cfg.reorder <= 0 || a.n < 2) return launch(s, a, cfg, st);
+  if (a.n > 0xFFFFFFFFull)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "reorder: at most 2^32 - 1 rays per call");
+  const size_t ray_bytes = align256(a.n * sizeof(bvhgpu_ray_t));
+  const size_t perm_bytes = align256(a.n * 4);
+  const size_t bytes = ray_bytes + perm_bytes + dev::reorder_scratch_bytes(a.n, cfg.reorder);
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "reorder scratch allocation failed");
+  auto* sorted = reinterpret_cast<bvhgpu_ray_t*>(p);
+  auto* perm = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(p) + ray_bytes);
+  e = dev::reorder_rays(a.rays, a.n, cfg.reorder, sorted, perm,
+                        static_cast<uint8_t*>(p) + ray_bytes + perm_bytes, st);
+  int rc;
+  if (e != cudaSuccess) {
+    rc = cuda_error(e, "reorder");
+  } else {
+    a.rays = sorted;
+    a.out_index = perm;
+    rc = launch(s, a, cfg, st);
+  }
+  e = cudaFreeAsync(p, st);
+  if (rc == BVHGPU_OK && e != cudaSuccess) rc = cuda_error(e, "reorder scratch free");
+  return rc;
 }
 
 extern "C" {
@@ -419,7 +457,7 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  return launch(s, a, cfg, (cudaStream_t)stream);
+  return launch_reordered(s, a, cfg, (cudaStream_t)stream);
 }
 
 int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
@@ -461,7 +499,7 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   a.counters = nullptr;
   a.depth_hist = nullptr;
   a.stack_cap = stack_cap(s);
-  rc = launch(s, a, cfg, st);
+  rc = launch_reordered(s, a, cfg, st);
   if (rc) return rc;
   e = cudaMemcpyAsync(closest ? (void*)hits : (void*)occluded, d_out,
                       closest ? n * sizeof(bvhgpu_hit_t) : n, cudaMemcpyDeviceToHost, st);
@@ -646,7 +684,7 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t s, float* fastrays, uint64_t n, int
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, hits.data(), nullptr, stream);
   if (rc) return rc;
   const uint32_t lm = (uint32_t)s->layout.leaf_memory;
@@ -674,7 +712,7 @@ int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t s, const float* fastrays,
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, nullptr, occ.data(), stream);
   if (rc) return rc;
   for (uint64_t i = 0; i < n; ++i) result[i] = (uint16_t)(result[i] + occ[i]);
@@ -760,6 +798,8 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
   dev::LaunchCfg cfg;
   int rc = check_opts(opts, cfg);
   if (rc) return rc;
+  if (cfg.reorder)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "no-alloc trace: reorder needs scratch memory");
   cfg.scheme = BVHGPU_PERSISTENT;
   for (int i = 0; i < n_batches; ++i) {
     const bvhgpu_batch_t& b = batches[i];

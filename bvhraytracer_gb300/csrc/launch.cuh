@@ -23,6 +23,7 @@ struct LaunchCfg {
   uint32_t top_nodes = 0;       // persistent scheme: inner records staged in shared memory
   uint32_t stall_bytes = 0;     // failure-detection tests (see bvhgpu_scene_inject_stall)
   bool save_distance = false;   // per-ray scheme: save-distance traversal (closest hits)
+  int reorder = 0;              // > 0: group rays into 6 reorder^2 direction bins first
 };
 
 template <typename K>

@@ -40,7 +40,14 @@ struct TraceArgs {
   uint32_t* counters;
   unsigned long long* depth_hist;
   int stack_cap;              // stack entries per ray
+  // Reordered traces: result slot of ray i is out_index[i] (null: i). The
+  // rays were permuted before the launch; results go back to input order.
+  const uint32_t* out_index = nullptr;
 };
+
+BVHGPU_DEV uint64_t out_slot(const TraceArgs& a, uint64_t rid) {
+  return a.out_index ? (uint64_t)__ldg(a.out_index + rid) : rid;
+}
 
 struct Counters {
   uint32_t node_visits = 0, leaf_visits = 0, box_tests = 0, box_hits = 0;
@@ -389,7 +396,7 @@ BVHGPU_DEV bvhgpu_ray_t load_ray(const bvhgpu_ray_t* rays, uint64_t i) {
 template <bool COUNT>
 BVHGPU_DEV void flush_counters(const TraceArgs& a, uint64_t rid, const Counters& c) {
   if (!COUNT || a.counters == nullptr) return;
-  uint32_t* o = a.counters + rid * BVHGPU_COUNTERS_PER_RAY;
+  uint32_t* o = a.counters + out_slot(a, rid) * BVHGPU_COUNTERS_PER_RAY;
   o[0] = c.node_visits;
   o[1] = c.leaf_visits;
   o[2] = c.box_tests;
@@ -403,8 +410,9 @@ BVHGPU_DEV void flush_counters(const TraceArgs& a, uint64_t rid, const Counters&
 template <int KIND>
 BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t rid, bool hit,
                              float tmax, const Best& best) {
+  const uint64_t slot = out_slot(a, rid);
   if (KIND == BVHGPU_ANY) {
-    a.occluded[rid] = hit ? 1 : 0;
+    a.occluded[slot] = hit ? 1 : 0;
     return;
   }
   bvhgpu_hit_t h;
@@ -419,7 +427,7 @@ BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t ri
     h.u = 0.f;
     h.v = 0.f;
   }
-  reinterpret_cast<float4*>(a.hits)[rid] =
+  reinterpret_cast<float4*>(a.hits)[slot] =
       make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
 }
 
@@ -715,7 +723,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
     best.v = best_v[tid];
     write_result<KIND>(sc, a, rid, hit, rays[tid].tmax, best);
     if (COUNT && a.counters) {
-      uint32_t* o = a.counters + rid * BVHGPU_COUNTERS_PER_RAY;
+      uint32_t* o = a.counters + out_slot(a, rid) * BVHGPU_COUNTERS_PER_RAY;
       for (int k = 0; k < 7; ++k) o[k] = ctrs[k * P + tid];
       o[7] = 0;
     }

@@ -57,19 +57,44 @@ def test_adjoint_matches_torch_autograd_moller_trumbore():
     assert rel_v < 1e-4 and rel_r < 1e-4, (rel_v.item(), rel_r.item())
 
 
+def test_adjoint_matches_fp64_chain_rule():
+    """The reverse pass against float64 PyTorch autograd of Moller-Trumbore on
+    the CPU, fed the same upstream gradient (from the FP32 forward t): with
+    the double-float reverse pass the two agree to FP32 accumulation error,
+    grazing rays included."""
+    v, f, r, scene, t_tgt, p_tgt = _case(n=64, res=128)
+    loss, gv, gr, prim, m = _loss_and_grads(v, f, r, scene, t_tgt, p_tgt)
+    t, _, _, _ = D.ray_hit(v, f, r, scene)
+    idx = torch.nonzero(m).squeeze(1)
+    up = (2 * (t.detach() - t_tgt))[idx].double().cpu()
+    V = v.detach().double().cpu().requires_grad_(True)
+    R = r.detach().double().cpu()[idx.cpu()].requires_grad_(True)
+    tri = f.cpu()[prim[idx].long().cpu()]
+    t64, _, _ = D.moller_trumbore_torch(R[:, 0:3], R[:, 4:7], V[tri[:, 0]], V[tri[:, 1]],
+                                        V[tri[:, 2]])
+    g_v, g_r = torch.autograd.grad(t64, (V, R), grad_outputs=up)
+    rel_v = (gv.double().cpu() - g_v).norm() / g_v.norm()
+    gr_hit = gr.double().cpu()[idx.cpu()][:, [0, 1, 2, 4, 5, 6]]
+    rel_r = (gr_hit - g_r[:, [0, 1, 2, 4, 5, 6]]).norm() / g_r.norm()
+    assert rel_v < 1e-5 and rel_r < 1e-5, (rel_v.item(), rel_r.item())
+
+
 def test_adjoint_barycentric_gradients():
+    """Gradients through the barycentrics against float64 PyTorch autograd of
+    Moller-Trumbore on the CPU (same hits, same upstream weights)."""
     v, f, r, scene, t_tgt, p_tgt = _case(n=32, res=48)
     t, u, w, prim = D.ray_hit(v, f, r, scene)
     m = prim >= 0
     loss = (u[m] * 0.7 - w[m] * 1.3).sum()
     gv, = torch.autograd.grad(loss, (v,))
-    v2 = v.detach().clone().requires_grad_(True)
-    idx = torch.nonzero(m).squeeze(1)
-    tri = f[prim[idx].long()]
-    _, b1, b2 = D.moller_trumbore_torch(r[idx, 0:3].detach(), r[idx, 4:7].detach(),
-                                        v2[tri[:, 0]], v2[tri[:, 1]], v2[tri[:, 2]])
-    gv2, = torch.autograd.grad((b1 * 0.7 - b2 * 1.3).sum(), (v2,))
-    assert (gv - gv2).norm() / gv2.norm() < 1e-4
+    idx = torch.nonzero(m).squeeze(1).cpu()
+    V = v.detach().double().cpu().requires_grad_(True)
+    R = r.detach().double().cpu()[idx]
+    tri = f.cpu()[prim[m].long().cpu()]
+    _, b1, b2 = D.moller_trumbore_torch(R[:, 0:3], R[:, 4:7], V[tri[:, 0]], V[tri[:, 1]],
+                                        V[tri[:, 2]])
+    g64, = torch.autograd.grad((b1 * 0.7 - b2 * 1.3).sum(), (V,))
+    assert (gv.double().cpu() - g64).norm() / g64.norm() < 1e-5
 
 
 def _fd_loss(o, d, p0, p1, p2, tgt):

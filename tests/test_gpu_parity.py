@@ -344,3 +344,36 @@ def test_save_distance_traversal(n, l, profile, fmt):
     with pytest.raises(pkg.BvhgpuError):
         scene.trace(dev(rays), scheme="persistent", save_distance=True)
     scene.status()
+
+
+@pytest.mark.parametrize("scheme,kw", [("per_ray", {}), ("persistent", {"policy": 2, "refill": 16}),
+                                       ("stream", {})], ids=["per_ray", "persistent", "stream"])
+@pytest.mark.parametrize("k", [1, 8, 32])
+def test_reorder_keeps_results_in_input_order(scheme, kw, k):
+    """reorder = K traces the rays grouped into 6 K^2 direction bins; hits,
+    occlusion and counters come back in input order, equal to the plain
+    trace; inactive (NaN) rays and a ragged count included."""
+    tris, b, cv = TS.bvh("clutter120", 8, 8)
+    rays = TS.clutter_rays(tris)[:5000 - 3].copy()
+    rays[::97, 0] = np.nan
+    scene = pkg.Scene(b)
+    d = dev(rays)
+    plain = scene.trace(d, scheme=scheme, counters=True, **kw)
+    got = scene.trace(d, scheme=scheme, counters=True, reorder=k, **kw)
+    assert torch.equal(plain["hits"].view(torch.int32), got["hits"].view(torch.int32))
+    assert torch.equal(plain["counters"], got["counters"])
+    prims = pkg.hit_prims(plain["hits"].cpu().numpy())
+    _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=4)
+    da = dev(ao)
+    occ = scene.trace(da, kind="any", scheme=scheme, **kw)["occluded"]
+    occ_r = scene.trace(da, kind="any", scheme=scheme, reorder=k, **kw)["occluded"]
+    assert torch.equal(occ, occ_r)
+    ref = O.trace_instrumented(cv, ao, shadow=True, counters=False)["occluded"]
+    assert np.array_equal(occ_r.cpu().numpy(), ref)
+    one = scene.trace(d[:1], reorder=k)["hits"]
+    assert torch.equal(one.view(torch.int32), plain["hits"][:1].view(torch.int32))
+    host = scene.trace_host(ao, kind="any", reorder=k)
+    assert np.array_equal(host, ref)
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace(d, reorder=33)
+    scene.status()
