@@ -63,10 +63,14 @@ struct bvhgpu_scene {
   unsigned long long* d_queue = nullptr;
   std::atomic<unsigned> queue_next{0};
   int sm_count = 0;
-  // Staging for bvhgpu_trace_host (grown on demand).
+  // Staging for bvhgpu_trace_host (grown on demand): one region per
+  // pipeline stream, and the streams / events that order them.
+  static constexpr int kHostStreams = 2;
   std::mutex staging_mu;
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
+  cudaStream_t host_stream[kHostStreams] = {nullptr, nullptr};
+  cudaEvent_t host_event[kHostStreams + 1] = {nullptr, nullptr, nullptr};
 
   dev::SceneDev dev_view() const {
     dev::SceneDev s;
@@ -90,6 +94,10 @@ struct bvhgpu_scene {
     cudaFree(d_queue);
     cudaFree(d_prim_slot);
     cudaFree(d_stage);
+    for (auto& h : host_stream)
+      if (h) cudaStreamDestroy(h);
+    for (auto& ev : host_event)
+      if (ev) cudaEventDestroy(ev);
     d_nodes = nullptr;
     d_leaves = nullptr;
     d_leaf_prim = nullptr;
@@ -474,12 +482,36 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  // Pipeline: the rays go in chunks over two internal streams, so the copy
+  // of one chunk in, the trace of another and the copy of a third out run at
+  // the same time. Both streams wait for `stream` first; `stream` waits for
+  // both at the end, and the call returns with the results on the host.
   std::lock_guard<std::mutex> lock(s->staging_mu);
-  const size_t ray_bytes = n * sizeof(bvhgpu_ray_t);
-  const size_t out_bytes = closest ? n * sizeof(bvhgpu_hit_t) : ((n + 15) / 16) * 16;
-  const size_t need = ray_bytes + out_bytes;
+  constexpr int NS = bvhgpu_scene::kHostStreams;
+  for (int i = 0; i < NS; ++i) {
+    if (!s->host_stream[i]) {
+      e = cudaStreamCreateWithFlags(&s->host_stream[i], cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cuda_error(e, "create pipeline stream");
+    }
+  }
+  for (auto& ev : s->host_event) {
+    if (!ev) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_error(e, "create pipeline event");
+    }
+  }
+  // Chunks of a quarter of the batch, between 256 Ki and 4 Mi rays.
+  uint64_t chunk = (n + 3) / 4;
+  chunk = std::max<uint64_t>(chunk, 256ull << 10);
+  chunk = std::min<uint64_t>(chunk, 4ull << 20);
+  chunk = std::min<uint64_t>(chunk, n);
+  const size_t out_rec = closest ? sizeof(bvhgpu_hit_t) : 1;
+  const size_t ray_bytes = align256(chunk * sizeof(bvhgpu_ray_t));
+  const size_t per_stream = ray_bytes + align256(chunk * out_rec);
+  const size_t need = per_stream * NS;
   if (need > s->stage_bytes) {
     cudaStreamSynchronize(st);
+    for (int i = 0; i < NS; ++i) cudaStreamSynchronize(s->host_stream[i]);
     cudaFree(s->d_stage);
     s->d_stage = nullptr;
     s->stage_bytes = 0;
@@ -487,24 +519,47 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
     if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "staging allocation failed");
     s->stage_bytes = need;
   }
-  auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(s->d_stage);
-  uint8_t* d_out = reinterpret_cast<uint8_t*>(s->d_stage) + ray_bytes;
-  e = cudaMemcpyAsync(d_rays, rays, ray_bytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_error(e, "copy rays in");
-  dev::TraceArgs a;
-  a.rays = d_rays;
-  a.n = n;
-  a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
-  a.occluded = closest ? nullptr : d_out;
-  a.counters = nullptr;
-  a.depth_hist = nullptr;
-  a.stack_cap = stack_cap(s);
-  rc = launch_reordered(s, a, cfg, st);
-  if (rc) return rc;
-  e = cudaMemcpyAsync(closest ? (void*)hits : (void*)occluded, d_out,
-                      closest ? n * sizeof(bvhgpu_hit_t) : n, cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return cuda_error(e, "copy results out");
+  e = cudaEventRecord(s->host_event[NS], st);
+  if (e != cudaSuccess) return cuda_error(e, "pipeline start event");
+  for (int i = 0; i < NS; ++i) {
+    e = cudaStreamWaitEvent(s->host_stream[i], s->host_event[NS], 0);
+    if (e != cudaSuccess) return cuda_error(e, "pipeline wait");
+  }
+  rc = BVHGPU_OK;
+  uint64_t k = 0;
+  for (uint64_t first = 0; first < n && rc == BVHGPU_OK; first += chunk, ++k) {
+    const uint64_t m = std::min<uint64_t>(chunk, n - first);
+    const int si = (int)(k % NS);
+    cudaStream_t cs = s->host_stream[si];
+    uint8_t* base = static_cast<uint8_t*>(s->d_stage) + per_stream * si;
+    auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(base);
+    uint8_t* d_out = base + ray_bytes;
+    e = cudaMemcpyAsync(d_rays, rays + first, m * sizeof(bvhgpu_ray_t), cudaMemcpyHostToDevice,
+                        cs);
+    if (e != cudaSuccess) {
+      rc = cuda_error(e, "copy rays in");
+      break;
+    }
+    dev::TraceArgs a;
+    a.rays = d_rays;
+    a.n = m;
+    a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
+    a.occluded = closest ? nullptr : d_out;
+    a.counters = nullptr;
+    a.depth_hist = nullptr;
+    a.stack_cap = stack_cap(s);
+    rc = launch_reordered(s, a, cfg, cs);
+    if (rc) break;
+    void* dst = closest ? (void*)(hits + first) : (void*)(occluded + first);
+    e = cudaMemcpyAsync(dst, d_out, m * out_rec, cudaMemcpyDeviceToHost, cs);
+    if (e != cudaSuccess) rc = cuda_error(e, "copy results out");
+  }
+  for (int i = 0; i < NS; ++i) {
+    cudaEventRecord(s->host_event[i], s->host_stream[i]);
+    cudaStreamWaitEvent(st, s->host_event[i], 0);
+  }
   e = cudaStreamSynchronize(st);
+  if (rc) return rc;
   if (e != cudaSuccess) return cuda_error(e, "synchronise");
   return BVHGPU_OK;
 }
