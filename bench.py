@@ -41,8 +41,10 @@ METRIC = "Mrays/s"
 # is the ray stream plus cold misses (the BVH stays in L2), so it grows with
 # the ray count and is scaled by it.
 # Source: profiles/trace_persistent_p2_ao_clutter250k_N8L8.md
-NCU_TRAFFIC_PER_AO_RAY = {"bytes": 140371712 / 4147200, "scheme": "persistent", "policy": 2,
-                          "layout": ("fp32", 0)}
+# With reorder = 8 the launch is the four reorder passes plus the trace
+# (rays read twice and written once more, the index array, the bins).
+# Source: profiles/reorder_k8_persistent_p2_ao_clutter250k_N8L8.md
+NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, 8: 565612800 / 4147200}
 
 
 def parse():
@@ -63,6 +65,8 @@ def parse():
     p.add_argument("--top-levels", type=int, default=0)
     p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
     p.add_argument("--refill", type=int, default=8, help="persistent: idle lanes per refill")
+    p.add_argument("--reorder", type=int, default=0,
+                   help="fixed scheme: group rays into 6 K^2 direction bins first (0 = off)")
     p.add_argument("--no-compare", action="store_true",
                    help="skip timing the other traversal schemes")
     p.add_argument("--profile", default="instrumented", choices=["instrumented", "fast"])
@@ -294,6 +298,8 @@ def run_ours(a):
         o = {"scheme": a.scheme}
         if a.scheme == "persistent":
             o.update(policy=a.policy, refill=a.refill)
+        if a.reorder:
+            o["reorder"] = a.reorder
         chosen = [(sc, o)] * 3
         method = f"{a.scheme} kernel, {a.nodes} nodes, top levels {a.top_levels}"
         plan_desc = None
@@ -395,9 +401,9 @@ def run_ours(a):
     traffic = None
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
-            and dom_opts.get("policy") == NCU_TRAFFIC_PER_AO_RAY["policy"]
-            and not dom_opts.get("reorder") and chosen[dom][0].node_format == "fp32"):
-        traffic = NCU_TRAFFIC_PER_AO_RAY["bytes"] * int(batches[dom][0].shape[0])
+            and dom_opts.get("policy") == 2 and dom_opts.get("reorder", 0) in NCU_TRAFFIC_PER_AO_RAY
+            and chosen[dom][0].node_format == "fp32"):
+        traffic = NCU_TRAFFIC_PER_AO_RAY[dom_opts.get("reorder", 0)] * int(batches[dom][0].shape[0])
 
     compare = {}
     if not a.no_compare:

@@ -27,6 +27,7 @@ import numpy as np
 from . import _native as N
 
 __all__ = ["Bvh", "Scene", "FastNodeManager", "CompactNodeManager", "sah_factor", "trace_jobs",
+           "camera_rays", "camera_transform", "ao_factor",
            "BvhgpuError", "CLOSEST", "ANY", "PER_RAY", "STREAM", "PERSISTENT", "PROFILE_INSTRUMENTED",
            "PROFILE_FAST"]
 
@@ -255,6 +256,29 @@ class Scene:
                                           _ptr(out), C.c_void_p(s.cuda_stream)))
         return out
 
+    def secondary_rays(self, primary, hits, *, light=None, ao_samples: int = 0,
+                       ao_length: float = 1.0, sampling: str = "cosine", seed: int = 0,
+                       offset: float = 0.001, stream=None):
+        """Shadow and AO rays from closest hits on the device
+        (bvhgpu_secondary_rays): returns ``(shadow or None, ao or None)``,
+        ``[n, 8]`` and ``[n * ao_samples, 8]`` float32 tensors; rays of missed
+        primaries are inactive (NaN origin). ``sampling``: ``"cosine"`` or
+        ``"reference"`` (the reference's hashed uniform hemisphere, ``seed`` =
+        pixel index of primary ray 0)."""
+        import torch
+        n = primary.shape[0]
+        dev = primary.device
+        sh = torch.empty((n, 8), dtype=torch.float32, device=dev) if light is not None else None
+        ao = (torch.empty((n * ao_samples, 8), dtype=torch.float32, device=dev)
+              if ao_samples > 0 else None)
+        p = N.Secondary((C.c_float * 3)(*(light if light is not None else (0.0, 0.0, 0.0))),
+                        offset, ao_samples, ao_length,
+                        N.AO_REFERENCE if sampling == "reference" else N.AO_COSINE, 0, seed)
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        N.check(N.lib().bvhgpu_secondary_rays(self._h, _ptr(primary), _ptr(hits), n, C.byref(p),
+                                              _ptr(sh), _ptr(ao), C.c_void_p(s.cuda_stream)))
+        return sh, ao
+
     def set_stack_limit(self, entries: int) -> None:
         """Caps the traversal stack (0 restores the tree's worst case)."""
         N.check(N.lib().bvhgpu_scene_set_stack_limit(self._h, entries))
@@ -274,6 +298,48 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+
+def camera_transform(pos, target, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """Camera-to-world matrix, column-major float32, of a camera at ``pos``
+    looking at ``target`` (the inverse of a right-handed lookAt: columns
+    right, up, -forward, pos)."""
+    pos = np.asarray(pos, np.float64)
+    f = np.asarray(target, np.float64) - pos
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    m = np.zeros((4, 4), np.float64)  # m[column][row]
+    m[0, :3], m[1, :3], m[2, :3], m[3, :3] = r, u, -f, pos
+    m[3, 3] = 1.0
+    return m.astype(np.float32).reshape(16)
+
+
+def camera_rays(pos, target, width: int, height: int, *, workgroup: int = 16,
+                focal: float = 0.866, tmax: float = 222222.0, transform=None, device: int = 0,
+                stream=None):
+    """Primary rays on the device (bvhgpu_camera_rays): ``[width * height, 8]``
+    float32, tile by tile like CameraFast's workgroups."""
+    import torch
+    m = camera_transform(pos, target) if transform is None else np.asarray(transform, np.float32)
+    cam = N.Camera((C.c_float * 3)(*np.asarray(pos, np.float32)),
+                   (C.c_float * 16)(*m.reshape(16)), width, height, workgroup, focal, tmax)
+    out = torch.empty((width * height, 8), dtype=torch.float32, device=torch.device("cuda", device))
+    s = stream if stream is not None else torch.cuda.current_stream(out.device)
+    N.check(N.lib().bvhgpu_camera_rays(C.byref(cam), _ptr(out), C.c_void_p(s.cuda_stream)))
+    return out
+
+
+def ao_factor(occluded, samples: int, stream=None):
+    """Per pixel 1 - occluded / samples (bvhgpu_ao_factor), float32."""
+    import torch
+    n = occluded.shape[0] // samples
+    out = torch.empty(n, dtype=torch.float32, device=occluded.device)
+    s = stream if stream is not None else torch.cuda.current_stream(occluded.device)
+    N.check(N.lib().bvhgpu_ao_factor(_ptr(occluded), n, samples, _ptr(out),
+                                     C.c_void_p(s.cuda_stream)))
+    return out
 
 
 def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: int = 16,

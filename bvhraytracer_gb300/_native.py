@@ -70,6 +70,21 @@ class Job(C.Structure):
 MAX_JOBS = 192
 
 
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("transform", C.c_float * 16), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("workgroup", C.c_int32), ("focal", C.c_float),
+                ("tmax", C.c_float)]
+
+
+class Secondary(C.Structure):
+    _fields_ = [("light", C.c_float * 3), ("offset", C.c_float), ("ao_samples", C.c_int32),
+                ("ao_length", C.c_float), ("sampling", C.c_int32), ("pad", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+AO_COSINE, AO_REFERENCE = 0, 1
+
+
 class BvhgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"bvhgpu error {code}: {msg}")
@@ -105,6 +120,10 @@ _SIGS = {
     "bvhgpu_trace_batches_noalloc": (C.c_int, [_P, C.POINTER(Batch), C.c_int32,
                                                 C.POINTER(TraceOpts), _P]),
     "bvhgpu_scene_status": (C.c_int, [_P, _P]),
+    "bvhgpu_camera_rays": (C.c_int, [C.POINTER(Camera), _P, _P]),
+    "bvhgpu_secondary_rays": (C.c_int, [_P, _P, _P, C.c_uint64, C.POINTER(Secondary), _P, _P,
+                                        _P]),
+    "bvhgpu_ao_factor": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
 }
 
 # Every symbol the public header declares (checked by the CPU tests).

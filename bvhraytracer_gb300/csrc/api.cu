@@ -18,6 +18,7 @@
 #include "bvhgpu_status.hpp"
 #include "launch.cuh"
 #include "reorder.cuh"
+#include "raygen.cuh"
 #include "batched.cuh"
 #include "adjoint.cuh"
 
@@ -83,6 +84,7 @@ struct bvhgpu_scene {
     s.leaf_memory = layout.leaf_memory;
     s.gang = layout.gang;
     s.status = d_status;
+    s.boxes_ordered = layout.boxes_ordered ? 1 : 0;
     return s;
   }
   void release() {
@@ -618,6 +620,7 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.nm = (int8_t)j.scene->layout.node_stride;
     d.fmt = (int8_t)j.scene->layout.node_format;
     d.kind = (int8_t)j.kind;
+    d.boxes_ordered = j.scene->layout.boxes_ordered ? 1 : 0;
     total += j.n;
     stack = std::max(stack, stack_cap(j.scene));
     sms = j.scene->sm_count;
@@ -710,6 +713,81 @@ int bvhgpu_scene_inject_stall(bvhgpu_scene_t s, int32_t on) {
   if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
   s->stall_bytes = on ? 16u : 0u;
   return BVHGPU_OK;
+}
+
+int bvhgpu_camera_rays(const bvhgpu_camera_t* c, bvhgpu_ray_t* rays, void* stream) {
+  if (!c) return set_error(BVHGPU_ERR_BAD_ARG, "null camera");
+  if (c->width == 0 || c->height == 0) return BVHGPU_OK;
+  if (!rays || ((uintptr_t)rays & 15))
+    return set_error(BVHGPU_ERR_BAD_ARG, "camera rays: null or not 16-byte aligned");
+  if (c->workgroup < 1 || c->workgroup > 4096)
+    return set_error(BVHGPU_ERR_BAD_ARG, "camera rays: workgroup must be 1..4096");
+  if ((uint64_t)c->width * c->height > (1ull << 36))
+    return set_error(BVHGPU_ERR_BAD_ARG, "camera rays: at most 2^36 pixels");
+  dev::CameraArgs a;
+  for (int k = 0; k < 3; ++k) a.pos[k] = c->pos[k];
+  for (int k = 0; k < 16; ++k) a.transform[k] = c->transform[k];
+  a.width = c->width;
+  a.height = c->height;
+  a.workgroup = c->workgroup;
+  a.focal = c->focal;
+  a.tmax = c->tmax;
+  a.n = (uint64_t)c->width * c->height;
+  cudaError_t e = dev::launch_camera_rays(a, rays, (cudaStream_t)stream);
+  return e == cudaSuccess ? BVHGPU_OK : cuda_error(e, "camera rays");
+}
+
+int bvhgpu_secondary_rays(bvhgpu_scene_t s, const bvhgpu_ray_t* primary, const bvhgpu_hit_t* hits,
+                          uint64_t n, const bvhgpu_secondary_t* p, bvhgpu_ray_t* shadow,
+                          bvhgpu_ray_t* ao, void* stream) {
+  if (!s || !p) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  if (p->ao_samples < 0 || p->ao_samples > 1024)
+    return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: ao_samples must be 0..1024");
+  if (p->sampling != BVHGPU_AO_COSINE && p->sampling != BVHGPU_AO_REFERENCE)
+    return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: sampling");
+  if (n == 0) return BVHGPU_OK;
+  if (n > (1ull << 36)) return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: at most 2^36 rays");
+  if (!primary || !hits || ((uintptr_t)primary & 15) || ((uintptr_t)hits & 15))
+    return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: primary rays / hits null or misaligned");
+  if (shadow && ((uintptr_t)shadow & 15))
+    return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: shadow not 16-byte aligned");
+  if (p->ao_samples > 0 && (!ao || ((uintptr_t)ao & 15)))
+    return set_error(BVHGPU_ERR_BAD_ARG, "secondary rays: ao null or not 16-byte aligned");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  {
+    std::lock_guard<std::mutex> lock(s->staging_mu);
+    if (!s->d_prim_slot) {
+      int rc = upload(&s->d_prim_slot, s->prim_slot);
+      if (rc) return rc;
+    }
+  }
+  dev::SecondaryArgs a;
+  a.primary = primary;
+  a.hits = reinterpret_cast<const float4*>(hits);
+  a.n = n;
+  a.prim_slot = s->d_prim_slot;
+  a.n_prims = (uint32_t)s->prim_slot.size();
+  a.shadow = shadow;
+  a.ao = p->ao_samples > 0 ? ao : nullptr;
+  for (int k = 0; k < 3; ++k) a.light[k] = p->light[k];
+  a.offset = p->offset;
+  a.ao_samples = p->ao_samples;
+  a.ao_length = p->ao_length;
+  a.sampling = p->sampling;
+  a.seed = p->seed;
+  e = dev::launch_secondary_rays(s->dev_view(), a, (cudaStream_t)stream);
+  return e == cudaSuccess ? BVHGPU_OK : cuda_error(e, "secondary rays");
+}
+
+int bvhgpu_ao_factor(const uint8_t* occluded, uint64_t n, int32_t samples, float* factor,
+                     void* stream) {
+  if (samples < 1) return set_error(BVHGPU_ERR_BAD_ARG, "ao factor: samples must be >= 1");
+  if (n == 0) return BVHGPU_OK;
+  if (n > (1ull << 36)) return set_error(BVHGPU_ERR_BAD_ARG, "ao factor: at most 2^36 pixels");
+  if (!occluded || !factor) return set_error(BVHGPU_ERR_BAD_ARG, "ao factor: null buffer");
+  cudaError_t e = dev::launch_ao_factor(occluded, n, samples, factor, (cudaStream_t)stream);
+  return e == cudaSuccess ? BVHGPU_OK : cuda_error(e, "ao factor");
 }
 
 int bvhgpu_scene_set_stack_limit(bvhgpu_scene_t s, int32_t entries) {

@@ -27,7 +27,8 @@ struct JobDev {
   int8_t nm;               // node slots: 4, 8, 12 or 16
   int8_t fmt;              // node format
   int8_t kind;             // BVHGPU_CLOSEST / BVHGPU_ANY
-  int8_t pad[7];
+  int8_t boxes_ordered;    // SceneDev::boxes_ordered of the job's scene
+  int8_t pad[6];
 };
 static_assert(sizeof(JobDev) == 80, "job record size");
 
@@ -117,6 +118,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
           sc.leaf_memory = J.leaf_memory;
           sc.gang = J.gang;
           sc.status = J.status;
+          sc.boxes_ordered = J.boxes_ordered;
           nm = J.nm;
           fmt = J.fmt;
           kind = J.kind;

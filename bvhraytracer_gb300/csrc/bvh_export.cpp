@@ -117,6 +117,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
   out.gang = gang;
   out.node_format = node_format;
   out.record_bytes = node_format == 0 ? fp32_record_bytes(nm) : q8_record_bytes(nm);
+  out.boxes_ordered = node_format == 0;
 
   const size_t n = bvh.nodes.size();
   // Leaf numbering: order of leaves in the reference's customTreeOrder.
@@ -212,6 +213,8 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
         for (int k = 0; k < 3; ++k) {
           box[k * nm + j] = ch.bmin[k];
           box[(3 + k) * nm + j] = ch.bmax[k];
+          if (!(std::isfinite(ch.bmin[k]) && std::isfinite(ch.bmax[k]) && ch.bmin[k] <= ch.bmax[k]))
+            out.boxes_ordered = false;
         }
       }
       meta = rec + 24 * nm;

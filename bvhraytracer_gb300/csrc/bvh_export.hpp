@@ -62,6 +62,9 @@ struct DeviceLayout {
   uint32_t n_inner = 0, n_leaves = 0;
   uint32_t root_entry = 0;            // stack entry of the root
   uint32_t top_nodes = 0;             // inner nodes laid out first
+  // Every child box is finite with lo <= hi on each axis (FP32 records), so
+  // a slab test may take the near / far planes by the sign of 1/direction.
+  bool boxes_ordered = true;
 };
 
 constexpr uint32_t kLeafBit = 0x80000000u;

@@ -183,6 +183,10 @@ template <bool MM> BVHGPU_DEV float tmax2(float a, float b) { return MM ? fmaxf(
 // (src/primitives/triangle.cpp:52-249), on points given in the ray's
 // permuted axes (x' = kx, y' = ky, z' = kz). Returns true on a hit with
 // t <= tmax; b1 / b2 are the weights of p1 / p2.
+#ifndef BVHGPU_EDGE_FIRST
+#define BVHGPU_EDGE_FIRST 0
+#endif
+
 template <bool MM>
 BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, float& t_out,
                            float& b1_out, float& b2_out) {
@@ -194,7 +198,11 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
   const float ix = sel3(r.kx, r.inv[0], r.inv[1], r.inv[2]);
   const float iy = sel3(r.ky, r.inv[0], r.inv[1], r.inv[2]);
   const float iz = sel3(r.code, r.inv[0], r.inv[1], r.inv[2]);
-  {
+  // The box pre-test and the edge-function sign test are both necessary
+  // conditions of a hit and free of side effects, so their order does not
+  // change any result; BVHGPU_EDGE_FIRST runs the (more selective) edge test
+  // first.
+  auto pretest = [&]() -> bool {
     // Triangle vertices are finite, so the bounds are NaN-free in both forms.
     float bmnx = fminf(fminf(p[0][0], p[1][0]), p[2][0]);
     float bmxx = fmaxf(fmaxf(p[0][0], p[1][0]), p[2][0]);
@@ -210,7 +218,11 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
     if (tmx < 0) return false;
     if (tmin > tmx) return false;
     if (tmax < tmin) return false;
-  }
+    return true;
+  };
+#if !BVHGPU_EDGE_FIRST
+  if (!pretest()) return false;
+#endif
   float p0x = p[0][0] - ox, p0y = p[0][1] - oy, p0z = p[0][2] - oz;
   float p1x = p[1][0] - ox, p1y = p[1][1] - oy, p1z = p[1][2] - oz;
   float p2x = p[2][0] - ox, p2y = p[2][1] - oy, p2z = p[2][2] - oz;
@@ -234,6 +246,9 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
     e2 = (float)(p1typ0tx - p1txp0ty);
   }
   if ((e0 < 0 || e1 < 0 || e2 < 0) && (e0 > 0 || e1 > 0 || e2 > 0)) return false;
+#if BVHGPU_EDGE_FIRST
+  if (!pretest()) return false;
+#endif
   float det = e0 + e1 + e2;
   if (det == 0) return false;
   p0z *= r.sz; p1z *= r.sz; p2z *= r.sz;

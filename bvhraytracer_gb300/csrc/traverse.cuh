@@ -30,7 +30,14 @@ struct SceneDev {
   int leaf_memory;
   int gang;
   int* status;                // first device-side error (0 = none)
+  // FP32 records whose child boxes are all finite with lo <= hi: NaN-free
+  // rays may take the near / far slab form (see visit_node).
+  int boxes_ordered;
 };
+
+#ifndef BVHGPU_NEARFAR
+#define BVHGPU_NEARFAR 1
+#endif
 
 struct TraceArgs {
   const bvhgpu_ray_t* rays;
@@ -129,7 +136,15 @@ BVHGPU_DEV float4 q8_row(uint32_t w, float origin, float step, bool up) {
 // Returns false on stack overflow.
 // DIST: the save-distance traversal; each push also stores the child's entry
 // distance in dstack (same slot layout as stack).
-template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, bool DIST = false>
+// NF: near / far form of the IEEE slab test for FP32 records whose boxes are
+// ordered (SceneDev::boxes_ordered) and NaN-free rays: per axis the near
+// plane is the low one when 1/d >= 0, else the high one, so the per-child
+// min / max pair of slab_mm disappears. With lo <= hi, (lo - o) * inv and
+// (hi - o) * inv are ordered by the sign of inv (rounding is monotonic), so
+// fminf / fmaxf of slab_mm return exactly the near / far values: same t0, t1
+// and boolean.
+template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, bool DIST = false,
+          bool NF = false>
 BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
                            int stride, int& sp, int cap, Counters& ctr, int& depth_out,
                            float* dstack = nullptr) {
@@ -153,6 +168,33 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   }
   uint32_t hit = 0;
   float dist[NM];
+  if (NF) {
+    // Row of the near plane per axis (0..2 low, 3..5 high); far = near ^ 3 + ...
+    const int nx = r.inv[0] >= 0.0f ? 0 : 3, ny = r.inv[1] >= 0.0f ? 1 : 4;
+    const int nz = r.inv[2] >= 0.0f ? 2 : 5;
+    const int fx = nx == 0 ? 3 : 0, fy = ny == 1 ? 4 : 1, fz = nz == 2 ? 5 : 2;
+#pragma unroll
+    for (int q = 0; q < NM / 4; ++q) {
+      const float4 ax = rec_f4<SH>(rec + (nx * NM + 4 * q) * 4);
+      const float4 bx = rec_f4<SH>(rec + (fx * NM + 4 * q) * 4);
+      const float4 ay = rec_f4<SH>(rec + (ny * NM + 4 * q) * 4);
+      const float4 by = rec_f4<SH>(rec + (fy * NM + 4 * q) * 4);
+      const float4 az = rec_f4<SH>(rec + (nz * NM + 4 * q) * 4);
+      const float4 bz = rec_f4<SH>(rec + (fz * NM + 4 * q) * 4);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (4 * q + k < N) {
+          float t0 = fmaxf((f4get(ax, k) - r.o[0]) * r.inv[0], 0.0f);
+          float t1 = fminf((f4get(bx, k) - r.o[0]) * r.inv[0], tmax);
+          t0 = fmaxf((f4get(ay, k) - r.o[1]) * r.inv[1], t0);
+          t1 = fminf((f4get(by, k) - r.o[1]) * r.inv[1], t1);
+          t0 = fmaxf((f4get(az, k) - r.o[2]) * r.inv[2], t0);
+          t1 = fminf((f4get(bz, k) - r.o[2]) * r.inv[2], t1);
+          hit |= (uint32_t)(t0 <= t1) << (4 * q + k);
+        }
+      }
+    }
+  } else
 #pragma unroll
   for (int q = 0; q < NM / 4; ++q) {
     float4 lx, ly, lz, hx, hy, hz;
@@ -369,6 +411,10 @@ BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_sme
   const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
     return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false, DIST>(
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+  constexpr bool kNF = BVHGPU_NEARFAR && FMT == kFmtFP32 && !DIST;
+  if (kNF && sc.boxes_ordered)
+    return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST, kNF>(
         rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
   return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST>(
       rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);

@@ -29,6 +29,11 @@
  *                             Moller-Trumbore (rayTracerTemplate.ispc:35-76)
  *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
  *                             structure, fastNodeManager.h:92-156, across scenes)
+ *   bvhgpu_camera_rays        Camera::getRayTargetPosition + FastRay (camera.h:82-98)
+ *   bvhgpu_secondary_rays     getSurfaceNormalPosition + shadow / AO set-up
+ *                             (fastNodeManager.h:1700-1713, cameraFast.h:366-381, 513-552,
+ *                             camera.cpp:21-52)
+ *   bvhgpu_ao_factor          the AO term of cameraData.h:403-406
  *   bvhgpu_intersect_fastrays FastNodeManager::intersectWideAlternative on FastRay
  *                             records (fastNodeManager.h:835-1049; FastRay: src/fastRay.h:14-29)
  *   bvhgpu_intersect_secondary_fastrays
@@ -294,6 +299,57 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t scene, const bvhgpu_batch_t* bat
  * (rays, hits 16-byte aligned); stream-ordered. */
 int bvhgpu_fp64_check(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
                       uint64_t n, int32_t profile, double* out, void* stream);
+
+/* ---- ray generation on the GPU ----------------------------------------- */
+/* Pinhole camera of Camera::getRayTargetPosition (camera.h:82-98): pixel (w, h)
+ * with w = col - width/2, h = height/2 - row (integers) has the target
+ * pos + transform * ((w, h, 0) / width + (0, 0, -focal)), and the ray is
+ * FastRay(pos, target) (fastRay.cpp:3-20): direction = target - pos, not
+ * normalised. Pixels are emitted tile by tile (workgroup x workgroup pixels,
+ * row-major tiles, row-major inside a tile; edge tiles keep the pixels inside
+ * the image), the order of CameraFast's workgroups (cameraFast.h:465-490). */
+typedef struct {
+  float pos[3];
+  float transform[16]; /* camera to world, column-major (glm::inverse(glm::lookAt(..))) */
+  uint32_t width, height;
+  int32_t workgroup;   /* tile side in pixels (16) */
+  float focal;         /* 0.866: 60 degree horizontal field of view */
+  float tmax;          /* 222222: FastRay's default */
+} bvhgpu_camera_t;
+
+/* Replaces the ray set-up loops of CameraFast::renderImage
+ * (cameraFast.h:484-490, 339-341). rays: width * height device records. */
+int bvhgpu_camera_rays(const bvhgpu_camera_t* camera, bvhgpu_ray_t* rays, void* stream);
+
+#define BVHGPU_AO_COSINE 0    /* cosine-distributed around the normal, hashed from (seed, ray, sample) */
+#define BVHGPU_AO_REFERENCE 1 /* Camera::getAmbientDirection: FNV-1a-hashed (u, v), uniform
+                                 hemisphere flipped to the normal side (camera.cpp:21-52) */
+typedef struct {
+  float light[3];      /* point light of the shadow rays */
+  float offset;        /* origin offset along the normal: 0.001 (cameraFast.h:373) */
+  int32_t ao_samples;  /* AO rays per primary ray (0: none) */
+  float ao_length;     /* tMax of the AO rays (ambientDistance) */
+  int32_t sampling;    /* BVHGPU_AO_* */
+  int32_t pad;
+  uint64_t seed;       /* cosine: hash seed; reference: pixel index of primary ray 0 */
+} bvhgpu_secondary_t;
+
+/* Secondary rays from closest hits, on the device: for primary ray i with a
+ * hit, the geometric normal and ray-plane hit point of getSurfaceNormalPosition
+ * (fastNodeManager.h:1700-1713), origin = point + normal * offset; shadow[i]
+ * toward the light (unit direction, tMax = distance) when `shadow` is
+ * non-null; ao[i * ao_samples + k] for k < ao_samples (unit directions, tMax =
+ * ao_length). Rays of a missed primary get a NaN origin (inactive), as in
+ * cameraFast.h:524-528. Replaces cameraFast.h:366-381 and 513-552. */
+int bvhgpu_secondary_rays(bvhgpu_scene_t scene, const bvhgpu_ray_t* primary,
+                          const bvhgpu_hit_t* hits, uint64_t n, const bvhgpu_secondary_t* params,
+                          bvhgpu_ray_t* shadow, bvhgpu_ray_t* ao, void* stream);
+
+/* factor[i] = 1 - (occluded AO samples of pixel i) / samples, the ambient
+ * term of CameraData (cameraData.h:403-406); occluded holds n * samples bytes
+ * in the layout of bvhgpu_secondary_rays. */
+int bvhgpu_ao_factor(const uint8_t* occluded, uint64_t n, int32_t samples, float* factor,
+                     void* stream);
 
 /* Caps the traversal stack at `entries` per ray (0: the tree's worst case,
  * the default, which never overflows). Rays that need more stop, report a
