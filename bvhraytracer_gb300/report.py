@@ -1,0 +1,133 @@
+"""Report files in the reference's formats, written from GPU counters and
+timings, so its analysis scripts (Analysis/DataManager.py, which reads every
+value as the first number after a fixed key) can consume GPU results.
+
+* ``<name><problem>_Info.txt`` — CameraData::renderImage's traversal
+  statistics (src/cameraData.h:241-325): per-ray node / leaf / box / triangle
+  counts, success ratios, waste factors, traversal fullness and the per-depth
+  node and leaf visit histograms, for primary and secondary rays. The
+  averages of the fullness sections come from the counters (every node visit
+  tests all its children and every leaf visit all its triangles, so average
+  child fullness = box tests / node visits and average leaf fullness =
+  triangle tests / leaf visits); the per-count fullness lines of the
+  reference are not written because the kernels do not histogram them.
+* ``<name><problem>_Perf.txt`` — CameraFast::renderImage's timing summary
+  (src/cameraFast.h:147-161) with the device time of the frame. The GPU does
+  not time rays and triangle tests separately, so those lines read ``n/a``
+  (DataManager then records no value for them).
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass
+class RayStats:
+    """Sums over one ray batch: per-ray counters (``[n, 8]``: node visits,
+    leaf visits, box tests, box hits, triangle tests, triangle hits, deepest
+    stack, reserved) and the ``[2, 64]`` per-depth node / leaf visit
+    histogram, as returned by ``Scene.trace(..., counters=True,
+    depth_hist=True)``."""
+    rays: int
+    node_visits: int
+    leaf_visits: int
+    box_tests: int
+    box_hits: int
+    tri_tests: int
+    tri_hits: int
+    node_depth: np.ndarray
+    leaf_depth: np.ndarray
+
+    @classmethod
+    def from_trace(cls, counters, depth_hist, rays_counted: int | None = None) -> "RayStats":
+        c = np.asarray(_host(counters), np.int64).reshape(-1, 8)
+        h = np.asarray(_host(depth_hist), np.int64).reshape(2, -1)
+        s = c.sum(0)
+        return cls(int(rays_counted if rays_counted is not None else c.shape[0]), int(s[0]),
+                   int(s[1]), int(s[2]), int(s[3]), int(s[4]), int(s[5]), h[0], h[1])
+
+
+def _host(x):
+    if hasattr(x, "cpu"):
+        return x.cpu().numpy()
+    return x
+
+
+def _fmt(v: float) -> str:
+    # std::ostream's default float formatting: 6 significant digits.
+    return f"{v:.6g}"
+
+
+def _section(prefix: str, s: RayStats, branching: int) -> list[str]:
+    f = 1.0 / max(s.rays, 1)
+    waste = (s.leaf_visits + s.node_visits - s.rays) / float(max(s.node_visits * branching, 1))
+    return [
+        f"{prefix} intersections node: {_fmt(s.node_visits * f)}",
+        f"{prefix} aabb intersections: {_fmt(s.box_tests * f)}",
+        f"{prefix} aabb success ration: {_fmt(s.box_hits / max(s.box_tests, 1))}",
+        f"{prefix} waste factor: {_fmt(1 - waste)}",
+        f"{prefix} intersections leaf: {_fmt(s.leaf_visits * f)}",
+        f"{prefix} primitive intersections: {_fmt(s.tri_tests * f)}",
+        f"{prefix} primitive success ratio: {_fmt(s.tri_hits / max(s.tri_tests, 1))}",
+    ]
+
+
+def write_info(path: str, name: str, problem: str, branching: int, leaf_size: int,
+               primary: RayStats, secondary: RayStats) -> str:
+    """Writes ``<path>/<name><problem>_Info.txt``; returns the file name."""
+    lines = [f"scenario {name} with branching factor of {branching} and leafsize of {leaf_size}",
+             "intersections counts are normalized per Ray", ""]
+    lines += _section("primary", primary, branching) + [""]
+    lines += _section("secondary", secondary, branching) + [""]
+    # Fullness is collected from primary rays only (collectPrimaryRayData,
+    # cameraData.h:577-621).
+    lines += ["intersections with nodes with x children :",
+              "average child fullness: "
+              f"{primary.box_tests / max(primary.node_visits, 1):.6f}", "",
+              "intersections with leaf nodes with x primitives :",
+              "average leaf fullness: "
+              f"{primary.tri_tests / max(primary.leaf_visits, 1):.6f}"]
+    for title, hist, s in (("primary node intersections at depth x :", primary.node_depth, primary),
+                           ("primary leaf intersections at depth x :", primary.leaf_depth, primary),
+                           ("secondary node intersections at depth x :", secondary.node_depth,
+                            secondary),
+                           ("secondary leaf intersections at depth x :", secondary.leaf_depth,
+                            secondary)):
+        last = int(np.max(np.nonzero(hist)[0])) + 1 if np.any(hist) else 0
+        lines += ["", title] + [f"{i} : {_fmt(hist[i] / max(s.rays, 1))}" for i in range(last)]
+    os.makedirs(path, exist_ok=True)
+    fn = os.path.join(path, f"{name}{problem}_Info.txt")
+    with open(fn, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return fn
+
+
+def write_perf(path: str, name: str, problem: str, branching: int, leaf_size: int, gang: int,
+               node_memory: int, leaf_memory: int, total_seconds: float,
+               average_depth: float, triangles: int) -> str:
+    """Writes ``<path>/<name><problem>_Perf.txt``; returns the file name."""
+    lines = [
+        f"scenario {name} with branching factor of {branching} and leafsize of {leaf_size}",
+        f"with a gang size of {gang}, a node meory of {node_memory}, and a leaf memory of "
+        f"{leaf_memory}",
+        f"Raytracer total time: {_fmt(total_seconds)}",
+        "Time for all rays (SUM): n/a",
+        "Time for triangle intersections (SUM): n/a",
+        "Time all rays(sum) - triangle(sum): n/a",
+        f"Average BVH depth: {_fmt(average_depth)}",
+        f"Triangle Count: {triangles}",
+    ]
+    os.makedirs(path, exist_ok=True)
+    fn = os.path.join(path, f"{name}{problem}_Perf.txt")
+    with open(fn, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return fn
+
+
+def average_leaf_depth(leaf_depth_hist_of_tree) -> float:
+    """Mean depth over a histogram of leaves per depth."""
+    h = np.asarray(leaf_depth_hist_of_tree, np.float64)
+    return float((h * np.arange(h.shape[0])).sum() / max(h.sum(), 1.0))

@@ -1,0 +1,53 @@
+"""Report files in the reference's formats: every value the reference's
+analysis script reads (the first number after its key) is present and
+equals the statistic computed from the counters."""
+import numpy as np
+
+from bvhraytracer_gb300 import report as R
+
+
+def first_number(text: str, key: str):
+    """DataManager.gatherVariable: first token after the key that parses as
+    a float, on the line containing the key (Analysis/DataManager.py:397-407)."""
+    hits = [ln for ln in text.splitlines() if key in ln]
+    assert len(hits) == 1, key
+    for t in hits[0].split():
+        try:
+            return float(t)
+        except ValueError:
+            pass
+    return None
+
+
+def _stats(seed, n):
+    rng = np.random.default_rng(seed)
+    c = rng.integers(0, 50, (n, 8))
+    h = np.zeros((2, 64), np.int64)
+    h[0, :5] = rng.integers(0, 100, 5)
+    h[1, 2:6] = rng.integers(0, 100, 4)
+    return R.RayStats.from_trace(c, h), c, h
+
+
+def test_info_file_values(tmp_path):
+    p, cp, hp = _stats(0, 100)
+    s, cs, _ = _stats(1, 300)
+    fn = R.write_info(str(tmp_path), "clutter", "_b8_l8", 8, 8, p, s)
+    text = open(fn).read()
+    assert first_number(text, "primary intersections node:") == float(f"{cp[:, 0].sum() / 100:.6g}")
+    assert first_number(text, "secondary intersections leaf:") == float(f"{cs[:, 1].sum() / 300:.6g}")
+    ratio = cp[:, 3].sum() / cp[:, 2].sum()
+    assert abs(first_number(text, "primary aabb success ration:") - ratio) < 1e-5
+    waste = 1 - (cp[:, 1].sum() + cp[:, 0].sum() - 100) / (cp[:, 0].sum() * 8)
+    assert abs(first_number(text, "primary waste factor:") - waste) < 1e-5
+    assert abs(first_number(text, "average child fullness:") - cp[:, 2].sum() / cp[:, 0].sum()) < 1e-5
+    assert "primary node intersections at depth x :" in text
+    assert f"4 : {hp[0, 4] / 100:.6g}" in text
+
+
+def test_perf_file_values(tmp_path):
+    fn = R.write_perf(str(tmp_path), "clutter", "_b8_l8_mb8_ml8", 8, 8, 4, 8, 8, 0.00958, 14.2,
+                      999744)
+    text = open(fn).read()
+    assert first_number(text, "Raytracer total time:") == 0.00958
+    assert first_number(text, "Time for triangle intersections (SUM):") is None
+    assert first_number(text, "Triangle Count:") == 999744
