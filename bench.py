@@ -75,6 +75,8 @@ def parse():
     p.add_argument("--ref-sample", type=float, default=0.1,
                    help="fraction of the frame traced per step by --impl reference")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--report", default="",
+                   help="clutter: write the reference's _Info.txt / _Perf.txt into this folder")
     p.add_argument("--workload", default="clutter",
                    choices=["clutter", "batch64", "adjoint", "scale8m", "terrain", "sweep"],
                    help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch; "
@@ -326,13 +328,28 @@ def run_ours(a):
     # Algorithmic bytes per launch from one counting pass (untimed):
     # node visits x node record bytes + triangle tests x 36 bytes.
     alg = []
+    stats = []
     for (r, kind, _), (sc, o) in zip(batches, chosen):
-        c = sc.trace(r, kind=kind, counters=True, profile=a.profile, **o)
+        c = sc.trace(r, kind=kind, counters=True, depth_hist=bool(a.report), profile=a.profile,
+                     **o)
         cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
+        if a.report:
+            from bvhraytracer_gb300 import report
+            stats.append(report.RayStats.from_trace(c["counters"], c["depth_hist"]))
         alg.append({"node_visits": int(cs[0]), "leaf_visits": int(cs[1]), "tri_tests": int(cs[4]),
                     "bytes": int(cs[0]) * sc.node_record_bytes + int(cs[4]) * 36})
     for sc, _ in chosen:
         sc.status()
+    if a.report and rank == 0:
+        # The reference's _Info.txt (primary rays; secondary = shadow + AO).
+        from bvhraytracer_gb300 import report
+        sec = report.RayStats(
+            stats[1].rays + stats[2].rays,
+            *[getattr(stats[1], k) + getattr(stats[2], k) for k in
+              ("node_visits", "leaf_visits", "box_tests", "box_hits", "tri_tests", "tri_hits")],
+            stats[1].node_depth + stats[2].node_depth, stats[1].leaf_depth + stats[2].leaf_depth)
+        report.write_info(a.report, f"clutter{a.objects}", f"_b{a.branching}_l{a.leaf}",
+                          a.branching, a.leaf, stats[0], sec)
     setup_s = time.time() - t_setup
 
     for _ in range(a.warmup):
@@ -417,6 +434,14 @@ def run_ours(a):
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, tris, bvh, primary, shadow, ao, a.cpu_sample)
 
+    if a.report and rank == 0:
+        from bvhraytracer_gb300 import report
+        cx = bvh.export_compact()
+        leaves = cx["child_count"] == 0
+        report.write_perf(a.report, f"clutter{a.objects}", f"_b{a.branching}_l{a.leaf}"
+                          f"_mb{a.branching}_ml{a.leaf}", a.branching, a.leaf, 4,
+                          -(-a.branching // 4) * 4, -(-a.leaf // 4) * 4, ms / a.steps / 1e3,
+                          float(cx["depth"][leaves].mean()), int(bvh.info["n_tris"]))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,

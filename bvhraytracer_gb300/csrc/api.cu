@@ -191,30 +191,27 @@ static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
-// launch() after grouping the rays by direction when cfg.reorder > 0: the
-// rays are copied in bin order to stream-ordered scratch, traced from there,
-// and every result is written to its input slot. The scratch (about 38 bytes
-// per ray) is allocated and freed on the stream.
+// launch() after grouping the rays by direction when cfg.reorder > 0: a
+// counting sort writes the input indices in bin order, the kernels take the
+// rays in that order and write every result to its input slot. The scratch
+// (about 6 bytes per ray) is allocated and freed on the stream.
 static int launch_reordered(bvhgpu_scene_t s, dev::TraceArgs a, const dev::LaunchCfg& cfg,
                             cudaStream_t st) {
   if (cfg.reorder <= 0 || a.n < 2) return launch(s, a, cfg, st);
   if (a.n > 0xFFFFFFFFull)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "reorder: at most 2^32 - 1 rays per call");
-  const size_t ray_bytes = align256(a.n * sizeof(bvhgpu_ray_t));
   const size_t perm_bytes = align256(a.n * 4);
-  const size_t bytes = ray_bytes + perm_bytes + dev::reorder_scratch_bytes(a.n, cfg.reorder);
+  const size_t bytes = perm_bytes + dev::reorder_scratch_bytes(a.n, cfg.reorder);
   void* p = nullptr;
   cudaError_t e = cudaMallocAsync(&p, bytes, st);
   if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "reorder scratch allocation failed");
-  auto* sorted = reinterpret_cast<bvhgpu_ray_t*>(p);
-  auto* perm = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(p) + ray_bytes);
-  e = dev::reorder_rays(a.rays, a.n, cfg.reorder, sorted, perm,
-                        static_cast<uint8_t*>(p) + ray_bytes + perm_bytes, st);
+  auto* perm = reinterpret_cast<uint32_t*>(p);
+  e = dev::reorder_rays(a.rays, a.n, cfg.reorder, perm, static_cast<uint8_t*>(p) + perm_bytes,
+                        st);
   int rc;
   if (e != cudaSuccess) {
     rc = cuda_error(e, "reorder");
   } else {
-    a.rays = sorted;
     a.out_index = perm;
     rc = launch(s, a, cfg, st);
   }

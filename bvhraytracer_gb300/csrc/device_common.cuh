@@ -183,49 +183,35 @@ template <bool MM> BVHGPU_DEV float tmax2(float a, float b) { return MM ? fmaxf(
 // (src/primitives/triangle.cpp:52-249), on points given in the ray's
 // permuted axes (x' = kx, y' = ky, z' = kz). Returns true on a hit with
 // t <= tmax; b1 / b2 are the weights of p1 / p2.
-#ifndef BVHGPU_EDGE_FIRST
-#define BVHGPU_EDGE_FIRST 0
-#endif
-
 template <bool MM>
 BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, float& t_out,
                            float& b1_out, float& b2_out) {
-  // Per-triangle box pre-test (triangle.cpp:55-79) in the permuted axes; the
-  // max / min of three values does not depend on the axis order.
   const float ox = sel3(r.kx, r.o[0], r.o[1], r.o[2]);
   const float oy = sel3(r.ky, r.o[0], r.o[1], r.o[2]);
   const float oz = sel3(r.code, r.o[0], r.o[1], r.o[2]);
-  const float ix = sel3(r.kx, r.inv[0], r.inv[1], r.inv[2]);
-  const float iy = sel3(r.ky, r.inv[0], r.inv[1], r.inv[2]);
-  const float iz = sel3(r.code, r.inv[0], r.inv[1], r.inv[2]);
-  // The box pre-test and the edge-function sign test are both necessary
-  // conditions of a hit and free of side effects, so their order does not
-  // change any result; BVHGPU_EDGE_FIRST runs the (more selective) edge test
-  // first.
-  auto pretest = [&]() -> bool {
-    // Triangle vertices are finite, so the bounds are NaN-free in both forms.
-    float bmnx = fminf(fminf(p[0][0], p[1][0]), p[2][0]);
-    float bmxx = fmaxf(fmaxf(p[0][0], p[1][0]), p[2][0]);
-    float bmny = fminf(fminf(p[0][1], p[1][1]), p[2][1]);
-    float bmxy = fmaxf(fmaxf(p[0][1], p[1][1]), p[2][1]);
-    float bmnz = fminf(fminf(p[0][2], p[1][2]), p[2][2]);
-    float bmxz = fmaxf(fmaxf(p[0][2], p[1][2]), p[2][2]);
-    float t1x = (bmnx - ox) * ix, t2x = (bmxx - ox) * ix;
-    float t1y = (bmny - oy) * iy, t2y = (bmxy - oy) * iy;
-    float t1z = (bmnz - oz) * iz, t2z = (bmxz - oz) * iz;
+  // Translate to the ray origin (triangle.cpp:98-101).
+  float p0x = p[0][0] - ox, p0y = p[0][1] - oy, p0z = p[0][2] - oz;
+  float p1x = p[1][0] - ox, p1y = p[1][1] - oy, p1z = p[1][2] - oz;
+  float p2x = p[2][0] - ox, p2y = p[2][1] - oy, p2z = p[2][2] - oz;
+  {
+    // Per-triangle box pre-test (triangle.cpp:55-79) in the permuted axes
+    // (the max / min of three values does not depend on the axis order).
+    // The reference computes (min(p) - o) * inv; rounding of a - o is
+    // monotonic in a, so min(p) - o == min(p - o) exactly and the translated
+    // coordinates above give the same bounds. Triangle vertices are finite,
+    // so the bounds are NaN-free in both min / max forms.
+    const float ix = sel3(r.kx, r.inv[0], r.inv[1], r.inv[2]);
+    const float iy = sel3(r.ky, r.inv[0], r.inv[1], r.inv[2]);
+    const float iz = sel3(r.code, r.inv[0], r.inv[1], r.inv[2]);
+    float t1x = fminf(fminf(p0x, p1x), p2x) * ix, t2x = fmaxf(fmaxf(p0x, p1x), p2x) * ix;
+    float t1y = fminf(fminf(p0y, p1y), p2y) * iy, t2y = fmaxf(fmaxf(p0y, p1y), p2y) * iy;
+    float t1z = fminf(fminf(p0z, p1z), p2z) * iz, t2z = fmaxf(fmaxf(p0z, p1z), p2z) * iz;
     float tmin = tmax2<MM>(tmax2<MM>(tmin2<MM>(t1x, t2x), tmin2<MM>(t1y, t2y)), tmin2<MM>(t1z, t2z));
     float tmx = tmin2<MM>(tmin2<MM>(tmax2<MM>(t1x, t2x), tmax2<MM>(t1y, t2y)), tmax2<MM>(t1z, t2z));
     if (tmx < 0) return false;
     if (tmin > tmx) return false;
     if (tmax < tmin) return false;
-    return true;
-  };
-#if !BVHGPU_EDGE_FIRST
-  if (!pretest()) return false;
-#endif
-  float p0x = p[0][0] - ox, p0y = p[0][1] - oy, p0z = p[0][2] - oz;
-  float p1x = p[1][0] - ox, p1y = p[1][1] - oy, p1z = p[1][2] - oz;
-  float p2x = p[2][0] - ox, p2y = p[2][1] - oy, p2z = p[2][2] - oz;
+  }
   p0x += r.sx * p0z; p0y += r.sy * p0z;
   p1x += r.sx * p1z; p1y += r.sy * p1z;
   p2x += r.sx * p2z; p2y += r.sy * p2z;
@@ -246,9 +232,6 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
     e2 = (float)(p1typ0tx - p1txp0ty);
   }
   if ((e0 < 0 || e1 < 0 || e2 < 0) && (e0 > 0 || e1 > 0 || e2 > 0)) return false;
-#if BVHGPU_EDGE_FIRST
-  if (!pretest()) return false;
-#endif
   float det = e0 + e1 + e2;
   if (det == 0) return false;
   p0z *= r.sz; p1z *= r.sz; p2z *= r.sz;

@@ -14,7 +14,9 @@
 //
 // Passes: (1) bin of every ray and per-block bin counts; (2) per bin, an
 // exclusive scan of the counts over blocks; (3) an exclusive scan of the bin
-// totals; (4) scatter of the rays and their input indices.
+// totals; (4) scatter of the input indices into bin order. The rays are not
+// copied: the trace kernels read ray perm[i] as their i-th ray and write its
+// results to slot perm[i].
 #include "reorder.cuh"
 
 namespace bvhgpu {
@@ -141,9 +143,8 @@ __global__ void __launch_bounds__(kThreads) scan_totals_kernel(Scratch s, int nb
   block_scan_inplace(s.base, (uint64_t)nb);
 }
 
-__global__ void __launch_bounds__(kThreads) scatter_kernel(const bvhgpu_ray_t* rays, uint64_t n,
-                                                           int k, Scratch s, uint64_t blocks,
-                                                           bvhgpu_ray_t* sorted, uint32_t* perm) {
+__global__ void __launch_bounds__(kThreads) scatter_kernel(uint64_t n, int k, Scratch s,
+                                                           uint64_t blocks, uint32_t* perm) {
   extern __shared__ uint32_t cursor[];
   const int nb = bins_for(k);
   for (int i = threadIdx.x; i < nb; i += kThreads)
@@ -153,11 +154,6 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(const bvhgpu_ray_t* r
   const uint64_t end = begin + kChunk < n ? begin + kChunk : n;
   for (uint64_t i = begin + threadIdx.x; i < end; i += kThreads) {
     const uint32_t pos = atomicAdd(&cursor[s.bins[i]], 1u);
-    const float4* p = reinterpret_cast<const float4*>(rays + i);
-    float4* q = reinterpret_cast<float4*>(sorted + pos);
-    const float4 a = __ldg(p), b = __ldg(p + 1);
-    q[0] = a;
-    q[1] = b;
     perm[pos] = (uint32_t)i;
   }
 }
@@ -169,8 +165,8 @@ size_t reorder_scratch_bytes(uint64_t n, int k) {
   return align256(n * 2) + align256(nb * blocks * 4) + 2 * align256(nb * 4);
 }
 
-cudaError_t reorder_rays(const bvhgpu_ray_t* rays, uint64_t n, int k, bvhgpu_ray_t* sorted,
-                         uint32_t* perm, void* scratch, cudaStream_t st) {
+cudaError_t reorder_rays(const bvhgpu_ray_t* rays, uint64_t n, int k, uint32_t* perm,
+                         void* scratch, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (k < 1 || k > kReorderMaxK || n > 0xFFFFFFFFull) return cudaErrorInvalidValue;
   const int nb = bins_for(k);
@@ -189,7 +185,7 @@ cudaError_t reorder_rays(const bvhgpu_ray_t* rays, uint64_t n, int k, bvhgpu_ray
   bin_count_kernel<<<(unsigned)blocks, kThreads, smem, st>>>(rays, n, k, s, blocks);
   scan_bins_kernel<<<nb, kThreads, 0, st>>>(s, blocks);
   scan_totals_kernel<<<1, kThreads, 0, st>>>(s, nb);
-  scatter_kernel<<<(unsigned)blocks, kThreads, smem, st>>>(rays, n, k, s, blocks, sorted, perm);
+  scatter_kernel<<<(unsigned)blocks, kThreads, smem, st>>>(n, k, s, blocks, perm);
   return cudaGetLastError();
 }
 

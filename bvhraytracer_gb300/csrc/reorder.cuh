@@ -13,11 +13,11 @@ constexpr int kReorderMaxK = 32;  // bins per face side: 6 * 32^2 + 1 bins at mo
 // Device scratch bytes for reordering n rays into 6 k^2 + 1 bins.
 size_t reorder_scratch_bytes(uint64_t n, int k);
 
-// Writes the rays grouped by direction bin into `sorted` and, for every
-// output position, the input index into `perm`; `scratch` holds
-// reorder_scratch_bytes(n, k) bytes (256-byte aligned). Asynchronous on s.
-cudaError_t reorder_rays(const bvhgpu_ray_t* rays, uint64_t n, int k, bvhgpu_ray_t* sorted,
-                         uint32_t* perm, void* scratch, cudaStream_t s);
+// Writes into perm[0..n) the input ray indices grouped by direction bin;
+// `scratch` holds reorder_scratch_bytes(n, k) bytes (256-byte aligned).
+// Asynchronous on s.
+cudaError_t reorder_rays(const bvhgpu_ray_t* rays, uint64_t n, int k, uint32_t* perm,
+                         void* scratch, cudaStream_t s);
 
 }  // namespace dev
 }  // namespace bvhgpu

@@ -47,8 +47,8 @@ struct TraceArgs {
   uint32_t* counters;
   unsigned long long* depth_hist;
   int stack_cap;              // stack entries per ray
-  // Reordered traces: result slot of ray i is out_index[i] (null: i). The
-  // rays were permuted before the launch; results go back to input order.
+  // Reordered traces: the i-th ray the kernel takes is input ray
+  // out_index[i] (null: i), and its results go to that input slot.
   const uint32_t* out_index = nullptr;
 };
 
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
   const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (rid >= a.n) return;
 
-  const bvhgpu_ray_t in = load_ray(a.rays, rid);
+  const bvhgpu_ray_t in = load_ray(a.rays, out_slot(a, rid));
   if (isnan(in.ox)) {
     Best none;
     write_result<KIND>(sc, a, rid, false, in.tmax, none);
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
   // inner node unless the whole tree is one leaf).
   bool active = false;
   if (rid < a.n) {
-    const bvhgpu_ray_t in = load_ray(a.rays, rid);
+    const bvhgpu_ray_t in = load_ray(a.rays, out_slot(a, rid));
     Ray r = make_ray<PROFILE>(in);
     pack_ray(r, rays[tid]);
     best_leaf[tid] = 0xFFFFFFFFu;
@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
         const uint64_t my = base + __popc(idle & below);
         if (my < a.n) {
           rid = my;
-          const bvhgpu_ray_t in = load_ray(a.rays, rid);
+          const bvhgpu_ray_t in = load_ray(a.rays, out_slot(a, rid));
           if (isnan(in.ox)) {
             Best none;
             write_result<KIND>(sc, a, rid, false, in.tmax, none);

@@ -188,11 +188,12 @@ typedef struct {
                         Any-hit rays are unaffected (their tMax never shrinks). Other
                         schemes: must be 0. */
   int32_t reorder;   /* 0: trace the rays in input order. K in 1..32: first group them
-                        by direction into 6 K^2 cube-map cells (a counting sort into
-                        stream-ordered scratch of about 38 bytes per ray), trace them
-                        in that order and write every result to its input slot; at
-                        most 2^32 - 1 rays per call. Results are identical either way;
-                        incoherent rays (ambient occlusion) run faster grouped. */
+                        by direction into 6 K^2 cube-map cells (a counting sort of their
+                        indices into stream-ordered scratch of about 6 bytes per ray),
+                        trace them in that order and write every result to its input
+                        slot; at most 2^32 - 1 rays per call. Results are identical
+                        either way; incoherent rays (ambient occlusion) run faster
+                        grouped. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):
