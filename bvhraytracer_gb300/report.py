@@ -131,3 +131,50 @@ def average_leaf_depth(leaf_depth_hist_of_tree) -> float:
     """Mean depth over a histogram of leaves per depth."""
     h = np.asarray(leaf_depth_hist_of_tree, np.float64)
     return float((h * np.arange(h.shape[0])).sum() / max(h.sum(), 1.0))
+
+
+def termination_steps(counters) -> np.ndarray:
+    """Step at which each ray of a ray-stream traversal terminates, in the
+    numbering of intersectWideAlternative's terminationsPerStep
+    (compactNode.cpp:418-590): an inactive ray terminates at step 0, an
+    active one after one node or leaf visit per step, i.e. at step
+    node visits + leaf visits. The same counts hold for every scheme (the
+    kernels visit the same nodes and leaves per ray)."""
+    c = np.asarray(_host(counters), np.int64).reshape(-1, 8)
+    return c[:, 0] + c[:, 1]
+
+
+def _whisker_rows(steps: np.ndarray, group: int):
+    """Per workgroup (median, min, max, average, standard deviation) of the
+    termination steps, sorted by (median, max) like
+    CameraData::workGroupAnalysisPerImage (cameraData.h:671-778)."""
+    n = steps.shape[0] // group
+    rows = []
+    for i in range(n):
+        d = np.sort(steps[i * group:(i + 1) * group])
+        avg = float(np.float32(d.sum()) / np.float32(group))
+        sd = float(np.sqrt(np.mean((d - avg) ** 2)))
+        rows.append((int(d[int(group * 0.5)]), int(d[0]), int(d[-1]), avg, sd))
+    rows.sort(key=lambda r: (r[0], r[2]))
+    return rows
+
+
+def write_workgroup_whisker(path: str, name: str, problem: str, camera_name: str,
+                            workgroup: int, wide_alternative: int, primary_counters,
+                            secondary_counters) -> list[str]:
+    """Writes ``WorkGroupSize_<wg>_Version_<v>/<name><problem><camera>_
+    {Primary,Secondary}WorkGroupWiskerPlot.txt`` from per-ray counters of rays
+    in workgroup order (workgroup^2 consecutive rays per workgroup, one
+    secondary ray per pixel)."""
+    folder = os.path.join(path, f"WorkGroupSize_{workgroup}_Version_{wide_alternative}")
+    os.makedirs(folder, exist_ok=True)
+    out = []
+    for kind, c in (("Primary", primary_counters), ("Secondary", secondary_counters)):
+        rows = _whisker_rows(termination_steps(c), workgroup * workgroup)
+        fn = os.path.join(folder, f"{name}{problem}{camera_name}_{kind}WorkGroupWiskerPlot.txt")
+        with open(fn, "w") as fh:
+            fh.write("median, min, max, lowerStdDeviation, upperStdDeviation\n")
+            for r in rows:
+                fh.write(f"{r[0]}, {r[1]}, {r[2]}, {_fmt(r[3])}, {_fmt(r[4])}\n")
+        out.append(fn)
+    return out

@@ -409,9 +409,7 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
 }
 
 /* intersectWideAlternative (compactNode.cpp:357-601) over packets of
- * `packet` consecutive rays. Per-ray results equal the per-ray traversal;
- * the per-step work statistics are written to steps (nullable): for each
- * packet, up to max_steps entries of {node rays, leaf rays} per step. */
+ * `packet` consecutive rays. Per-ray results equal the per-ray traversal. */
 int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* rays, uint64_t n,
                                      int shadow, int packet, ohit_t* hits, uint8_t* occluded,
                                      octr_t* ctrs, uint64_t* hist) {

@@ -51,3 +51,28 @@ def test_perf_file_values(tmp_path):
     assert first_number(text, "Raytracer total time:") == 0.00958
     assert first_number(text, "Time for triangle intersections (SUM):") is None
     assert first_number(text, "Triangle Count:") == 999744
+
+
+def test_termination_steps_match_stream_oracle():
+    """The termination step of every ray (node + leaf visits) reproduces the
+    per-step termination counts of the stream traversal."""
+    from oracle import oracle as O
+    from tests import _scenes as TS
+    tris, b, cv = TS.bvh("clutter120", 8, 8)
+    rays = TS.clutter_rays(tris)[:256 * 4]
+    rays[5, 0] = np.nan
+    r = O.trace_instrumented(cv, rays, False, packet=256)
+    steps = R.termination_steps(r["counters"])
+    assert steps[5] == 0 and (steps[np.arange(len(steps)) != 5] > 0).all()
+    assert np.array_equal(steps, r["counters"][:, 0].astype(np.int64) + r["counters"][:, 1])
+
+
+def test_whisker_file(tmp_path):
+    c = np.zeros((8, 8), np.int64)
+    c[:, 0] = [3, 1, 2, 5, 9, 9, 9, 9]
+    c[:, 1] = [1, 1, 1, 1, 0, 1, 2, 3]
+    files = R.write_workgroup_whisker(str(tmp_path), "s", "_b8_l8", "_c0", 2, 1, c, c)
+    lines = open(files[0]).read().splitlines()
+    assert lines[0] == "median, min, max, lowerStdDeviation, upperStdDeviation"
+    # groups: [4,2,3,6] -> median 4 (index 2 of sorted 2,3,4,6), [9,10,11,12] -> 11
+    assert lines[1].startswith("4, 2, 6, 3.75") and lines[2].startswith("11, 9, 12, 10.5")
