@@ -41,10 +41,11 @@ METRIC = "Mrays/s"
 # is the ray stream plus cold misses (the BVH stays in L2), so it grows with
 # the ray count and is scaled by it.
 # Source: profiles/trace_persistent_p2_ao_clutter250k_N8L8.md
-# With reorder = 8 the launch is the four reorder passes plus the trace
-# (rays read twice and written once more, the index array, the bins).
+# With reorder = 8 the launch is the four reorder passes plus the trace (the
+# rays read once to bin them and once, gathered in bin order, by the trace;
+# the bins and the index permutation).
 # Source: profiles/reorder_k8_persistent_p2_ao_clutter250k_N8L8.md
-NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, 8: 565612800 / 4147200}
+NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, 8: 445689088 / 4147200}
 
 
 def parse():

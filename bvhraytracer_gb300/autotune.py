@@ -30,6 +30,8 @@ DEFAULT_OPTIONS = (
     {"scheme": "per_ray", "block": 128, "reorder": 8},
     {"scheme": "persistent", "policy": 0, "refill": 16, "reorder": 8},
     {"scheme": "persistent", "policy": 2, "refill": 16, "reorder": 8},
+    {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 8},
+    {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10},
 )
 DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
 

@@ -499,10 +499,12 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
       if (e != cudaSuccess) return cuda_error(e, "create pipeline event");
     }
   }
-  // Chunks of a quarter of the batch, between 256 Ki and 4 Mi rays.
-  uint64_t chunk = (n + 3) / 4;
+  // Chunks of an eighth of the batch, between 256 Ki and 2 Mi rays: small
+  // enough that the first copy in and the last copy out (the parts that do
+  // not overlap a trace) are short, large enough to fill the GPU.
+  uint64_t chunk = (n + 7) / 8;
   chunk = std::max<uint64_t>(chunk, 256ull << 10);
-  chunk = std::min<uint64_t>(chunk, 4ull << 20);
+  chunk = std::min<uint64_t>(chunk, 2ull << 20);
   chunk = std::min<uint64_t>(chunk, n);
   const size_t out_rec = closest ? sizeof(bvhgpu_hit_t) : 1;
   const size_t ray_bytes = align256(chunk * sizeof(bvhgpu_ray_t));

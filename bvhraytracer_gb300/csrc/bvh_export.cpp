@@ -268,18 +268,21 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
     std::memcpy(meta + 8, &leaf_mask, 2);
     meta[10] = (uint8_t)c.child_count;
     meta[11] = c.depth;
-    // Push sequences per axis and direction, one child per nibble.
+    // Per axis: the push sequence of rays whose direction[axis] <= 0 (the
+    // traverseOrderEachAxis order, one child per nibble) and its inverse
+    // (the position of each child in it). The other direction pushes the
+    // same children in the opposite order.
     const int wb = perm_word_bytes(nm);
     uint8_t* perm = meta + 12;
     for (int a = 0; a < 3; ++a) {
       const size_t c_n = bn->order[a].size();
-      uint64_t up = 0, down = 0;
+      uint64_t up = 0, inv = 0;
       for (size_t k = 0; k < c_n; ++k) {
         up |= (uint64_t)(uint8_t)bn->order[a][k] << (4 * k);
-        down |= (uint64_t)(uint8_t)bn->order[a][c_n - 1 - k] << (4 * k);
+        inv |= (uint64_t)k << (4 * (uint8_t)bn->order[a][k]);
       }
       std::memcpy(perm + (a * 2 + 0) * wb, &up, wb);
-      std::memcpy(perm + (a * 2 + 1) * wb, &down, wb);
+      std::memcpy(perm + (a * 2 + 1) * wb, &inv, wb);
     }
     uint8_t* lcnt = meta + 12 + 6 * wb;
     for (uint32_t j = 0; j < c.child_count; ++j) {

@@ -249,29 +249,42 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   };
   // Push sequence: child-index order for fast any-hit rays
   // (fastNodeManager.h:1481-1488), else traverseOrderEachAxis[code] in the
-  // ray's direction.
+  // ray's direction: ascending positions of the stored sequence when
+  // direction[code] <= 0, descending otherwise (compactNode.cpp:781-809).
+  // pm holds the positions of the hit children, built from the inverse
+  // sequence over the hit children only.
   uint64_t perm;
+  uint32_t pm;
+  bool descending = false;
   if (PROFILE == BVHGPU_PROFILE_FAST && KIND == BVHGPU_ANY) {
     perm = 0xFEDCBA9876543210ull;
+    pm = hit;
   } else {
-    const uint8_t* pp = rec + F::PERM + (r.code * 2 + (r.reverse ? 0 : 1)) * F::PW;
+    const uint8_t* pp = rec + F::PERM + r.code * 2 * F::PW;
+    uint64_t inv;
     if (F::PW == 2) {
-      perm = rec_u32<SH>(pp - ((uintptr_t)pp & 2)) >> (((uintptr_t)pp & 2) * 8);
-      perm &= 0xFFFFull;
+      const uint32_t w = rec_u32<SH>(pp);  // sequence | inverse << 16, 4-byte aligned
+      perm = w & 0xFFFFu;
+      inv = w >> 16;
     } else if (F::PW == 4) {
       perm = rec_u32<SH>(pp);
+      inv = rec_u32<SH>(pp + 4);
     } else {
       perm = (uint64_t)rec_u32<SH>(pp) | ((uint64_t)rec_u32<SH>(pp + 4) << 32);
+      inv = (uint64_t)rec_u32<SH>(pp + 8) | ((uint64_t)rec_u32<SH>(pp + 12) << 32);
     }
+    pm = 0;
+    uint32_t h = hit;
+    while (h) {
+      const int c = __ffs(h) - 1;
+      h &= h - 1u;
+      pm |= 1u << (uint32_t)((inv >> (4 * c)) & 15u);
+    }
+    descending = !r.reverse;
   }
-  // Positions in the push sequence whose child was hit.
-  uint32_t pm = 0;
-#pragma unroll
-  for (int k = 0; k < NM; ++k) pm |= ((hit >> (uint32_t)((perm >> (4 * k)) & 15u)) & 1u) << k;
-  pm &= (1u << count) - 1u;
   while (pm) {
-    const int k = __ffs(pm) - 1;
-    pm &= pm - 1u;
+    const int k = descending ? 31 - __clz(pm) : __ffs(pm) - 1;
+    pm &= ~(1u << k);
     const int c = (int)((perm >> (4 * k)) & 15u);
     if (sp >= cap) return false;
     stack[sp * stride] = entry(c);
