@@ -419,9 +419,10 @@ def run_ours(a):
     traffic = None
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
-            and dom_opts.get("policy") == 2 and dom_opts.get("reorder", 0) in NCU_TRAFFIC_PER_AO_RAY
-            and chosen[dom][0].node_format == "fp32"):
-        traffic = NCU_TRAFFIC_PER_AO_RAY[dom_opts.get("reorder", 0)] * int(batches[dom][0].shape[0])
+            and dom_opts.get("policy") == 2 and chosen[dom][0].node_format == "fp32"):
+        # The reorder passes' bytes per ray do not depend on the bin count K.
+        key = 8 if dom_opts.get("reorder", 0) else 0
+        traffic = NCU_TRAFFIC_PER_AO_RAY[key] * int(batches[dom][0].shape[0])
 
     compare = {}
     if not a.no_compare:
@@ -469,7 +470,8 @@ def run_ours(a):
                 else "fallback",
                 "traffic": traffic,
                 "traffic_source": ("ncu DRAM bytes per AO ray of a 4.1M-ray capture on the "
-                                   "251k-triangle scene, scaled by rays" if traffic else None),
+                                   "251k-triangle scene (reorder K=8 when the plan reorders), "
+                                   "scaled by rays" if traffic else None),
                 "algorithmic_bytes_per_launch": alg[dom]["bytes"],
                 "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
             },

@@ -102,6 +102,17 @@ class Bvh:
                                               "prim_ids", "prim_tri9")]))
         return out
 
+    def node_records(self, *, gang: int = 4, leaf_memory: int = 0, node_format: str = "fp32",
+                     top_levels: int = 0) -> np.ndarray:
+        """Node records of the device layout as encoded on the host (uint8)."""
+        p = N.SceneParams(gang, leaf_memory, _FORMAT[node_format], top_levels, 0)
+        n = C.c_uint64()
+        N.check(N.lib().bvhgpu_bvh_node_records(self._h, C.byref(p), None, 0, C.byref(n)))
+        out = np.empty(n.value, np.uint8)
+        N.check(N.lib().bvhgpu_bvh_node_records(self._h, C.byref(p), _ptr(out), n.value,
+                                                C.byref(n)))
+        return out
+
     def export_fast(self, gang: int = 4, node_memory: int = 0, leaf_memory: int = 0) -> dict:
         """FastNodeManager<gang, node_memory> arrays and trianglePoints."""
         node_memory = node_memory or -(-self.info["branching"] // gang) * gang
@@ -287,6 +298,14 @@ class Scene:
         """Raises if a kernel of this scene recorded a device-side error."""
         sp = stream.cuda_stream if stream is not None else 0
         N.check(N.lib().bvhgpu_scene_status(self._h, C.c_void_p(sp)))
+
+    def node_records(self) -> np.ndarray:
+        """The device node records, copied to the host (uint8)."""
+        n = C.c_uint64()
+        N.check(N.lib().bvhgpu_scene_node_records(self._h, None, 0, C.byref(n)))
+        out = np.empty(n.value, np.uint8)
+        N.check(N.lib().bvhgpu_scene_node_records(self._h, _ptr(out), n.value, C.byref(n)))
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None):

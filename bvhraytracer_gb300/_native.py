@@ -124,6 +124,9 @@ _SIGS = {
     "bvhgpu_secondary_rays": (C.c_int, [_P, _P, _P, C.c_uint64, C.POINTER(Secondary), _P, _P,
                                         _P]),
     "bvhgpu_ao_factor": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
+    "bvhgpu_scene_node_records": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "bvhgpu_bvh_node_records": (C.c_int, [_P, C.POINTER(SceneParams), _P, C.c_uint64,
+                                          C.POINTER(C.c_uint64)]),
 }
 
 # Every symbol the public header declares (checked by the CPU tests).

@@ -19,6 +19,7 @@
 #include "launch.cuh"
 #include "reorder.cuh"
 #include "raygen.cuh"
+#include "q8_encode.cuh"
 #include "batched.cuh"
 #include "adjoint.cuh"
 
@@ -353,8 +354,15 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   auto* s = new (std::nothrow) bvhgpu_scene();
   if (!s) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   s->device = params->device;
-  int rc = build_device_layout(h->bvh, params->gang, params->leaf_memory, params->node_format,
+  // Q8 records are encoded on the device from the FP32 ones.
+  const bool q8 = params->node_format == BVHGPU_NODES_Q8;
+  int rc = build_device_layout(h->bvh, params->gang, params->leaf_memory, BVHGPU_NODES_FP32,
                                params->top_levels, s->layout);
+  if (rc == BVHGPU_OK && q8) {
+    s->layout.node_format = BVHGPU_NODES_Q8;
+    s->layout.record_bytes = q8_record_bytes(s->layout.node_stride);
+    s->layout.boxes_ordered = false;
+  }
   if (rc) {
     delete s;
     return set_error(rc, "device layout failed (gang 4/8, leaf_memory >= L and a gang multiple <= 16)");
@@ -389,6 +397,23 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   }
   e = cudaMalloc((void**)&s->d_status, 16);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, 16);
+  if (e == cudaSuccess && q8) {
+    uint8_t* q8_nodes = nullptr;
+    const size_t bytes = std::max<size_t>((size_t)s->layout.n_inner * s->layout.record_bytes, 16);
+    e = cudaMalloc((void**)&q8_nodes, bytes);
+    if (e == cudaSuccess)
+      e = dev::launch_q8_encode(s->layout.node_stride, s->d_nodes, q8_nodes, s->layout.n_inner,
+                                s->d_status, nullptr);
+    int st = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(s->d_nodes);
+    s->d_nodes = q8_nodes;
+    if (e == cudaSuccess && st != 0) {
+      s->release();
+      delete s;
+      return set_error(BVHGPU_ERR_UNSUPPORTED, "Q8 encoding: a box could not be enclosed");
+    }
+  }
   if (e == cudaSuccess)
     e = cudaMalloc((void**)&s->d_queue, sizeof(unsigned long long) * bvhgpu_scene::kQueueSlots);
   if (e == cudaSuccess)
@@ -412,6 +437,30 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   s->layout.leaves.clear();
   s->layout.leaves.shrink_to_fit();
   *out = s;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_scene_node_records(bvhgpu_scene_t s, void* out, uint64_t capacity, uint64_t* bytes) {
+  if (!s || !bytes) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  const uint64_t n = (uint64_t)s->layout.n_inner * (uint64_t)s->layout.record_bytes;
+  *bytes = n;
+  if (!out) return BVHGPU_OK;
+  if (capacity < n) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e == cudaSuccess) e = cudaMemcpy(out, s->d_nodes, n, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? BVHGPU_OK : cuda_error(e, "node records");
+}
+
+int bvhgpu_bvh_node_records(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* p, void* out,
+                            uint64_t capacity, uint64_t* bytes) {
+  if (!h || !p || !bytes) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  DeviceLayout lay;
+  int rc = build_device_layout(h->bvh, p->gang, p->leaf_memory, p->node_format, p->top_levels, lay);
+  if (rc) return set_error(rc, "device layout failed");
+  *bytes = lay.nodes.size();
+  if (!out) return BVHGPU_OK;
+  if (capacity < lay.nodes.size()) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
+  std::memcpy(out, lay.nodes.data(), lay.nodes.size());
   return BVHGPU_OK;
 }
 

@@ -24,6 +24,7 @@ constexpr uint32_t kLeafIndexMask = (1u << 27) - 1;
 // Device error codes recorded in the scene's status word.
 constexpr int kDevErrStackOverflow = BVHGPU_ERR_STACK_OVERFLOW;
 constexpr int kDevErrTimeout = BVHGPU_ERR_TIMEOUT;
+constexpr int kDevErrQ8Encode = BVHGPU_ERR_UNSUPPORTED;
 
 // pbrt gamma(n) = (n*eps/2) / (1 - n*eps/2), evaluated in double and rounded
 // to float as MSVC does for the reference (src/util.h:13-17, 44-48).

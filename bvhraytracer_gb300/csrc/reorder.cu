@@ -158,7 +158,110 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(uint64_t n, int k, Sc
   }
 }
 
+// Job of grid chunk c: the last job whose first chunk is <= c.
+__device__ __forceinline__ int seg_job_of(const SegTable& t, uint32_t c) {
+  int lo = 0, hi = t.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t.jobs[mid].first_chunk <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kThreads) seg_bin_count_kernel(const __grid_constant__ SegTable t) {
+  extern __shared__ uint32_t hist[];
+  const int nb = bins_for(t.k);
+  const SegJob& J = t.jobs[seg_job_of(t, blockIdx.x)];
+  const uint32_t chunk = blockIdx.x - J.first_chunk;
+  for (int i = threadIdx.x; i < nb; i += kThreads) hist[i] = 0;
+  __syncthreads();
+  const uint64_t begin = (uint64_t)chunk * kChunk;
+  const uint64_t end = begin + kChunk < J.n ? begin + kChunk : J.n;
+  for (uint64_t i = begin + threadIdx.x; i < end; i += kThreads) {
+    const float4* p = reinterpret_cast<const float4*>(J.rays + i);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    const uint32_t bin = dir_bin(a.x, b.x, b.y, b.z, t.k);
+    J.bins[i] = (uint16_t)bin;
+    atomicAdd(&hist[bin], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += kThreads)
+    J.counts[(uint64_t)i * J.nchunks + chunk] = hist[i];
+}
+
+// blockIdx.x = bin, blockIdx.y = job: scan of the bin's counts over the
+// job's chunks; the bin total goes to base[bin] (scanned next).
+__global__ void __launch_bounds__(kThreads) seg_scan_bins_kernel(const __grid_constant__ SegTable t) {
+  const SegJob& J = t.jobs[blockIdx.y];
+  const uint32_t total = block_scan_inplace(J.counts + (uint64_t)blockIdx.x * J.nchunks, J.nchunks);
+  if (threadIdx.x == 0) J.base[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kThreads) seg_scan_totals_kernel(const __grid_constant__ SegTable t) {
+  const SegJob& J = t.jobs[blockIdx.x];
+  block_scan_inplace(J.base, (uint64_t)bins_for(t.k));
+}
+
+__global__ void __launch_bounds__(kThreads) seg_scatter_kernel(const __grid_constant__ SegTable t) {
+  extern __shared__ uint32_t cursor[];
+  const int nb = bins_for(t.k);
+  const SegJob& J = t.jobs[seg_job_of(t, blockIdx.x)];
+  const uint32_t chunk = blockIdx.x - J.first_chunk;
+  for (int i = threadIdx.x; i < nb; i += kThreads)
+    cursor[i] = J.base[i] + J.counts[(uint64_t)i * J.nchunks + chunk];
+  __syncthreads();
+  const uint64_t begin = (uint64_t)chunk * kChunk;
+  const uint64_t end = begin + kChunk < J.n ? begin + kChunk : J.n;
+  for (uint64_t i = begin + threadIdx.x; i < end; i += kThreads) {
+    const uint32_t pos = atomicAdd(&cursor[J.bins[i]], 1u);
+    J.perm[pos] = (uint32_t)i;
+  }
+}
+
 }  // namespace
+
+uint32_t seg_chunks(uint64_t n) { return (uint32_t)((n + kChunk - 1) / kChunk); }
+
+size_t seg_job_scratch_bytes(uint64_t n, int k) {
+  const uint64_t nb = bins_for(k);
+  return align256(n * 4) + align256(n * 2) + align256(nb * seg_chunks(n) * 4) + align256(nb * 4);
+}
+
+void seg_job_carve(SegJob& j, void* scratch, uint64_t n, int k) {
+  const uint64_t nb = bins_for(k);
+  uint8_t* b = static_cast<uint8_t*>(scratch);
+  j.perm = reinterpret_cast<uint32_t*>(b);
+  b += align256(n * 4);
+  j.bins = reinterpret_cast<uint16_t*>(b);
+  b += align256(n * 2);
+  j.counts = reinterpret_cast<uint32_t*>(b);
+  b += align256(nb * seg_chunks(n) * 4);
+  j.base = reinterpret_cast<uint32_t*>(b);
+  j.n = (uint32_t)n;
+  j.nchunks = seg_chunks(n);
+}
+
+cudaError_t reorder_jobs(const SegTable& t, cudaStream_t st) {
+  if (t.n_jobs == 0 || t.total_chunks == 0) return cudaSuccess;
+  if (t.k < 1 || t.k > kReorderMaxK || t.n_jobs > kSegMaxJobs) return cudaErrorInvalidValue;
+  const int nb = bins_for(t.k);
+  const size_t smem = (size_t)nb * 4;
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(seg_bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(seg_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  seg_bin_count_kernel<<<t.total_chunks, kThreads, smem, st>>>(t);
+  seg_scan_bins_kernel<<<dim3(nb, t.n_jobs), kThreads, 0, st>>>(t);
+  seg_scan_totals_kernel<<<t.n_jobs, kThreads, 0, st>>>(t);
+  seg_scatter_kernel<<<t.total_chunks, kThreads, smem, st>>>(t);
+  return cudaGetLastError();
+}
 
 size_t reorder_scratch_bytes(uint64_t n, int k) {
   const uint64_t nb = bins_for(k), blocks = blocks_for(n);

@@ -352,6 +352,17 @@ int bvhgpu_secondary_rays(bvhgpu_scene_t scene, const bvhgpu_ray_t* primary,
 int bvhgpu_ao_factor(const uint8_t* occluded, uint64_t n, int32_t samples, float* factor,
                      void* stream);
 
+/* ---- node records (no reference counterpart) --------------------------- */
+/* Copies the scene's device node records (n_inner * record bytes; Q8 scenes
+ * encode them on the device) to `out`; *bytes gets the size (out may be null
+ * to query it). */
+int bvhgpu_scene_node_records(bvhgpu_scene_t scene, void* out, uint64_t capacity,
+                              uint64_t* bytes);
+/* The same records as encoded on the host by the layout builder, for the
+ * given scene parameters (the specification the device encoding matches). */
+int bvhgpu_bvh_node_records(bvhgpu_bvh_t bvh, const bvhgpu_scene_params_t* params, void* out,
+                            uint64_t capacity, uint64_t* bytes);
+
 /* Caps the traversal stack at `entries` per ray (0: the tree's worst case,
  * the default, which never overflows). Rays that need more stop, report a
  * miss and record BVHGPU_ERR_STACK_OVERFLOW for bvhgpu_scene_status; the

@@ -377,3 +377,13 @@ def test_reorder_keeps_results_in_input_order(scheme, kw, k):
     with pytest.raises(pkg.BvhgpuError):
         scene.trace(d, reorder=33)
     scene.status()
+
+
+@pytest.mark.parametrize("n,l", [(4, 4), (8, 8), (12, 4), (16, 16)])
+def test_device_q8_encoding_matches_host(n, l):
+    """Q8 scenes encode their node records on the device; the bytes equal the
+    host layout builder's, which is the format's specification."""
+    tris, b, _ = TS.bvh("clutter120", n, l)
+    for fmt, top in (("q8", 0), ("q8", 2), ("fp32", 0)):
+        sc = pkg.Scene(b, node_format=fmt, top_levels=top)
+        assert np.array_equal(sc.node_records(), b.node_records(node_format=fmt, top_levels=top))
