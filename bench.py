@@ -86,6 +86,9 @@ def parse():
                         "512x512 + shadow rays; sweep: the clutter frame for every N, L in "
                         "{4,8,12,16}^2, per-ray vs ray-stream")
     p.add_argument("--scenes", type=int, default=64)
+    p.add_argument("--job-reorder", type=int, default=8,
+                   help="batch64: direction bins per cube face side for the AO jobs (0 = off)")
+    p.add_argument("--job-refill", type=int, default=24, help="batch64: refill threshold")
     p.add_argument("--tune-nl", action="store_true",
                    help="batch64: let the autotuner pick N/L per scene")
     return p.parse_args()
@@ -531,7 +534,7 @@ def run_batch(a):
     from bvhraytracer_gb300 import scenes as S
     dev = torch.device("cuda", 0)
     t_setup = time.time()
-    scenes, jobs_plain, chosen = [], [], []
+    scenes, jobs_plain, chosen, job_reorder = [], [], [], []
     n_tris = n_rays = 0
     for kind, tt, rr, i in batch_scenes(a):
         tris, primary, light = make_batch_scene(kind, tt, rr, i)
@@ -559,10 +562,11 @@ def run_batch(a):
         m, p, n = S.surface(tris, primary, pkg.hit_prims(h.cpu().numpy()))
         sh = torch.from_numpy(S.shadow_rays(p, n, light)).to(dev)
         ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris), seed=i)).to(dev)
-        for rays, k in ((d_p, "closest"), (sh, "any"), (ao, "any")):
+        for rays, k, ro in ((d_p, "closest", 0), (sh, "any", 0), (ao, "any", a.job_reorder)):
             out = (torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
                    if k == "closest" else torch.empty(rays.shape[0], dtype=torch.uint8, device=dev))
             jobs_plain.append((scene, rays, k, out))
+            job_reorder.append(ro)
             n_rays += rays.shape[0]
         scenes.append({"kind": kind, "triangles": int(bvh.info["n_tris"]), "N": bn, "L": bl,
                        "block": block, "rays": int(d_p.shape[0] + sh.shape[0] + ao.shape[0])})
@@ -576,8 +580,11 @@ def run_batch(a):
         for (scene, rays, k, out), b in zip(jobs_plain, blocks):
             scene.trace(rays, kind=k, scheme="per_ray", block=b, out=out)
 
+    # The AO jobs' rays are grouped by direction inside the batched call.
+    jobs_batched = [j + (ro,) for j, ro in zip(jobs_plain, job_reorder)]
+
     def batched():
-        pkg.trace_jobs(jobs_plain, policy=2, refill=16)
+        pkg.trace_jobs(jobs_batched, policy=2, refill=a.job_refill)
 
     def timed(fn, steps):
         for _ in range(a.warmup):
@@ -618,13 +625,17 @@ def run_batch(a):
             "workload": f"{a.scenes} scenes in one persistent launch, triangles log-uniform "
                         f"1k-500k, rays log-uniform 4k-2M (primary:shadow:AO 1:1:4)",
             "triangles_total": n_tris, "rays_per_step": n_rays, "jobs": len(jobs_plain),
-            "method": "bvhgpu_trace_jobs (speculative any-hit policy) in a CUDA graph",
+            "method": "bvhgpu_trace_jobs (speculative any-hit policy, AO jobs grouped into "
+                      f"6x{a.job_reorder}x{a.job_reorder} direction bins) in a CUDA graph"
+                      if a.job_reorder else
+                      "bvhgpu_trace_jobs (speculative any-hit policy) in a CUDA graph",
             "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,
             "ms_sequential_plain_launches": ms_seq,
             "speedup_vs_sequential": ms_seq / ms_graph, "results_identical": bool(same),
             "autotuned_nl": bool(a.tune_nl), "scenes": scenes, "setup_s": round(setup_s, 1),
         },
-        "clocks": clocks, "gpu_launches": a.steps,
+        # one batched launch per step, plus the four segmented reorder passes
+        "clocks": clocks, "gpu_launches": a.steps * (5 if a.job_reorder else 1),
     }
     print(json.dumps(line))
 

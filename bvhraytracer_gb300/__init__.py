@@ -365,19 +365,22 @@ def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: 
                stream=None) -> None:
     """Traces many (scene, rays) jobs in one persistent launch.
 
-    ``jobs``: list of ``(scene, rays, kind, out)`` with device tensors (rays
-    ``[n, 8]`` float32; ``out`` ``[n, 4]`` float32 for ``"closest"``, ``[n]``
-    uint8 for ``"any"``); up to 192 jobs, scenes of any N, L and node format.
-    Per-ray results equal :meth:`Scene.trace`'s. Stream-ordered (default:
-    torch's current stream); allocates nothing, so it can be recorded in a
-    CUDA graph.
+    ``jobs``: list of ``(scene, rays, kind, out)`` or ``(scene, rays, kind,
+    out, reorder)`` with device tensors (rays ``[n, 8]`` float32; ``out``
+    ``[n, 4]`` float32 for ``"closest"``, ``[n]`` uint8 for ``"any"``); up to
+    192 jobs, scenes of any N, L and node format; ``reorder`` = K groups that
+    job's rays into 6 K^2 direction bins first. Per-ray results equal
+    :meth:`Scene.trace`'s. Stream-ordered (default: torch's current stream)
+    and graph-capturable; reordered jobs take stream-ordered scratch.
     """
     import torch
     arr = (N.Job * max(1, len(jobs)))()
     dev = None
-    for i, (scene, rays, kind, out) in enumerate(jobs):
+    for i, job in enumerate(jobs):
+        scene, rays, kind, out = job[:4]
+        reorder = job[4] if len(job) > 4 else 0
         k = _KIND[kind]
-        arr[i] = N.Job(scene.handle, _ptr(rays), rays.shape[0], k, 0,
+        arr[i] = N.Job(scene.handle, _ptr(rays), rays.shape[0], k, reorder,
                        _ptr(out) if k == N.CLOSEST else None, _ptr(out) if k == N.ANY else None)
         dev = rays.device
     o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)

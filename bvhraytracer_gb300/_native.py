@@ -63,7 +63,7 @@ class Batch(C.Structure):
 
 class Job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("n", C.c_uint64),
-                ("kind", C.c_int32), ("pad", C.c_int32), ("hits", C.c_void_p),
+                ("kind", C.c_int32), ("reorder", C.c_int32), ("hits", C.c_void_p),
                 ("occluded", C.c_void_p)]
 
 

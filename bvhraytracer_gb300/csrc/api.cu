@@ -640,9 +640,20 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
   int device = -1, stack = 1, sms = 0;
   bvhgpu_scene_t first = nullptr;
   int nj = 0;
+  // Reordered jobs: one segmented counting sort over all of them.
+  std::unique_ptr<dev::SegTable> seg(new (std::nothrow) dev::SegTable());
+  if (!seg) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  int seg_k = 0;
+  size_t seg_bytes = 0;
+  std::vector<size_t> seg_off;
+  std::vector<int> seg_job;  // job table slot of each reordered job
   for (int i = 0; i < n_jobs; ++i) {
     const bvhgpu_job_t& j = jobs[i];
     if (!j.scene) return set_error(BVHGPU_ERR_BAD_ARG, "job without a scene");
+    if (j.reorder < 0 || j.reorder > dev::kReorderMaxK)
+      return set_error(BVHGPU_ERR_BAD_ARG, "job reorder must be 0..32");
+    if (j.reorder && seg_k && j.reorder != seg_k)
+      return set_error(BVHGPU_ERR_UNSUPPORTED, "reordered jobs of one call must share K");
     if (j.kind != BVHGPU_CLOSEST && j.kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "job kind");
     if (j.n >= (1ull << 32)) return set_error(BVHGPU_ERR_BAD_ARG, "job with 2^32 rays or more");
     if (device >= 0 && j.scene->device != device)
@@ -669,6 +680,16 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.fmt = (int8_t)j.scene->layout.node_format;
     d.kind = (int8_t)j.kind;
     d.boxes_ordered = j.scene->layout.boxes_ordered ? 1 : 0;
+    d.perm = nullptr;
+    if (j.reorder && j.n > 1) {
+      seg_k = j.reorder;
+      seg_off.push_back(seg_bytes);
+      seg_bytes += dev::seg_job_scratch_bytes(j.n, seg_k);
+      seg_job.push_back(nj - 1);
+      dev::SegJob& sj = seg->jobs[seg->n_jobs++];
+      sj.rays = j.rays;
+      sj.n = (uint32_t)j.n;
+    }
     total += j.n;
     stack = std::max(stack, stack_cap(j.scene));
     sms = j.scene->sm_count;
@@ -684,7 +705,32 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
   t->policy = cfg.policy;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  e = dev::launch_batched(*t, cfg.profile, sms, (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  if (seg->n_jobs > 0) {
+    e = cudaMallocAsync(&scratch, seg_bytes, st);
+    if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "reorder scratch allocation failed");
+    seg->k = seg_k;
+    uint32_t chunk = 0;
+    for (int i = 0; i < seg->n_jobs; ++i) {
+      dev::SegJob& sj = seg->jobs[i];
+      dev::seg_job_carve(sj, static_cast<uint8_t*>(scratch) + seg_off[i], sj.n, seg_k);
+      sj.first_chunk = chunk;
+      chunk += sj.nchunks;
+      t->jobs[seg_job[i]].perm = sj.perm;
+    }
+    seg->total_chunks = chunk;
+    e = dev::reorder_jobs(*seg, st);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(scratch, st);
+      return cuda_error(e, "job reorder");
+    }
+  }
+  e = dev::launch_batched(*t, cfg.profile, sms, st);
+  if (scratch) {
+    cudaError_t f = cudaFreeAsync(scratch, st);
+    if (e == cudaSuccess) e = f;
+  }
   if (e != cudaSuccess) return cuda_error(e, "batched launch");
   return BVHGPU_OK;
 }

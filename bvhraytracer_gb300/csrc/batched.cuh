@@ -10,7 +10,7 @@
 namespace bvhgpu {
 namespace dev {
 
-constexpr int kMaxJobs = 192;  // 192 jobs x 80 bytes in the parameter block
+constexpr int kMaxJobs = 192;  // 192 jobs x 88 bytes in the parameter block
 
 struct JobDev {
   const uint8_t* nodes;
@@ -29,8 +29,11 @@ struct JobDev {
   int8_t kind;             // BVHGPU_CLOSEST / BVHGPU_ANY
   int8_t boxes_ordered;    // SceneDev::boxes_ordered of the job's scene
   int8_t pad[6];
+  // Reordered job: the job's i-th ray in queue order is ray perm[i], and its
+  // result goes to slot perm[i] (null: i).
+  const uint32_t* perm;
 };
-static_assert(sizeof(JobDev) == 80, "job record size");
+static_assert(sizeof(JobDev) == 88, "job record size");
 
 struct JobTable {
   JobDev jobs[kMaxJobs];
@@ -111,6 +114,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
           job = lo;
           const JobDev& J = t.jobs[job];
           local = (uint32_t)(g - J.ray_begin);
+          if (J.perm) local = __ldg(J.perm + local);
           sc.nodes = J.nodes;
           sc.leaves = J.leaves;
           sc.leaf_prim = J.leaf_prim;

@@ -223,14 +223,19 @@ int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n
  * fastNodeManager.h:92-156, 277-450, extended across scenes). Results per ray
  * equal bvhgpu_trace's. All scenes must live on the stream's device; the
  * options' profile and policy (0 or 2) apply to every job. Stream-ordered, no
- * allocation, no synchronisation (so it can be recorded in a CUDA graph). */
+ * synchronisation (so it can be recorded in a CUDA graph); no allocation
+ * unless a job is reordered, whose scratch (about 6 bytes per ray) comes from
+ * the stream-ordered allocator (cudaMallocAsync / cudaFreeAsync on the
+ * stream, which graph capture records as memory nodes). */
 #define BVHGPU_MAX_JOBS 192
 typedef struct {
   bvhgpu_scene_t scene;
   const bvhgpu_ray_t* rays; /* device, 16-byte aligned */
   uint64_t n;               /* < 2^32 */
   int32_t kind;             /* BVHGPU_CLOSEST or BVHGPU_ANY */
-  int32_t pad;
+  int32_t reorder;          /* 0, or K (1..32): trace the job's rays grouped into 6 K^2
+                               direction bins (see bvhgpu_trace_opts_t.reorder); all
+                               reordered jobs of a call use the same K */
   bvhgpu_hit_t* hits;       /* closest: device, 16-byte aligned */
   uint8_t* occluded;        /* any: device */
 } bvhgpu_job_t;

@@ -104,3 +104,45 @@ def test_jobs_limits():
     with pytest.raises(pkg.BvhgpuError):
         pkg.trace_jobs(jobs * 100)  # 200 jobs > 192
     pkg.trace_jobs([])
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_reordered_jobs(graph):
+    """Jobs whose rays are grouped by direction first (per-job segmented
+    counting sort, results back in input order) equal the per-scene traces,
+    eagerly and recorded in a CUDA graph (the scratch is stream-ordered)."""
+    items = _scenes()
+    jobs, refs = _jobs(items, "instrumented")
+    jobs = [j + ((8 if j[2] == "any" or i % 4 == 0 else 0),) for i, j in enumerate(jobs)]
+
+    def check():
+        for (scene, rays, kind, out, _), ref in zip(jobs, refs):
+            if kind == "closest":
+                assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
+            else:
+                assert torch.equal(out, ref)
+
+    if not graph:
+        for j in jobs:
+            j[3].fill_(7)
+        pkg.trace_jobs(jobs, policy=2, refill=24)
+        torch.cuda.synchronize()
+        check()
+        with pytest.raises(pkg.BvhgpuError):
+            pkg.trace_jobs([jobs[1], jobs[3][:4] + (10,)])  # reordered jobs must share K
+        return
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        pkg.trace_jobs(jobs, stream=s)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        pkg.trace_jobs(jobs)
+    for _ in range(2):
+        for j in jobs:
+            j[3].fill_(5)
+        g.replay()
+        torch.cuda.synchronize()
+        check()
