@@ -735,7 +735,8 @@ def run_adjoint(a):
         def step():
             t, u, w, prim = D.ray_hit(v, f, r, scene)
             m = (prim >= 0) & (p_tgt >= 0)
-            loss = ((t - t_tgt)[m] ** 2).sum()
+            # masked by multiplication (no boolean indexing, so no host sync)
+            loss = torch.where(m, (t - t_tgt) ** 2, torch.zeros_like(t)).sum()
             gv, gr = torch.autograd.grad(loss, (v, r))
             return loss, gv, gr, prim, m
 

@@ -180,10 +180,26 @@ __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a
   const float3 g_p0 = to_f3(df3{df_neg(df_add(df_add(g_s.x, g_e1.x), g_e2.x)),
                                 df_neg(df_add(df_add(g_s.y, g_e1.y), g_e2.y)),
                                 df_neg(df_add(df_add(g_s.z, g_e1.z), g_e2.z))});
-  float* gt9 = a.grad_tri9 + (size_t)prim * 9;
-  atomicAdd(gt9 + 0, g_p0.x); atomicAdd(gt9 + 1, g_p0.y); atomicAdd(gt9 + 2, g_p0.z);
-  atomicAdd(gt9 + 3, g_p1.x); atomicAdd(gt9 + 4, g_p1.y); atomicAdd(gt9 + 5, g_p1.z);
-  atomicAdd(gt9 + 6, g_p2.x); atomicAdd(gt9 + 7, g_p2.y); atomicAdd(gt9 + 8, g_p2.z);
+  if (a.faces) {
+    const int32_t* fv = a.faces + (size_t)prim * 3;
+    const uint32_t v0 = (uint32_t)__ldg(fv + 0), v1 = (uint32_t)__ldg(fv + 1);
+    const uint32_t v2 = (uint32_t)__ldg(fv + 2);
+    if (v0 >= a.n_verts || v1 >= a.n_verts || v2 >= a.n_verts) {
+      record_error(sc.status, BVHGPU_ERR_BAD_ARG);
+    } else {
+      float* g0 = a.grad_verts + (size_t)v0 * 3;
+      float* g1 = a.grad_verts + (size_t)v1 * 3;
+      float* g2 = a.grad_verts + (size_t)v2 * 3;
+      atomicAdd(g0 + 0, g_p0.x); atomicAdd(g0 + 1, g_p0.y); atomicAdd(g0 + 2, g_p0.z);
+      atomicAdd(g1 + 0, g_p1.x); atomicAdd(g1 + 1, g_p1.y); atomicAdd(g1 + 2, g_p1.z);
+      atomicAdd(g2 + 0, g_p2.x); atomicAdd(g2 + 1, g_p2.y); atomicAdd(g2 + 2, g_p2.z);
+    }
+  } else {
+    float* gt9 = a.grad_tri9 + (size_t)prim * 9;
+    atomicAdd(gt9 + 0, g_p0.x); atomicAdd(gt9 + 1, g_p0.y); atomicAdd(gt9 + 2, g_p0.z);
+    atomicAdd(gt9 + 3, g_p1.x); atomicAdd(gt9 + 4, g_p1.y); atomicAdd(gt9 + 5, g_p1.z);
+    atomicAdd(gt9 + 6, g_p2.x); atomicAdd(gt9 + 7, g_p2.y); atomicAdd(gt9 + 8, g_p2.z);
+  }
   reinterpret_cast<float4*>(gr)[0] = make_float4(g_o.x, g_o.y, g_o.z, 0.f);
   reinterpret_cast<float4*>(gr)[1] = make_float4(g_dd.x, g_dd.y, g_dd.z, 0.f);
 }

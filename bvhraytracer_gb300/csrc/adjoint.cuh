@@ -14,6 +14,11 @@ struct AdjointArgs {
   float* grad_tri9;         // per input triangle: dL/dp0, dL/dp1, dL/dp2 (accumulated)
   float* grad_rays;         // per ray: dL/do (3), 0, dL/dd (3), 0 (written)
   int stack_cap;
+  // With faces: the vertex gradients are added into grad_verts[3 * v + axis]
+  // for the triangle's vertex ids faces[3 * prim + k] instead of grad_tri9.
+  const int32_t* faces = nullptr;
+  float* grad_verts = nullptr;
+  uint32_t n_verts = 0;     // vertex ids outside [0, n_verts) are skipped and reported
 };
 
 cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s);

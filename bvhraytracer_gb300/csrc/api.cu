@@ -759,6 +759,36 @@ int bvhgpu_adjoint(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n, const
   return BVHGPU_OK;
 }
 
+
+int bvhgpu_adjoint_vertices(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
+                            const float* grad_hits, const int32_t* faces, uint64_t n_faces,
+                            uint64_t n_verts, float* grad_verts, float* grad_rays,
+                            void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  if (n == 0) return BVHGPU_OK;
+  if (!rays || !grad_hits || !faces || !grad_verts || !grad_rays || ((uintptr_t)rays & 15) ||
+      ((uintptr_t)grad_hits & 15) || ((uintptr_t)grad_rays & 15) || ((uintptr_t)faces & 3) ||
+      ((uintptr_t)grad_verts & 3))
+    return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: null or misaligned buffer");
+  if (n_faces < s->prim_slot.size())
+    return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: fewer faces than input triangles");
+  if (n_verts >= (1ull << 32)) return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: 2^32 vertices or more");
+  if (s->layout.node_format != BVHGPU_NODES_FP32)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "adjoint: FP32 node scenes only");
+  if ((size_t)s->max_stack * 128 * 4 > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  dev::AdjointArgs a{rays, n, reinterpret_cast<const float4*>(grad_hits), nullptr, grad_rays,
+                     stack_cap(s)};
+  a.faces = faces;
+  a.grad_verts = grad_verts;
+  a.n_verts = (uint32_t)n_verts;
+  e = dev::launch_adjoint(s->dev_view(), s->layout.node_stride, a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "adjoint launch");
+  return BVHGPU_OK;
+}
+
 }  // extern "C"
 
 namespace bvhgpu {

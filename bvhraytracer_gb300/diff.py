@@ -24,7 +24,8 @@ class _RayHit(torch.autograd.Function):
         res = scene.trace(rays.detach().contiguous(), profile="fast")["hits"]
         ctx.scene = scene
         ctx.n_verts = verts.shape[0]
-        ctx.save_for_backward(rays, faces)
+        faces32 = faces.to(torch.int32).contiguous()
+        ctx.save_for_backward(rays, faces32)
         prim = res.view(torch.int32)[:, 0].clone()
         ctx.mark_non_differentiable(prim)
         return res[:, 1].clone(), res[:, 2].clone(), res[:, 3].clone(), prim
@@ -40,14 +41,15 @@ class _RayHit(torch.autograd.Function):
             return z if x is None else x.to(torch.float32)
 
         grad_hits = torch.stack([z, g(gt), g(gu), g(gv)], dim=1).contiguous()
-        grad_tri9 = torch.zeros((faces.shape[0], 9), dtype=torch.float32, device=dev)
         grad_rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
-        stream = torch.cuda.current_stream(dev)
-        N.check(N.lib().bvhgpu_adjoint(ctx.scene.handle, rays.data_ptr(), n, grad_hits.data_ptr(),
-                                       grad_tri9.data_ptr(), grad_rays.data_ptr(),
-                                       C.c_void_p(stream.cuda_stream)))
         grad_verts = torch.zeros((ctx.n_verts, 3), dtype=torch.float32, device=dev)
-        grad_verts.index_add_(0, faces.reshape(-1), grad_tri9.view(-1, 3))
+        stream = torch.cuda.current_stream(dev)
+        # The kernel adds each hit triangle's vertex gradients straight into
+        # grad_verts through the face indices.
+        N.check(N.lib().bvhgpu_adjoint_vertices(
+            ctx.scene.handle, rays.data_ptr(), n, grad_hits.data_ptr(), faces.data_ptr(),
+            faces.shape[0], ctx.n_verts, grad_verts.data_ptr(), grad_rays.data_ptr(),
+            C.c_void_p(stream.cuda_stream)))
         return grad_verts, grad_rays, None, None
 
 

@@ -25,7 +25,7 @@
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
  *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
- *   bvhgpu_adjoint            no reference counterpart: reverse pass of triIntersect{L}'s
+ *   bvhgpu_adjoint[_vertices] no reference counterpart: reverse pass of triIntersect{L}'s
  *                             Moller-Trumbore (rayTracerTemplate.ispc:35-76)
  *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
  *                             structure, fastNodeManager.h:92-156, across scenes)
@@ -271,6 +271,17 @@ int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t scene, const float* fastr
  * 16-byte aligned; stream-ordered. */
 int bvhgpu_adjoint(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                    const float* grad_hits, float* grad_tri9, float* grad_rays, void* stream);
+
+/* The same backward pass for an indexed mesh: instead of grad_tri9, the
+ * gradients of the hit triangle's three vertices are added (atomically: zero
+ * first) into grad_verts[3 * v .. 3 * v + 2] for v = faces[3 * prim + k]
+ * (int32 vertex ids of each input triangle, n_faces >= the input triangle
+ * count). Vertex ids outside [0, n_verts) are skipped and recorded as
+ * BVHGPU_ERR_BAD_ARG for bvhgpu_scene_status. */
+int bvhgpu_adjoint_vertices(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
+                            const float* grad_hits, const int32_t* faces, uint64_t n_faces,
+                            uint64_t n_verts, float* grad_verts, float* grad_rays,
+                            void* stream);
 
 /* ---- tracing without allocation --------------------------------------- */
 /* No counterpart in the reference (its renderer allocates nothing on a GPU).

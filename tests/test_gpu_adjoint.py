@@ -169,3 +169,42 @@ def test_adjoint_against_fp64_finite_differences():
             adr.append(gR[i, comp])
     fdr, adr = np.array(fdr), np.array(adr)
     assert np.linalg.norm(adr - fdr) / np.linalg.norm(fdr) < 1e-4
+
+
+def test_per_triangle_and_per_vertex_entry_points_agree():
+    """bvhgpu_adjoint (per-triangle gradients, scattered by the caller) and
+    bvhgpu_adjoint_vertices (accumulated through the face indices) give the
+    same vertex gradients; out-of-range vertex ids are reported, not written."""
+    import ctypes as C
+    from bvhraytracer_gb300 import _native as N
+    v, f, r, scene, t_tgt, p_tgt = _case(n=32, res=64)
+    n = r.shape[0]
+    gh = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    gh[:, 1] = torch.linspace(-1, 1, n, device="cuda")
+    gh[:, 2] = 0.3
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    tri9 = torch.zeros((f.shape[0], 9), dtype=torch.float32, device="cuda")
+    gr1 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    rays = r.detach().contiguous()
+    N.check(N.lib().bvhgpu_adjoint(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
+                                   tri9.data_ptr(), gr1.data_ptr(), st))
+    gv1 = torch.zeros((v.shape[0], 3), dtype=torch.float32, device="cuda")
+    gv1.index_add_(0, f.reshape(-1), tri9.view(-1, 3))
+    f32 = f.to(torch.int32).contiguous()
+    gv2 = torch.zeros_like(gv1)
+    gr2 = torch.empty_like(gr1)
+    N.check(N.lib().bvhgpu_adjoint_vertices(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
+                                            f32.data_ptr(), f32.shape[0], v.shape[0],
+                                            gv2.data_ptr(), gr2.data_ptr(), st))
+    torch.cuda.synchronize()
+    assert torch.equal(gr1, gr2)
+    assert (gv1 - gv2).abs().max() <= 1e-5 * gv1.abs().max()
+    bad = f32.clone()
+    bad[:] = v.shape[0] + 5
+    gv3 = torch.zeros_like(gv1)
+    N.check(N.lib().bvhgpu_adjoint_vertices(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
+                                            bad.data_ptr(), bad.shape[0], v.shape[0],
+                                            gv3.data_ptr(), gr2.data_ptr(), st))
+    with pytest.raises(Exception):
+        scene.status()
+    assert torch.count_nonzero(gv3) == 0
