@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--ao", type=int, default=8)
     p.add_argument("--scheme", default="auto",
                    choices=["auto", "per_ray", "stream", "persistent"])
+    p.add_argument("--plan", default="",
+                   help="fixed per-batch plan instead of the autotuner: three "
+                        "'scheme[,policy,refill,reorder]' specs joined by ';'")
     p.add_argument("--nodes", default="fp32", choices=["fp32", "q8"])
     p.add_argument("--top-levels", type=int, default=0)
     p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
@@ -290,7 +293,24 @@ def run_ours(a):
     names = ["primary (closest)", "shadow (any)", "AO (any)"]
 
     # Per-batch configuration: the autotuner's choice, or one fixed scheme.
-    if a.scheme == "auto":
+    if a.plan:
+        # A fixed per-batch plan, e.g. the autotuner's usual choice, so that a
+        # profiler run (whose serialisation skews the autotuner's timings)
+        # traces the same launches: "scheme[,policy,refill,reorder]" per batch.
+        chosen = []
+        for spec in a.plan.split(";"):
+            f = spec.split(",")
+            o = {"scheme": f[0]}
+            if len(f) > 1:
+                o.update(policy=int(f[1]), refill=int(f[2]))
+            if len(f) > 3 and int(f[3]):
+                o["reorder"] = int(f[3])
+            chosen.append((plain, o))
+        if len(chosen) != 3:
+            raise SystemExit("--plan needs three batch specs (primary;shadow;AO)")
+        method = f"fixed plan {a.plan}"
+        plan_desc = [dict(o, layout="fp32/top0") for _, o in chosen]
+    elif a.scheme == "auto":
         plan, scenes = autotune.tune_scene(bvh, [(r, k) for r, k, _ in batches],
                                            profile=a.profile, reps=2, device=local,
                                            scenes={("fp32", 0): plain})
