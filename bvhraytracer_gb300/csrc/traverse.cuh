@@ -38,6 +38,10 @@ struct SceneDev {
 #ifndef BVHGPU_NEARFAR
 #define BVHGPU_NEARFAR 1
 #endif
+// 1: leaf triangles loaded four at a time with 128-bit loads; 0: one at a time.
+#ifndef BVHGPU_LEAF_VEC
+#define BVHGPU_LEAF_VEC 1
+#endif
 
 struct TraceArgs {
   const bvhgpu_ray_t* rays;
@@ -333,6 +337,7 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
   // Row offsets: instrumented rays read the permuted axes directly.
   int ax0 = 0, ax1 = 1, ax2 = 2;
   if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) { ax0 = r.kx; ax1 = r.ky; ax2 = r.code; }
+#if BVHGPU_LEAF_VEC
   for (int g = 0; g < cnt; g += 4) {
     float4 c[3][3];
 #pragma unroll
@@ -350,6 +355,17 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
       for (int v = 0; v < 3; ++v)
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[v][a] = f4get(c[v][a], k);
+#else
+  {
+    for (int i = 0; i < cnt; ++i) {
+      float p[3][3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        p[v][0] = __ldg(blk + (v * 3 + ax0) * stride + i);
+        p[v][1] = __ldg(blk + (v * 3 + ax1) * stride + i);
+        p[v][2] = __ldg(blk + (v * 3 + ax2) * stride + i);
+      }
+#endif
       float t, b1, b2;
       bool h;
       if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED)
