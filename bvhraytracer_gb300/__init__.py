@@ -73,6 +73,9 @@ class Bvh:
                           int(drop_zero_area))
         h = C.c_void_p()
         N.check(N.lib().bvhgpu_bvh_build(t.ctypes.data, t.shape[0], C.byref(p), C.byref(h)))
+        self._adopt(h, p)
+
+    def _adopt(self, h, p) -> None:
         self._h = h
         self.params = p
         info = N.BvhInfo()
@@ -80,6 +83,27 @@ class Bvh:
         self.info = {f: getattr(info, f) for f, _ in N.BvhInfo._fields_}
         self.info["root_lo"] = list(info.root_lo)
         self.info["root_hi"] = list(info.root_hi)
+
+    @classmethod
+    def from_compact(cls, arrays: dict, branching: int, leaf_size: int) -> "Bvh":
+        """A tree built elsewhere (the reference's own builder), from its
+        CompactNodeV3 arrays in the layout :meth:`export_compact` returns
+        (bvhgpu_bvh_import_compact)."""
+        a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        dt = {"lo3": np.float32, "hi3": np.float32, "child_begin": np.uint32,
+              "child_count": np.uint32, "prim_begin": np.uint32, "prim_count": np.uint32,
+              "order48": np.int8, "prim_ids": np.uint32, "prim_tri9": np.float32}
+        a = {k: np.ascontiguousarray(a[k], dt[k]) for k in dt}
+        n = a["child_count"].shape[0]
+        h = C.c_void_p()
+        N.check(N.lib().bvhgpu_bvh_import_compact(
+            n, *[_ptr(a[k]) for k in ("lo3", "hi3", "child_begin", "child_count", "prim_begin",
+                                      "prim_count", "order48")],
+            a["prim_ids"].shape[0], _ptr(a["prim_ids"]), _ptr(a["prim_tri9"]), branching,
+            leaf_size, C.byref(h)))
+        self = cls.__new__(cls)
+        self._adopt(h, N.BuildParams(branching, leaf_size, 1, 1, 1.0, 1))
+        return self
 
     @property
     def handle(self):

@@ -99,6 +99,8 @@ _SIGS = {
     "bvhgpu_last_error": (C.c_char_p, []),
     "bvhgpu_bvh_build": (C.c_int, [_P, C.c_uint64, C.POINTER(BuildParams), C.POINTER(_P)]),
     "bvhgpu_bvh_info": (C.c_int, [_P, C.POINTER(BvhInfo)]),
+    "bvhgpu_bvh_import_compact": (C.c_int, [C.c_uint64] + [_P] * 7 + [C.c_uint64, _P, _P,
+                                            C.c_int32, C.c_int32, C.POINTER(_P)]),
     "bvhgpu_bvh_free": (C.c_int, [_P]),
     "bvhgpu_sah_factor": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "bvhgpu_bvh_export_compact": (C.c_int, [_P] + [_P] * 10),

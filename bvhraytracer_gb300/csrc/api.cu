@@ -192,6 +192,37 @@ static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
+// Stream-ordered scratch for the reorder passes comes from a memory pool of
+// the library's own (one per device, created on first use) that keeps freed
+// memory instead of returning it at every synchronisation, so repeated
+// traces reuse it; the process's default pool is left as the caller set it.
+static int scratch_alloc(int device, void** p, size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+    if (!pools[device]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = device;
+      cudaError_t e = cudaMemPoolCreate(&pools[device], &props);
+      if (e != cudaSuccess) {
+        pools[device] = nullptr;
+        return cuda_error(e, "scratch memory pool");
+      }
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pools[device], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = pools[device];
+  }
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+  return e == cudaSuccess ? BVHGPU_OK : set_error(BVHGPU_ERR_OOM, "scratch allocation failed");
+}
+
 // launch() after grouping the rays by direction when cfg.reorder > 0: a
 // counting sort writes the input indices in bin order, the kernels take the
 // rays in that order and write every result to its input slot. The scratch
@@ -204,8 +235,9 @@ static int launch_reordered(bvhgpu_scene_t s, dev::TraceArgs a, const dev::Launc
   const size_t perm_bytes = align256(a.n * 4);
   const size_t bytes = perm_bytes + dev::reorder_scratch_bytes(a.n, cfg.reorder);
   void* p = nullptr;
-  cudaError_t e = cudaMallocAsync(&p, bytes, st);
-  if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "reorder scratch allocation failed");
+  int arc = scratch_alloc(s->device, &p, bytes, st);
+  if (arc) return arc;
+  cudaError_t e;
   auto* perm = reinterpret_cast<uint32_t*>(p);
   e = dev::reorder_rays(a.rays, a.n, cfg.reorder, perm, static_cast<uint8_t*>(p) + perm_bytes,
                         st);
@@ -251,6 +283,37 @@ int bvhgpu_bvh_build(const float* tris, uint64_t n_tris, const bvhgpu_build_para
                          "finite vertices, at least one non-degenerate triangle)");
   }
   h->n_input = n_tris;
+  *out = h;
+  return BVHGPU_OK;
+}
+
+int bvhgpu_bvh_import_compact(uint64_t n_nodes, const float* lo3, const float* hi3,
+                              const uint32_t* child_begin, const uint32_t* child_count,
+                              const uint32_t* prim_begin, const uint32_t* prim_count,
+                              const int8_t* order48, uint64_t n_prims, const uint32_t* prim_ids,
+                              const float* prim_tri9, int32_t branching, int32_t leaf_size,
+                              bvhgpu_bvh_t* out) {
+  if (!out) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
+  *out = nullptr;
+  auto* h = new (std::nothrow) bvhgpu_bvh();
+  if (!h) return set_error(BVHGPU_ERR_OOM, "host allocation failed");
+  int rc;
+  try {
+    rc = h->bvh.import_compact(n_nodes, lo3, hi3, child_begin, child_count, prim_begin,
+                               prim_count, order48, n_prims, prim_ids, prim_tri9, branching,
+                               leaf_size);
+  } catch (const std::bad_alloc&) {
+    rc = BVHGPU_ERR_OOM;
+  }
+  if (rc != BVHGPU_OK) {
+    delete h;
+    return set_error(rc, "import: not a valid CompactNodeV3 tree (children after their parent, "
+                         "one parent each, orders are permutations, leaves of 1..L primitives "
+                         "inside the primitive array, finite vertices)");
+  }
+  uint32_t max_id = 0;
+  for (uint64_t i = 0; i < n_prims; ++i) max_id = std::max(max_id, prim_ids[i]);
+  h->n_input = (uint64_t)max_id + 1;
   *out = h;
   return BVHGPU_OK;
 }
@@ -708,8 +771,8 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
   cudaStream_t st = (cudaStream_t)stream;
   void* scratch = nullptr;
   if (seg->n_jobs > 0) {
-    e = cudaMallocAsync(&scratch, seg_bytes, st);
-    if (e != cudaSuccess) return set_error(BVHGPU_ERR_OOM, "reorder scratch allocation failed");
+    int arc = scratch_alloc(device, &scratch, seg_bytes, st);
+    if (arc) return arc;
     seg->k = seg_k;
     uint32_t chunk = 0;
     for (int i = 0; i < seg->n_jobs; ++i) {

@@ -329,4 +329,120 @@ int Bvh::build(const float* tri9, uint64_t n_tris, const BuildParams& prm) {
   return BVHGPU_OK;
 }
 
+int Bvh::import_compact(uint64_t n_nodes, const float* lo3, const float* hi3,
+                        const uint32_t* child_begin, const uint32_t* child_count,
+                        const uint32_t* prim_begin, const uint32_t* prim_count,
+                        const int8_t* order48, uint64_t n_prims, const uint32_t* prim_ids,
+                        const float* prim_tri9, int branching, int leaf_size) {
+  if (!lo3 || !hi3 || !child_begin || !child_count || !prim_begin || !prim_count || !order48 ||
+      !prim_ids || !prim_tri9)
+    return BVHGPU_ERR_BAD_ARG;
+  if (n_nodes == 0 || n_nodes > (1ull << 27) || n_prims == 0 || n_prims > (1ull << 31))
+    return BVHGPU_ERR_BAD_ARG;
+  if (branching < 2 || branching > 16 || leaf_size < 1 || leaf_size > 16) return BVHGPU_ERR_BAD_ARG;
+  params = BuildParams();
+  params.branching = branching;
+  params.leaf_size = leaf_size;
+  // Structure: children after their parent, in range, one parent each; leaf
+  // ranges inside the primitive array; per-axis orders are permutations.
+  std::vector<uint8_t> parents(n_nodes, 0);
+  std::vector<uint8_t> depth(n_nodes, 0);
+  for (uint64_t id = 0; id < n_nodes; ++id) {
+    const uint32_t cc = child_count[id], pc = prim_count[id];
+    if (cc > 0) {
+      if (pc != 0 || cc < 1 || (int)cc > branching) return BVHGPU_ERR_BAD_ARG;
+      const uint64_t cb = child_begin[id];
+      if (cb <= id || cb + cc > n_nodes) return BVHGPU_ERR_BAD_ARG;
+      for (int a = 0; a < 3; ++a) {
+        uint32_t seen = 0;
+        for (uint32_t i = 0; i < cc; ++i) {
+          const int v = order48[id * 48 + a * 16 + i];
+          if (v < 0 || (uint32_t)v >= cc || (seen >> v) & 1u) return BVHGPU_ERR_BAD_ARG;
+          seen |= 1u << v;
+        }
+      }
+      for (uint32_t j = 0; j < cc; ++j) {
+        if (parents[cb + j]++) return BVHGPU_ERR_BAD_ARG;
+        if (depth[id] >= 255) return BVHGPU_ERR_BAD_ARG;
+        depth[cb + j] = (uint8_t)(depth[id] + 1);
+      }
+    } else {
+      if (pc < 1 || (int)pc > leaf_size || (uint64_t)prim_begin[id] + pc > n_prims)
+        return BVHGPU_ERR_BAD_ARG;
+    }
+  }
+  for (uint64_t id = 1; id < n_nodes; ++id)
+    if (parents[id] != 1) return BVHGPU_ERR_BAD_ARG;
+  // Triangles in sorted order.
+  tris.assign(n_prims, Triangle{});
+  prims.resize(n_prims);
+  for (uint64_t i = 0; i < n_prims; ++i) {
+    Triangle& t = tris[i];
+    for (int v = 0; v < 3; ++v)
+      for (int k = 0; k < 3; ++k) {
+        t.p[v][k] = prim_tri9[i * 9 + v * 3 + k];
+        if (!std::isfinite(t.p[v][k])) return BVHGPU_ERR_BAD_ARG;
+      }
+    for (int k = 0; k < 3; ++k) {
+      t.bmin[k] = std::min(std::min(t.p[0][k], t.p[1][k]), t.p[2][k]);
+      t.bmax[k] = std::max(std::max(t.p[0][k], t.p[1][k]), t.p[2][k]);
+      t.center[k] = t.bmax[k] * 0.5f + t.bmin[k] * 0.5f;
+    }
+    t.id = prim_ids[i];
+    prims[i] = (uint32_t)i;
+  }
+  nodes.assign(n_nodes, CompactNode{});
+  node_ptr.assign(n_nodes, nullptr);
+  imported_.clear();
+  imported_.reserve(n_nodes);
+  root.reset();
+  leaf_count = inner_count = 0;
+  bvh_depth = 0;
+  for (uint64_t id = 0; id < n_nodes; ++id) {
+    CompactNode& c = nodes[id];
+    for (int k = 0; k < 3; ++k) {
+      c.bmin[k] = lo3[id * 3 + k];
+      c.bmax[k] = hi3[id * 3 + k];
+    }
+    c.depth = depth[id];
+    std::fill(&c.order[0][0], &c.order[0][0] + 48, (int8_t)0);
+    auto bn = std::make_unique<BuildNode>();
+    for (int k = 0; k < 3; ++k) {
+      bn->bmin[k] = c.bmin[k];
+      bn->bmax[k] = c.bmax[k];
+    }
+    bn->depth = c.depth;
+    if (child_count[id] > 0) {
+      c.child_begin = child_begin[id];
+      c.child_count = child_count[id];
+      for (int a = 0; a < 3; ++a)
+        for (uint32_t i = 0; i < c.child_count; ++i) {
+          c.order[a][i] = order48[id * 48 + a * 16 + i];
+          bn->order[a].push_back(c.order[a][i]);
+        }
+      ++inner_count;
+    } else {
+      c.prim_begin = prim_begin[id];
+      c.prim_count = prim_count[id];
+      bn->begin = c.prim_begin;
+      bn->end = c.prim_begin + c.prim_count;
+      ++leaf_count;
+      bvh_depth = std::max(bvh_depth, (int)c.depth + 1);
+    }
+    node_ptr[id] = bn.get();
+    imported_.push_back(std::move(bn));
+  }
+  // Worst-case depth-first stack: 1 + max over root-to-leaf paths of the sum
+  // of (children - 1); children are numbered after their parents.
+  std::vector<int> extra(n_nodes, 0);
+  for (uint64_t id = n_nodes; id-- > 0;) {
+    if (child_count[id] == 0) continue;
+    int m = 0;
+    for (uint32_t j = 0; j < child_count[id]; ++j) m = std::max(m, extra[child_begin[id] + j]);
+    extra[id] = (int)child_count[id] - 1 + m;
+  }
+  max_stack = 1 + extra[0];
+  return BVHGPU_OK;
+}
+
 }  // namespace bvhgpu

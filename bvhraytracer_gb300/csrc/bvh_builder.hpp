@@ -72,6 +72,21 @@ class Bvh {
 
   // Builds from T x 9 floats (p0, p1, p2). Returns 0 or a bvhgpu status.
   int build(const float* tri9, uint64_t n_tris, const BuildParams& p);
+
+  // Adopts a tree built elsewhere (e.g. by the reference's own builder), given
+  // as the CompactNodeV3 view that export_compact writes: nodes in reference
+  // numbering (root 0, children consecutive and numbered after their parent),
+  // order48[node*48 + axis*16 + i], primitives in sorted order with their
+  // input ids. The structure is validated; depths and the worst-case stack
+  // height are recomputed. Returns 0 or a bvhgpu status.
+  int import_compact(uint64_t n_nodes, const float* lo3, const float* hi3,
+                     const uint32_t* child_begin, const uint32_t* child_count,
+                     const uint32_t* prim_begin, const uint32_t* prim_count,
+                     const int8_t* order48, uint64_t n_prims, const uint32_t* prim_ids,
+                     const float* prim_tri9, int branching, int leaf_size);
+
+ private:
+  std::vector<std::unique_ptr<BuildNode>> imported_;  // per-node orders of an imported tree
 };
 
 }  // namespace bvhgpu

@@ -57,6 +57,7 @@ int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, Fast
               (i < (int)bn->order[0].size()) ? bn->order[a][i] : (int8_t)0;
     }
     if (c.prim_count > 0) {
+      if (c.prim_count > (uint32_t)leaf_memory) return BVHGPU_ERR_BAD_ARG;
       int real = (((int)c.prim_count - 1) / gang + 1) * gang;
       size_t p_begin = out.tri_points.size();
       size_t p_tmp = p_begin + real;
@@ -299,6 +300,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
   for (size_t id = 0; id < n; ++id) {
     const CompactNode& c = bvh.nodes[id];
     if (c.child_count != 0) continue;
+    if (c.prim_count > (uint32_t)leaf_memory) return BVHGPU_ERR_BAD_ARG;
     const size_t k = (size_t)leaf_id[id];
     float* blk = &out.leaves[k * 9 * leaf_memory];
     const int real = (((int)c.prim_count - 1) / gang + 1) * gang;

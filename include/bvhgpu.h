@@ -13,6 +13,8 @@
  *                              src/accelerationStructure/aabb.cpp:71-206,
  *                              src/rayTracer.cpp:604-623)
  *   bvhgpu_sah_factor         RayTracer::loadSahFactor (src/rayTracer.cpp:880-925)
+ *   bvhgpu_bvh_import_compact the upload of a tree the reference built itself
+ *                             (its CompactNodeManager arrays, compactNode.cpp:11-116)
  *   bvhgpu_bvh_export_compact CompactNodeManager<CompactNodeV3> constructor
  *                             (src/accelerationStructure/compactNode.cpp:11-116)
  *   bvhgpu_bvh_export_fast    FastNodeManager constructor
@@ -95,6 +97,23 @@ typedef struct {
 int bvhgpu_bvh_build(const float* tris, uint64_t n_tris, const bvhgpu_build_params_t* params,
                      bvhgpu_bvh_t* out);
 int bvhgpu_bvh_info(bvhgpu_bvh_t bvh, bvhgpu_bvh_info_t* info);
+
+/* A tree built elsewhere — typically by the reference's own builder — handed
+ * over as its CompactNodeV3 arrays (the layout bvhgpu_bvh_export_compact
+ * writes: CompactNodeManager's compactNodes and the primitive list,
+ * compactNode.cpp:11-116): n_nodes nodes in reference numbering (root 0,
+ * children consecutive and numbered after their parent, as customTreeOrder
+ * gives), order48[node*48 + axis*16 + i] = traverseOrderEachAxis, leaves of
+ * 1..leaf_size primitives; n_prims triangles (prim_tri9, 9 floats each, in
+ * the primitive list's order) with their input ids. The arrays are copied and
+ * validated; depths and the worst-case stack height are recomputed. The
+ * result is used like a bvhgpu_bvh_build result. */
+int bvhgpu_bvh_import_compact(uint64_t n_nodes, const float* lo3, const float* hi3,
+                              const uint32_t* child_begin, const uint32_t* child_count,
+                              const uint32_t* prim_begin, const uint32_t* prim_count,
+                              const int8_t* order48, uint64_t n_prims, const uint32_t* prim_ids,
+                              const float* prim_tri9, int32_t branching, int32_t leaf_size,
+                              bvhgpu_bvh_t* out);
 int bvhgpu_bvh_free(bvhgpu_bvh_t bvh);
 
 /* sahNodeFactor for (N, L) from the reference's SSE table, with N and L

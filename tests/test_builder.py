@@ -152,3 +152,45 @@ def test_fast_export_layout(gang, n, l):
             for a in range(3):
                 assert np.array_equal(f["order"][i, a * nm:a * nm + cnt], c["order48"][i, a * 16:a * 16 + cnt])
     assert tp.shape[0] == b.info["n_leaves"] * lm * 9
+
+
+def test_import_compact_round_trip():
+    """A tree handed over as CompactNodeV3 arrays (bvhgpu_bvh_import_compact)
+    exports the same arrays, FastNodeManager view and device records, with
+    the same worst-case stack height."""
+    from tests import _scenes as TS
+    for n, l in ((4, 4), (8, 8), (16, 4)):
+        _, b, _ = TS.bvh("clutter120", n, l)
+        c = b.export_compact()
+        b2 = pkg.Bvh.from_compact(c, n, l)
+        c2 = b2.export_compact()
+        for k in c:
+            assert np.array_equal(c[k], c2[k]), k
+        f, f2 = b.export_fast(), b2.export_fast()
+        for k in ("bounds", "begin", "order", "child_type", "tri_points"):
+            assert np.array_equal(np.asarray(f[k]).view(np.uint8), np.asarray(f2[k]).view(np.uint8)), k
+        for fmt in ("fp32", "q8"):
+            assert np.array_equal(b.node_records(node_format=fmt), b2.node_records(node_format=fmt))
+        assert b2.info["max_stack"] == b.info["max_stack"]
+        assert b2.info["depth"] == b.info["depth"]
+
+
+def test_import_compact_rejects_bad_trees():
+    from tests import _scenes as TS
+    _, b, _ = TS.bvh("clutter120", 4, 4)
+    c = b.export_compact()
+    inner = np.nonzero(c["child_count"] > 0)[0]
+    leaf = np.nonzero(c["child_count"] == 0)[0]
+
+    def bad(mut):
+        d = {k: v.copy() for k, v in c.items()}
+        mut(d)
+        with pytest.raises(pkg.BvhgpuError):
+            pkg.Bvh.from_compact(d, 4, 4)
+
+    bad(lambda d: d["child_begin"].__setitem__(inner[1], 0))            # child before parent
+    bad(lambda d: d["child_begin"].__setitem__(inner[0], len(d["child_count"])))  # out of range
+    bad(lambda d: d["order48"].__setitem__((inner[0], 1), d["order48"][inner[0], 0]))  # not a permutation
+    bad(lambda d: d["prim_count"].__setitem__(leaf[0], 5))               # leaf above L
+    bad(lambda d: d["prim_begin"].__setitem__(leaf[0], len(d["prim_ids"])))  # outside the primitives
+    bad(lambda d: d["prim_tri9"].__setitem__((0, 0), np.inf))            # non-finite vertex

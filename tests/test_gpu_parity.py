@@ -387,3 +387,15 @@ def test_device_q8_encoding_matches_host(n, l):
     for fmt, top in (("q8", 0), ("q8", 2), ("fp32", 0)):
         sc = pkg.Scene(b, node_format=fmt, top_levels=top)
         assert np.array_equal(sc.node_records(), b.node_records(node_format=fmt, top_levels=top))
+
+
+def test_imported_tree_traces_like_the_built_one():
+    """A scene made from CompactNodeV3 arrays handed over by another builder
+    (here: this builder's export) traces bit for bit like the original."""
+    tris, b, cv = TS.bvh("clutter120", 8, 8)
+    b2 = pkg.Bvh.from_compact(b.export_compact(), 8, 8)
+    rays = dev(TS.clutter_rays(tris))
+    a = pkg.Scene(b).trace(rays, counters=True)
+    c = pkg.Scene(b2).trace(rays, counters=True)
+    assert torch.equal(a["hits"].view(torch.int32), c["hits"].view(torch.int32))
+    assert torch.equal(a["counters"], c["counters"])
