@@ -569,13 +569,16 @@ def run_batch(a):
                 tris, batches_fn, pairs=tuple((n, l) for n in (4, 8, 16) for l in (4, 8, 16)),
                 layouts=(("fp32", 0),), options=({"scheme": "per_ray", "block": 32},
                                                  {"scheme": "per_ray", "block": 64},
-                                                 {"scheme": "per_ray", "block": 128}),
+                                                 {"scheme": "per_ray", "block": 128},
+                                                 {"scheme": "per_ray", "block": 128,
+                                                  "stack": "local"}),
                 reps=1)
             _, (bn, bl), bvh, plan, tuned = best
             scene = tuned[("fp32", 0)]
             block = plan.choices[0][1]["block"]
+            stack = plan.choices[0][1].get("stack", "shared")
         else:
-            bn, bl, block = a.branching, a.leaf, 128
+            bn, bl, block, stack = a.branching, a.leaf, 128, "shared"
             bvh = pkg.Bvh(tris, bn, bl)
             scene = pkg.Scene(bvh)
         h = scene.trace(d_p)["hits"]
@@ -589,16 +592,17 @@ def run_batch(a):
             job_reorder.append(ro)
             n_rays += rays.shape[0]
         scenes.append({"kind": kind, "triangles": int(bvh.info["n_tris"]), "N": bn, "L": bl,
-                       "block": block, "rays": int(d_p.shape[0] + sh.shape[0] + ao.shape[0])})
-        chosen.append(block)
+                       "block": block, "stack": stack,
+                       "rays": int(d_p.shape[0] + sh.shape[0] + ao.shape[0])})
+        chosen.append((block, stack))
         n_tris += int(bvh.info["n_tris"])
     setup_s = time.time() - t_setup
     stream = torch.cuda.current_stream(dev)
     blocks = [b for b in chosen for _ in range(3)]
 
     def sequential():
-        for (scene, rays, k, out), b in zip(jobs_plain, blocks):
-            scene.trace(rays, kind=k, scheme="per_ray", block=b, out=out)
+        for (scene, rays, k, out), (b, st) in zip(jobs_plain, blocks):
+            scene.trace(rays, kind=k, scheme="per_ray", block=b, stack=st, out=out)
 
     # The AO jobs' rays are grouped by direction inside the batched call.
     jobs_batched = [j + (ro,) for j, ro in zip(jobs_plain, job_reorder)]

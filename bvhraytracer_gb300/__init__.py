@@ -195,7 +195,7 @@ class Scene:
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
               policy: int = 0, refill: int = 0, counters: bool = False,
               depth_hist: bool = False, save_distance: bool = False, reorder: int = 0,
-              out=None, stream=None) -> dict:
+              stack: str = "shared", out=None, stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -204,7 +204,8 @@ class Scene:
         (default: torch's current stream). ``save_distance`` (per-ray scheme):
         intersectSaveDistance / intersectImmediately(ray, useDistance=true).
         ``reorder`` = K > 0 traces the rays grouped into 6 K^2 direction bins
-        (results identical, in input order).
+        (results identical, in input order). ``stack`` (per-ray scheme):
+        ``"shared"`` or ``"local"`` memory for the traversal stacks.
         """
         import torch
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
@@ -229,7 +230,7 @@ class Scene:
             res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
             hh = _ptr(res["depth_hist"])
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
-                        int(save_distance), int(reorder))
+                        int(save_distance), int(reorder), int(stack == "local"))
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
                                      C.c_void_p(s.cuda_stream)))

@@ -53,7 +53,7 @@ class TraceOpts(C.Structure):
     _fields_ = [("kind", C.c_int32), ("scheme", C.c_int32), ("profile", C.c_int32),
                 ("workgroup", C.c_int32), ("block", C.c_int32), ("policy", C.c_int32),
                 ("refill", C.c_int32), ("save_distance", C.c_int32),
-                ("reorder", C.c_int32)]
+                ("reorder", C.c_int32), ("stack_local", C.c_int32)]
 
 
 class Batch(C.Structure):

@@ -4,9 +4,10 @@ with the lowest measured time.
 Candidates cover the knobs the reference exposes in config.txt (branching
 factor N and leaf size L: a scene is built per (N, L) pair) plus the GPU
 ones: traversal scheme (per-ray, ray-stream with its workgroup size,
-persistent with its refill threshold and divergence policy), whether the rays
-are grouped by direction first (reorder), node format (FP32 / Q8) and how many
-top levels are staged in shared memory. Every
+persistent with its refill threshold and divergence policy), stack placement
+(shared or local memory), whether the rays are grouped by direction first
+(reorder), node format (FP32 / Q8) and how many top levels are staged in
+shared memory. Every
 candidate gives the same hits (the kernels are bit-exact with one another and
 Q8 keeps hit sets identical), so the choice only changes speed.
 """
@@ -20,6 +21,7 @@ from . import Bvh, Scene
 DEFAULT_OPTIONS = (
     {"scheme": "per_ray", "block": 128},
     {"scheme": "per_ray", "block": 64},
+    {"scheme": "per_ray", "block": 128, "stack": "local"},
     {"scheme": "stream", "workgroup": 8},
     {"scheme": "stream", "workgroup": 16},
     {"scheme": "persistent", "policy": 0, "refill": 8},

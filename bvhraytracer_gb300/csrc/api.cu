@@ -157,6 +157,9 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (o->reorder < 0 || o->reorder > dev::kReorderMaxK)
     return set_error(BVHGPU_ERR_BAD_ARG, "reorder must be 0..32 bins per cube face side");
   c.reorder = o->reorder;
+  if (o->stack_local && o->scheme != BVHGPU_PER_RAY)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack_local needs the per-ray scheme");
+  c.stack_local = o->stack_local != 0;
   return BVHGPU_OK;
 }
 
@@ -1004,7 +1007,7 @@ int bvhgpu_intersect_fastrays(bvhgpu_scene_t s, float* fastrays, uint64_t n, int
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_CLOSEST, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, hits.data(), nullptr, stream);
   if (rc) return rc;
   const uint32_t lm = (uint32_t)s->layout.leaf_memory;
@@ -1032,7 +1035,7 @@ int bvhgpu_intersect_secondary_fastrays(bvhgpu_scene_t s, const float* fastrays,
   } catch (const std::bad_alloc&) {
     return set_error(BVHGPU_ERR_OOM, "host allocation failed");
   }
-  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0};
+  bvhgpu_trace_opts_t o{BVHGPU_ANY, scheme, BVHGPU_PROFILE_FAST, 16, 128, 0, 0, 0, 0, 0};
   int rc = bvhgpu_trace_host(s, rays.data(), n, &o, nullptr, occ.data(), stream);
   if (rc) return rc;
   for (uint64_t i = 0; i < n; ++i) result[i] = (uint16_t)(result[i] + occ[i]);

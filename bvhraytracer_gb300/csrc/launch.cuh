@@ -24,7 +24,10 @@ struct LaunchCfg {
   uint32_t stall_bytes = 0;     // failure-detection tests (see bvhgpu_scene_inject_stall)
   bool save_distance = false;   // per-ray scheme: save-distance traversal (closest hits)
   int reorder = 0;              // > 0: group rays into 6 reorder^2 direction bins first
+  bool stack_local = false;     // per-ray scheme: stacks in local memory (cap <= kLocalStack)
 };
+
+constexpr int kLocalStack = 64;  // entries of the local-memory stack variant
 
 template <typename K>
 inline cudaError_t set_smem(K kernel, size_t bytes) {
@@ -42,9 +45,11 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     // never dropped: save-distance any-hit traversal is the plain one.
     constexpr bool kDist = KIND == BVHGPU_CLOSEST;
     const bool dist = kDist && cfg.save_distance;
-    const size_t smem = (size_t)a.stack_cap * bs * 4 * (dist ? 2 : 1);
+    const bool local = cfg.stack_local && !dist && !COUNT && a.stack_cap <= kLocalStack;
+    const size_t smem = local ? 0 : (size_t)a.stack_cap * bs * 4 * (dist ? 2 : 1);
     auto k = dist ? trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, kDist>
-                  : trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, false>;
+             : local ? trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, false, (COUNT ? 0 : kLocalStack)>
+                     : trace_dfs_kernel<NM, PROFILE, KIND, COUNT, FMT, false>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     const uint64_t grid = (a.n + bs - 1) / bs;

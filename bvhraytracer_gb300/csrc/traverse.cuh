@@ -514,11 +514,15 @@ BVHGPU_DEV void write_result(const SceneDev& sc, const TraceArgs& a, uint64_t ri
 // every entry also carries its box's entry distance (in a second shared
 // array after the stack), the root enters with 0, and a pop whose distance
 // exceeds the current tMax is dropped before it is visited or counted.
-template <int N, int PROFILE, int KIND, bool COUNT, int FMT, bool DIST = false>
+// LSTACK > 0: the stack is a per-thread array of LSTACK entries in local
+// memory (stride 1) instead of shared memory (the stack-placement knob of the
+// autotuner); the caller guarantees a_stack_cap <= LSTACK.
+template <int N, int PROFILE, int KIND, bool COUNT, int FMT, bool DIST = false, int LSTACK = 0>
 __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a) {
   extern __shared__ uint32_t smem[];
-  const int stride = blockDim.x;
-  uint32_t* stack = smem + threadIdx.x;
+  uint32_t lstack[LSTACK > 0 ? LSTACK : 1];
+  const int stride = LSTACK > 0 ? 1 : (int)blockDim.x;
+  uint32_t* stack = LSTACK > 0 ? lstack : smem + threadIdx.x;
   float* dstack = DIST ? reinterpret_cast<float*>(smem + (size_t)a.stack_cap * stride) + threadIdx.x
                        : nullptr;
   unsigned long long* hist = nullptr;

@@ -213,6 +213,9 @@ typedef struct {
                         slot; at most 2^32 - 1 rays per call. Results are identical
                         either way; incoherent rays (ambient occlusion) run faster
                         grouped. */
+  int32_t stack_local; /* per-ray scheme, nonzero: each thread's traversal stack in local
+                        memory (when the tree needs at most 64 entries; else shared
+                        memory, the default placement). Same results. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):

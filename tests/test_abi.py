@@ -47,7 +47,7 @@ def test_status_codes_match_header():
 def test_struct_sizes_match_header_layout():
     assert C.sizeof(N.BuildParams) == 24
     assert C.sizeof(N.SceneParams) == 20
-    assert C.sizeof(N.TraceOpts) == 36
+    assert C.sizeof(N.TraceOpts) == 40
 
 
 def _tri():
@@ -90,7 +90,7 @@ def test_build_rejects_unsorted_splits():
 
 def test_trace_rejects_null_scene_and_options():
     lib = N.lib()
-    o = N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0)
+    o = N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0, 0)
     assert lib.bvhgpu_trace(None, None, 1, C.byref(o), None, None, None, None, None) == N.ERR_BAD_ARG
     assert lib.bvhgpu_trace_host(None, None, 1, C.byref(o), None, None, None) == N.ERR_BAD_ARG
     assert lib.bvhgpu_scene_status(None, None) == N.ERR_BAD_ARG

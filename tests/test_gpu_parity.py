@@ -399,3 +399,22 @@ def test_imported_tree_traces_like_the_built_one():
     c = pkg.Scene(b2).trace(rays, counters=True)
     assert torch.equal(a["hits"].view(torch.int32), c["hits"].view(torch.int32))
     assert torch.equal(a["counters"], c["counters"])
+
+
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+def test_local_memory_stacks(profile):
+    """The stack-placement knob: per-thread stacks in local memory give the
+    same results as shared-memory stacks (closest and any hit)."""
+    tris, b, cv = TS.bvh("clutter120", 8, 8)
+    rays = dev(TS.clutter_rays(tris))
+    scene = pkg.Scene(b)
+    a = scene.trace(rays, profile=profile)["hits"]
+    c = scene.trace(rays, profile=profile, stack="local")["hits"]
+    assert torch.equal(a.view(torch.int32), c.view(torch.int32))
+    prims = pkg.hit_prims(a.cpu().numpy())
+    _, ao = TS.secondary(tris, TS.clutter_rays(tris), prims, LIGHT)
+    d = dev(ao)
+    assert torch.equal(scene.trace(d, kind="any", profile=profile)["occluded"],
+                       scene.trace(d, kind="any", profile=profile, stack="local")["occluded"])
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace(rays, scheme="persistent", stack="local")
