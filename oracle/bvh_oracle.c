@@ -2,8 +2,8 @@
  * CPU oracle for the BVH traversal hot path — TEST INFRASTRUCTURE ONLY.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
- * this file, and only as the checker or the timed CPU baseline; the product
- * (libbvhgpu.so) never links or calls it.
+ * this file, and only to verify the GPU results or as the timed CPU baseline;
+ * the product (libbvhgpu.so) never links or calls it.
  *
  * It restates, in plain C, the reference's (Hengoo/BVHRaytracer) scalar
  * algorithms for the path:

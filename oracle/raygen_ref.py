@@ -1,6 +1,6 @@
 """Ray generation restated in numpy float32 — TEST INFRASTRUCTURE ONLY.
 
-Only tests/ use this module, as the checker of the ray-generation kernels
+Only tests/ use this module, to verify the ray-generation kernels
 (bvhgpu_camera_rays, bvhgpu_secondary_rays, bvhgpu_ao_factor). It restates,
 operation by operation in float32 (no fused multiply-add), the reference's
 arithmetic:
