@@ -64,7 +64,7 @@ def parse():
                    choices=["auto", "per_ray", "stream", "persistent"])
     p.add_argument("--plan", default="",
                    help="fixed per-batch plan instead of the autotuner: three "
-                        "'scheme[,policy,refill,reorder]' specs joined by ';'")
+                        "'scheme[,policy,refill,reorder[,any_order]]' specs joined by ';'")
     p.add_argument("--nodes", default="fp32", choices=["fp32", "q8"])
     p.add_argument("--top-levels", type=int, default=0)
     p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
@@ -92,6 +92,9 @@ def parse():
     p.add_argument("--job-reorder", type=int, default=8,
                    help="batch64: direction bins per cube face side for the AO jobs (0 = off)")
     p.add_argument("--job-refill", type=int, default=24, help="batch64: refill threshold")
+    p.add_argument("--job-any-order", type=int, default=1,
+                   help="batch64: child-index push order for the AO jobs (1) or the "
+                        "reference's order (0)")
     p.add_argument("--tune-nl", action="store_true",
                    help="batch64: let the autotuner pick N/L per scene")
     return p.parse_args()
@@ -296,7 +299,8 @@ def run_ours(a):
     if a.plan:
         # A fixed per-batch plan, e.g. the autotuner's usual choice, so that a
         # profiler run (whose serialisation skews the autotuner's timings)
-        # traces the same launches: "scheme[,policy,refill,reorder]" per batch.
+        # traces the same launches: "scheme[,policy,refill,reorder[,any_order]]"
+        # per batch.
         chosen = []
         for spec in a.plan.split(";"):
             f = spec.split(",")
@@ -305,6 +309,8 @@ def run_ours(a):
                 o.update(policy=int(f[1]), refill=int(f[2]))
             if len(f) > 3 and int(f[3]):
                 o["reorder"] = int(f[3])
+            if len(f) > 4 and int(f[4]):
+                o["any_order"] = True
             chosen.append((plain, o))
         if len(chosen) != 3:
             raise SystemExit("--plan needs three batch specs (primary;shadow;AO)")
@@ -585,11 +591,12 @@ def run_batch(a):
         m, p, n = S.surface(tris, primary, pkg.hit_prims(h.cpu().numpy()))
         sh = torch.from_numpy(S.shadow_rays(p, n, light)).to(dev)
         ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris), seed=i)).to(dev)
-        for rays, k, ro in ((d_p, "closest", 0), (sh, "any", 0), (ao, "any", a.job_reorder)):
+        for rays, k, ro, ao_job in ((d_p, "closest", 0, 0), (sh, "any", 0, 0),
+                                    (ao, "any", a.job_reorder, a.job_any_order)):
             out = (torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
                    if k == "closest" else torch.empty(rays.shape[0], dtype=torch.uint8, device=dev))
             jobs_plain.append((scene, rays, k, out))
-            job_reorder.append(ro)
+            job_reorder.append((ro, ao_job))
             n_rays += rays.shape[0]
         scenes.append({"kind": kind, "triangles": int(bvh.info["n_tris"]), "N": bn, "L": bl,
                        "block": block, "stack": stack,
@@ -605,7 +612,7 @@ def run_batch(a):
             scene.trace(rays, kind=k, scheme="per_ray", block=b, stack=st, out=out)
 
     # The AO jobs' rays are grouped by direction inside the batched call.
-    jobs_batched = [j + (ro,) for j, ro in zip(jobs_plain, job_reorder)]
+    jobs_batched = [j + x for j, x in zip(jobs_plain, job_reorder)]
 
     def batched():
         pkg.trace_jobs(jobs_batched, policy=2, refill=a.job_refill)
@@ -650,7 +657,9 @@ def run_batch(a):
                         f"1k-500k, rays log-uniform 4k-2M (primary:shadow:AO 1:1:4)",
             "triangles_total": n_tris, "rays_per_step": n_rays, "jobs": len(jobs_plain),
             "method": "bvhgpu_trace_jobs (speculative any-hit policy, AO jobs grouped into "
-                      f"6x{a.job_reorder}x{a.job_reorder} direction bins) in a CUDA graph"
+                      f"6x{a.job_reorder}x{a.job_reorder} direction bins"
+                      + (", child-index push order" if a.job_any_order else "")
+                      + ") in a CUDA graph"
                       if a.job_reorder else
                       "bvhgpu_trace_jobs (speculative any-hit policy) in a CUDA graph",
             "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,

@@ -195,7 +195,7 @@ class Scene:
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
               policy: int = 0, refill: int = 0, counters: bool = False,
               depth_hist: bool = False, save_distance: bool = False, reorder: int = 0,
-              stack: str = "shared", out=None, stream=None) -> dict:
+              stack: str = "shared", any_order: bool = False, out=None, stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -206,6 +206,9 @@ class Scene:
         ``reorder`` = K > 0 traces the rays grouped into 6 K^2 direction bins
         (results identical, in input order). ``stack`` (per-ray scheme):
         ``"shared"`` or ``"local"`` memory for the traversal stacks.
+        ``any_order``: any-hit rays without counters push hit children in
+        child-index order in both profiles (same results; faster for short
+        rays such as ambient occlusion).
         """
         import torch
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
@@ -230,7 +233,8 @@ class Scene:
             res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
             hh = _ptr(res["depth_hist"])
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
-                        int(save_distance), int(reorder), int(stack == "local"))
+                        int(save_distance), int(reorder), int(stack == "local"),
+                        int(any_order))
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
                                      C.c_void_p(s.cuda_stream)))
@@ -239,16 +243,18 @@ class Scene:
     def trace_host(self, rays: np.ndarray, *, kind: str = "closest", scheme: str = "per_ray",
                    profile: str = "instrumented", workgroup: int = 16, block: int = 128,
                    policy: int = 0, refill: int = 0, save_distance: bool = False,
-                   reorder: int = 0, out: Optional[np.ndarray] = None,
-                   stream=None) -> np.ndarray:
-        """Host rays in, host results out (copies inside the call)."""
+                   reorder: int = 0, any_order: bool = False, stack: str = "shared",
+                   out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+        """Host rays in, host results out (copies inside the call); options
+        as in :meth:`trace`."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = rays.shape[0]
         k = _KIND[kind]
         if out is None:
             out = (np.empty((n, 4), np.float32) if k == N.CLOSEST else np.empty(n, np.uint8))
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
-                        int(save_distance), int(reorder))
+                        int(save_distance), int(reorder), int(stack == "local"),
+                        int(any_order))
         sp = 0
         if stream is not None:
             sp = stream.cuda_stream
@@ -390,11 +396,13 @@ def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: 
                stream=None) -> None:
     """Traces many (scene, rays) jobs in one persistent launch.
 
-    ``jobs``: list of ``(scene, rays, kind, out)`` or ``(scene, rays, kind,
-    out, reorder)`` with device tensors (rays ``[n, 8]`` float32; ``out``
-    ``[n, 4]`` float32 for ``"closest"``, ``[n]`` uint8 for ``"any"``); up to
-    192 jobs, scenes of any N, L and node format; ``reorder`` = K groups that
-    job's rays into 6 K^2 direction bins first. Per-ray results equal
+    ``jobs``: list of ``(scene, rays, kind, out)``, ``(scene, rays, kind,
+    out, reorder)`` or ``(scene, rays, kind, out, reorder, any_order)`` with
+    device tensors (rays ``[n, 8]`` float32; ``out`` ``[n, 4]`` float32 for
+    ``"closest"``, ``[n]`` uint8 for ``"any"``); up to 192 jobs, scenes of
+    any N, L and node format; ``reorder`` = K groups that job's rays into
+    6 K^2 direction bins first; ``any_order`` as in :meth:`Scene.trace`.
+    Per-ray results equal
     :meth:`Scene.trace`'s. Stream-ordered (default: torch's current stream)
     and graph-capturable; reordered jobs take stream-ordered scratch.
     """
@@ -404,9 +412,11 @@ def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: 
     for i, job in enumerate(jobs):
         scene, rays, kind, out = job[:4]
         reorder = job[4] if len(job) > 4 else 0
+        any_order = int(job[5]) if len(job) > 5 else 0
         k = _KIND[kind]
         arr[i] = N.Job(scene.handle, _ptr(rays), rays.shape[0], k, reorder,
-                       _ptr(out) if k == N.CLOSEST else None, _ptr(out) if k == N.ANY else None)
+                       _ptr(out) if k == N.CLOSEST else None, _ptr(out) if k == N.ANY else None,
+                       any_order, 0)
         dev = rays.device
     o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)
     s = stream if stream is not None else torch.cuda.current_stream(dev)

@@ -53,7 +53,7 @@ class TraceOpts(C.Structure):
     _fields_ = [("kind", C.c_int32), ("scheme", C.c_int32), ("profile", C.c_int32),
                 ("workgroup", C.c_int32), ("block", C.c_int32), ("policy", C.c_int32),
                 ("refill", C.c_int32), ("save_distance", C.c_int32),
-                ("reorder", C.c_int32), ("stack_local", C.c_int32)]
+                ("reorder", C.c_int32), ("stack_local", C.c_int32), ("any_order", C.c_int32)]
 
 
 class Batch(C.Structure):
@@ -64,7 +64,7 @@ class Batch(C.Structure):
 class Job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("n", C.c_uint64),
                 ("kind", C.c_int32), ("reorder", C.c_int32), ("hits", C.c_void_p),
-                ("occluded", C.c_void_p)]
+                ("occluded", C.c_void_p), ("any_order", C.c_int32), ("pad", C.c_int32)]
 
 
 MAX_JOBS = 192

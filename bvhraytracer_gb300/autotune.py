@@ -34,6 +34,9 @@ DEFAULT_OPTIONS = (
     {"scheme": "persistent", "policy": 2, "refill": 16, "reorder": 8},
     {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 8},
     {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10},
+    # any-hit batches only: child-index push order
+    {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10, "any_order": True},
+    {"scheme": "persistent", "policy": 2, "refill": 16, "any_order": True},
 )
 DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
 
@@ -75,6 +78,8 @@ def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFA
         best = None
         for (lay, sc), opts in itertools.product(scenes.items(), options):
             if lay[0] != "fp32" and opts["scheme"] == "stream":
+                continue
+            if opts.get("any_order") and kind != "any":
                 continue
             ms = _time(sc, rays, kind, opts, profile, reps)
             plan.table[(bi, lay, tuple(sorted(opts.items())))] = ms

@@ -160,6 +160,7 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (o->stack_local && o->scheme != BVHGPU_PER_RAY)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stack_local needs the per-ray scheme");
   c.stack_local = o->stack_local != 0;
+  c.any_order = o->any_order != 0;
   return BVHGPU_OK;
 }
 
@@ -169,7 +170,8 @@ constexpr uint32_t kTopStageBytes = 8192;
 
 static int launch(bvhgpu_scene_t s, const dev::TraceArgs& a, dev::LaunchCfg cfg,
                   cudaStream_t st) {
-  const dev::SceneDev sc = s->dev_view();
+  dev::SceneDev sc = s->dev_view();
+  sc.any_index_order = cfg.any_order ? 1 : 0;
   cfg.sm_count = s->sm_count;
   cfg.queue = s->d_queue + (s->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
   cfg.fmt = s->layout.node_format;
@@ -746,6 +748,7 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.fmt = (int8_t)j.scene->layout.node_format;
     d.kind = (int8_t)j.kind;
     d.boxes_ordered = j.scene->layout.boxes_ordered ? 1 : 0;
+    d.any_index_order = j.any_order ? 1 : 0;
     d.perm = nullptr;
     if (j.reorder && j.n > 1) {
       seg_k = j.reorder;
@@ -1145,7 +1148,8 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
   // The heads keep the previous call's values: clear the ones this call uses.
   e = cudaMemsetAsync(heads, 0, sizeof(unsigned long long) * (size_t)n_batches, st);
   if (e != cudaSuccess) return cuda_error(e, "no-alloc trace: clear queue heads");
-  const dev::SceneDev sc = s->dev_view();
+  dev::SceneDev sc = s->dev_view();
+  sc.any_index_order = cfg.any_order ? 1 : 0;
   for (int i = 0; i < n_batches; ++i) {
     const bvhgpu_batch_t& b = batches[i];
     if (b.n == 0) continue;

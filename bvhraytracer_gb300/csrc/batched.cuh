@@ -28,7 +28,8 @@ struct JobDev {
   int8_t fmt;              // node format
   int8_t kind;             // BVHGPU_CLOSEST / BVHGPU_ANY
   int8_t boxes_ordered;    // SceneDev::boxes_ordered of the job's scene
-  int8_t pad[6];
+  int8_t any_index_order;  // SceneDev::any_index_order for the job's rays
+  int8_t pad[5];
   // Reordered job: the job's i-th ray in queue order is ray perm[i], and its
   // result goes to slot perm[i] (null: i).
   const uint32_t* perm;
@@ -123,6 +124,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
           sc.gang = J.gang;
           sc.status = J.status;
           sc.boxes_ordered = J.boxes_ordered;
+          sc.any_index_order = J.any_index_order;
           nm = J.nm;
           fmt = J.fmt;
           kind = J.kind;

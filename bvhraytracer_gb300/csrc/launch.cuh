@@ -25,6 +25,7 @@ struct LaunchCfg {
   bool save_distance = false;   // per-ray scheme: save-distance traversal (closest hits)
   int reorder = 0;              // > 0: group rays into 6 reorder^2 direction bins first
   bool stack_local = false;     // per-ray scheme: stacks in local memory (cap <= kLocalStack)
+  bool any_order = false;       // any-hit rays without counters: child-index push order
 };
 
 constexpr int kLocalStack = 64;  // entries of the local-memory stack variant

@@ -33,6 +33,9 @@ struct SceneDev {
   // FP32 records whose child boxes are all finite with lo <= hi: NaN-free
   // rays may take the near / far slab form (see visit_node).
   int boxes_ordered;
+  // Any-hit rays without counters push hit children in child-index order
+  // (bvhgpu_trace_opts_t.any_order), else in the profile's order.
+  int any_index_order = 0;
 };
 
 #ifndef BVHGPU_NEARFAR
@@ -151,7 +154,7 @@ template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, b
           bool NF = false>
 BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
                            int stride, int& sp, int cap, Counters& ctr, int& depth_out,
-                           float* dstack = nullptr) {
+                           float* dstack = nullptr, bool index_order = false) {
   using F = NodeFmt<N, FMT>;
   constexpr int NM = F::NM;
   const uint4 meta = rec_u4<SH>(rec + F::META);
@@ -256,11 +259,14 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   // ray's direction: ascending positions of the stored sequence when
   // direction[code] <= 0, descending otherwise (compactNode.cpp:781-809).
   // pm holds the positions of the hit children, built from the inverse
-  // sequence over the hit children only.
+  // sequence over the hit children only. With index_order, any-hit rays
+  // without counters take child-index order in both profiles: tMax stays
+  // fixed until the first hit, which ends the ray, so the order in which
+  // the reachable leaves are tested changes no result.
   uint64_t perm;
   uint32_t pm;
   bool descending = false;
-  if (PROFILE == BVHGPU_PROFILE_FAST && KIND == BVHGPU_ANY) {
+  if (KIND == BVHGPU_ANY && (PROFILE == BVHGPU_PROFILE_FAST || (!COUNT && index_order))) {
     perm = 0xFEDCBA9876543210ull;
     pm = hit;
   } else {
@@ -433,20 +439,20 @@ BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_sme
     const uint8_t* rec = top_smem + (size_t)e * REC;
     if (r.exact)
       return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true, DIST>(
-          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
   }
   const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
     return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
   constexpr bool kNF = BVHGPU_NEARFAR && FMT == kFmtFP32 && !DIST;
   if (kNF && sc.boxes_ordered)
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST, kNF>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
   return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST>(
-      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack);
+      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
 }
 
 template <int PROFILE, int KIND, bool COUNT>

@@ -216,6 +216,13 @@ typedef struct {
   int32_t stack_local; /* per-ray scheme, nonzero: each thread's traversal stack in local
                         memory (when the tree needs at most 64 entries; else shared
                         memory, the default placement). Same results. */
+  int32_t any_order; /* 0: any-hit rays push the hit children of a node in the reference's
+                        order (instrumented profile: traverseOrderEachAxis of the ray's
+                        major axis; fast profile: child-index order). Nonzero: any-hit
+                        rays without counters push them in child-index order in both
+                        profiles. Same results (an any-hit ray's result does not depend
+                        on the order in which its leaves are reached); short rays
+                        (ambient occlusion) run faster, long rays toward a light slower. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):
@@ -260,6 +267,8 @@ typedef struct {
                                reordered jobs of a call use the same K */
   bvhgpu_hit_t* hits;       /* closest: device, 16-byte aligned */
   uint8_t* occluded;        /* any: device */
+  int32_t any_order;        /* any: see bvhgpu_trace_opts_t.any_order (per job here) */
+  int32_t pad;              /* 0 */
 } bvhgpu_job_t;
 
 int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_trace_opts_t* opts,

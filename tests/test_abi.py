@@ -47,7 +47,8 @@ def test_status_codes_match_header():
 def test_struct_sizes_match_header_layout():
     assert C.sizeof(N.BuildParams) == 24
     assert C.sizeof(N.SceneParams) == 20
-    assert C.sizeof(N.TraceOpts) == 40
+    assert C.sizeof(N.TraceOpts) == 44
+    assert C.sizeof(N.Job) == 56
 
 
 def _tri():
@@ -90,7 +91,7 @@ def test_build_rejects_unsorted_splits():
 
 def test_trace_rejects_null_scene_and_options():
     lib = N.lib()
-    o = N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0, 0)
+    o = N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0, 0, 0)
     assert lib.bvhgpu_trace(None, None, 1, C.byref(o), None, None, None, None, None) == N.ERR_BAD_ARG
     assert lib.bvhgpu_trace_host(None, None, 1, C.byref(o), None, None, None) == N.ERR_BAD_ARG
     assert lib.bvhgpu_scene_status(None, None) == N.ERR_BAD_ARG
@@ -125,3 +126,37 @@ def test_sah_factor_table():
     assert pkg.sah_factor(3, 2) == pkg.sah_factor(4, 4)
     assert pkg.sah_factor(9, 5) == pkg.sah_factor(12, 8)
     assert pkg.sah_factor(8, 8, gang=8) == 1.0
+
+
+def test_struct_layouts_match_the_c_header(tmp_path):
+    """The ctypes mirrors have the sizes and field offsets the C compiler
+    gives the header's structs."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [("bvhgpu_build_params_t", N.BuildParams), ("bvhgpu_bvh_info_t", N.BvhInfo),
+             ("bvhgpu_scene_params_t", N.SceneParams), ("bvhgpu_trace_opts_t", N.TraceOpts),
+             ("bvhgpu_batch_t", N.Batch), ("bvhgpu_job_t", N.Job),
+             ("bvhgpu_camera_t", N.Camera), ("bvhgpu_secondary_t", N.Secondary)]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "bvhgpu.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parents[1] / "include"
+    subprocess.run([cc, "-std=c11", f"-I{inc}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {}
+    for line in out.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, py in pairs:
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])

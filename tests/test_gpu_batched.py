@@ -146,3 +146,21 @@ def test_reordered_jobs(graph):
         g.replay()
         torch.cuda.synchronize()
         check()
+
+
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+def test_jobs_any_order(profile):
+    """Any-hit jobs with child-index push order (per job) equal the
+    per-scene traces, next to jobs in the reference's order."""
+    items = _scenes()
+    jobs, refs = _jobs(items, profile)
+    jobs = [j + ((8 if i % 3 == 1 else 0), i % 2) for i, j in enumerate(jobs)]
+    for j in jobs:
+        j[3].fill_(3)
+    pkg.trace_jobs(jobs, profile=profile, policy=2, refill=24)
+    torch.cuda.synchronize()
+    for (scene, rays, kind, out, _, _), ref in zip(jobs, refs):
+        if kind == "closest":
+            assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
+        else:
+            assert torch.equal(out, ref)

@@ -379,6 +379,45 @@ def test_reorder_keeps_results_in_input_order(scheme, kw, k):
     scene.status()
 
 
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+@pytest.mark.parametrize("fmt", ["fp32", "q8"])
+def test_any_order_keeps_any_hit_results(profile, fmt):
+    """any_order: any-hit rays without counters push hit children in
+    child-index order in both profiles; occlusion equals the oracle's for
+    every scheme (shadow and AO rays, inactive rays included), and traces
+    with counters keep the reference's order and counts."""
+    tris, b, cv = TS.bvh("clutter120", 8, 4)
+    fv = O.FastView(b.export_fast()) if profile == "fast" else None
+    rays = TS.clutter_rays(tris)[:3000 - 5].copy()
+    scene = pkg.Scene(b, node_format=fmt)
+    prims = pkg.hit_prims(scene.trace(dev(rays), profile=profile)["hits"].cpu().numpy())
+    shadow, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=4)
+    for sec in (shadow, ao):
+        sec = sec.copy()
+        sec[::89, 0] = np.nan
+        if profile == "instrumented":
+            ref = O.trace_instrumented(cv, sec, shadow=True, counters=False)["occluded"]
+        else:
+            ref = O.trace_fast(fv, cv, sec, any_hit=True, counters=False)["occluded"]
+        d = dev(sec)
+        for scheme, kw in (("per_ray", {}), ("per_ray", {"stack": "local"}),
+                           ("stream", {}), ("persistent", {"policy": 0, "refill": 8}),
+                           ("persistent", {"policy": 2, "refill": 24, "reorder": 10})):
+            if fmt == "q8" and scheme == "stream":
+                continue
+            got = scene.trace(d, kind="any", scheme=scheme, profile=profile, any_order=True,
+                              **kw)["occluded"]
+            assert np.array_equal(got.cpu().numpy(), ref), (scheme, kw)
+        c0 = scene.trace(d, kind="any", profile=profile, counters=True)
+        c1 = scene.trace(d, kind="any", profile=profile, counters=True, any_order=True)
+        assert torch.equal(c0["counters"], c1["counters"])
+        assert torch.equal(c0["occluded"], c1["occluded"])
+        host = scene.trace_host(sec, kind="any", profile=profile, scheme="persistent", policy=2,
+                                refill=24, any_order=True)
+        assert np.array_equal(host, ref)
+    scene.status()
+
+
 @pytest.mark.parametrize("n,l", [(4, 4), (8, 8), (12, 4), (16, 16)])
 def test_device_q8_encoding_matches_host(n, l):
     """Q8 scenes encode their node records on the device; the bytes equal the
