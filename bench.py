@@ -64,7 +64,8 @@ def parse():
                    choices=["auto", "per_ray", "stream", "persistent"])
     p.add_argument("--plan", default="",
                    help="fixed per-batch plan instead of the autotuner: three "
-                        "'scheme[,policy,refill,reorder[,any_order]]' specs joined by ';'")
+                        "'scheme[,policy,refill,reorder[,any_order]]' specs joined by ';' "
+                        "(scheme per_ray_local: per-ray with stacks in local memory)")
     p.add_argument("--nodes", default="fp32", choices=["fp32", "q8"])
     p.add_argument("--top-levels", type=int, default=0)
     p.add_argument("--policy", type=int, default=0, help="persistent: 0 while-while, 1 if-if")
@@ -305,6 +306,8 @@ def run_ours(a):
         for spec in a.plan.split(";"):
             f = spec.split(",")
             o = {"scheme": f[0]}
+            if f[0] == "per_ray_local":  # per-ray scheme, stacks in local memory
+                o = {"scheme": "per_ray", "stack": "local"}
             if len(f) > 1:
                 o.update(policy=int(f[1]), refill=int(f[2]))
             if len(f) > 3 and int(f[3]):

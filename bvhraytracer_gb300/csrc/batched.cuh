@@ -68,8 +68,15 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
   }
 }
 
+// Five blocks per SM (up to 102 registers per thread): the kernel carries
+// every node width, format and ray kind, and at six blocks (80 registers)
+// it spills more (batch of 64 scenes: 11.23 ms at six blocks, 10.96 at five,
+// 11.70 at four).
+#ifndef BVHGPU_BATCHED_MIN_BLOCKS
+#define BVHGPU_BATCHED_MIN_BLOCKS 5
+#endif
 template <int PROFILE>
-__global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
     trace_batched_kernel(const __grid_constant__ JobTable t) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int stride = blockDim.x;
