@@ -2,9 +2,10 @@
 // closest hit with respect to the three triangle vertices and the ray origin
 // and direction, through a fixed visibility set.
 //
-// The kernel does not read stored hits: it re-traces each ray (per-ray
-// depth-first, fast profile, so the hit is the forward pass's), then runs the
-// reverse pass of the Moller-Trumbore expressions of triIntersect{L}
+// adjoint_kernel re-traces each ray (per-ray depth-first, fast profile, so
+// the hit is the forward pass's); adjoint_hits_kernel takes the forward
+// pass's stored hits instead. Both then run the reverse pass of the
+// Moller-Trumbore expressions of triIntersect{L}
 // (rayTracerTemplate.ispc:35-76):
 //   e1 = p1 - p0, e2 = p2 - p0, s1 = d x e2, div = s1.e1, inv = 1/div,
 //   s = o - p0, b1 = (s.s1) inv, s2 = s x e1, b2 = (d.s2) inv,
@@ -86,61 +87,26 @@ BVHGPU_DEV df3 cross3(df3 a, df3 b) {
 }
 BVHGPU_DEV float3 to_f3(df3 a) { return make_float3(df_float(a.x), df_float(a.y), df_float(a.z)); }
 
-template <int N>
-__global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a) {
-  extern __shared__ uint32_t smem[];
-  const int stride = blockDim.x;
-  uint32_t* stack = smem + threadIdx.x;
-  const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (rid >= a.n) return;
+// Reverse pass for ray rid whose closest hit is lane `lane` of leaf `leaf`
+// (input triangle `prim`); writes the ray gradients and adds the vertex
+// gradients.
+BVHGPU_DEV void adjoint_reverse(const SceneDev& sc, const AdjointArgs& a, uint64_t rid,
+                                const bvhgpu_ray_t& in, uint32_t leaf, int i, uint32_t prim) {
   float* gr = a.grad_rays + rid * 8;
-  const bvhgpu_ray_t in = load_ray(a.rays, rid);
-  if (isnan(in.ox)) {
-    for (int k = 0; k < 8; ++k) gr[k] = 0.f;
-    return;
-  }
-  // Re-trace: closest hit, fast profile, depth-first.
-  const Ray r = make_ray<BVHGPU_PROFILE_FAST>(in);
-  float tmax = r.tmax;
-  Best best;
-  Counters ctr;
-  int sp = 1;
-  stack[0] = sc.root_entry;
-  bool ok = true;
-  while (sp > 0) {
-    --sp;
-    const uint32_t e = stack[sp * stride];
-    if (e & kLeafBit) {
-      leaf_step<BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false>(sc, e, r, tmax, best, ctr);
-    } else {
-      int depth;
-      if (!node_step<N, BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false, kFmtFP32>(
-              sc, e, nullptr, 0u, r, tmax, stack, stride, sp, a.stack_cap, ctr, depth)) {
-        record_error(sc.status, kDevErrStackOverflow);
-        ok = false;
-        break;
-      }
-    }
-  }
-  if (!ok || best.lane < 0) {
-    for (int k = 0; k < 8; ++k) gr[k] = 0.f;
-    return;
-  }
   // Vertices of the hit triangle from its leaf block (original axes).
-  const float* blk = sc.leaves + (size_t)best.leaf * 9 * sc.leaf_memory;
+  const float* blk = sc.leaves + (size_t)leaf * 9 * sc.leaf_memory;
   // Stride = leaf count rounded up to the gang: recover it from the sentinel.
   int stride_l = sc.leaf_memory;
   {
     const float last = blk[sc.leaf_memory * 9 - 1];
     if (isnan(last)) stride_l = (int)blk[sc.leaf_memory * 9 - 2];
   }
-  const int i = best.lane;
   const float3 p0 = make_float3(blk[0 * stride_l + i], blk[1 * stride_l + i], blk[2 * stride_l + i]);
   const float3 p1 = make_float3(blk[3 * stride_l + i], blk[4 * stride_l + i], blk[5 * stride_l + i]);
   const float3 p2 = make_float3(blk[6 * stride_l + i], blk[7 * stride_l + i], blk[8 * stride_l + i]);
-  const uint32_t prim = __ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + i);
-  const float3 of = make_float3(r.o[0], r.o[1], r.o[2]);
-  const df3 d = d3f(r.d[0], r.d[1], r.d[2]);
+  // The fast profile's ray: origin and direction as given (FastRay).
+  const float3 of = make_float3(in.ox, in.oy, in.oz);
+  const df3 d = d3f(in.dx, in.dy, in.dz);
 
   // Forward intermediates in double-float: the differences of float inputs
   // are exact, so a grazing ray (small s1.e1) loses no bits to cancellation
@@ -204,9 +170,86 @@ __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a
   reinterpret_cast<float4*>(gr)[1] = make_float4(g_dd.x, g_dd.y, g_dd.z, 0.f);
 }
 
+BVHGPU_DEV void zero_ray_grad(const AdjointArgs& a, uint64_t rid) {
+  float4* gr = reinterpret_cast<float4*>(a.grad_rays + rid * 8);
+  gr[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+  gr[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Re-trace, then the reverse pass.
+template <int N>
+__global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a) {
+  extern __shared__ uint32_t smem[];
+  const int stride = blockDim.x;
+  uint32_t* stack = smem + threadIdx.x;
+  const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (rid >= a.n) return;
+  const bvhgpu_ray_t in = load_ray(a.rays, rid);
+  if (isnan(in.ox)) {
+    zero_ray_grad(a, rid);
+    return;
+  }
+  // Re-trace: closest hit, fast profile, depth-first.
+  const Ray r = make_ray<BVHGPU_PROFILE_FAST>(in);
+  float tmax = r.tmax;
+  Best best;
+  Counters ctr;
+  int sp = 1;
+  stack[0] = sc.root_entry;
+  bool ok = true;
+  while (sp > 0) {
+    --sp;
+    const uint32_t e = stack[sp * stride];
+    if (e & kLeafBit) {
+      leaf_step<BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false>(sc, e, r, tmax, best, ctr);
+    } else {
+      int depth;
+      if (!node_step<N, BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false, kFmtFP32>(
+              sc, e, nullptr, 0u, r, tmax, stack, stride, sp, a.stack_cap, ctr, depth)) {
+        record_error(sc.status, kDevErrStackOverflow);
+        ok = false;
+        break;
+      }
+    }
+  }
+  if (!ok || best.lane < 0) {
+    zero_ray_grad(a, rid);
+    return;
+  }
+  const uint32_t prim = __ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + best.lane);
+  adjoint_reverse(sc, a, rid, in, best.leaf, best.lane, prim);
+}
+
+// The reverse pass from stored closest hits (the forward pass's records):
+// no traversal. A hit's prim selects the triangle through the input id ->
+// leaf slot map; misses (prim -1) get zero gradients, unknown ids too (and
+// are recorded as a bad argument).
+__global__ void __launch_bounds__(128) adjoint_hits_kernel(SceneDev sc, AdjointArgs a) {
+  const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (rid >= a.n) return;
+  const bvhgpu_ray_t in = load_ray(a.rays, rid);
+  const uint32_t prim = __float_as_uint(__ldg(a.hits + rid).x);
+  if (isnan(in.ox) || prim == 0xFFFFFFFFu) {
+    zero_ray_grad(a, rid);
+    return;
+  }
+  const uint32_t slot = prim < a.n_prims ? __ldg(a.prim_slot + prim) : 0xFFFFFFFFu;
+  if (slot == 0xFFFFFFFFu) {
+    record_error(sc.status, BVHGPU_ERR_BAD_ARG);
+    zero_ray_grad(a, rid);
+    return;
+  }
+  const uint32_t lm = (uint32_t)sc.leaf_memory;
+  adjoint_reverse(sc, a, rid, in, slot / lm, (int)(slot % lm), prim);
+}
+
 cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const int bs = 128;
+  if (a.hits) {
+    adjoint_hits_kernel<<<(unsigned)((a.n + bs - 1) / bs), bs, 0, s>>>(sc, a);
+    return cudaGetLastError();
+  }
   const size_t smem = (size_t)a.stack_cap * bs * 4;
   const uint64_t grid = (a.n + bs - 1) / bs;
   auto pick = [&](auto k) -> cudaError_t {

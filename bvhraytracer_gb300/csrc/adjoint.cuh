@@ -19,6 +19,10 @@ struct AdjointArgs {
   const int32_t* faces = nullptr;
   float* grad_verts = nullptr;
   uint32_t n_verts = 0;     // vertex ids outside [0, n_verts) are skipped and reported
+  // Stored closest hits (prim, t, u, v) of the forward pass: no re-trace.
+  const float4* hits = nullptr;
+  const uint32_t* prim_slot = nullptr;  // input triangle id -> leaf * leaf_memory + lane
+  uint32_t n_prims = 0;
 };
 
 cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s);

@@ -858,6 +858,47 @@ int bvhgpu_adjoint_vertices(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t
   return BVHGPU_OK;
 }
 
+int bvhgpu_adjoint_hits(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
+                        uint64_t n, const float* grad_hits, const int32_t* faces,
+                        uint64_t n_faces, uint64_t n_verts, float* grad_verts, float* grad_tri9,
+                        float* grad_rays, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  if (n == 0) return BVHGPU_OK;
+  if (!rays || !hits || !grad_hits || !grad_rays || ((uintptr_t)rays & 15) ||
+      ((uintptr_t)hits & 15) || ((uintptr_t)grad_hits & 15) || ((uintptr_t)grad_rays & 15))
+    return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: null or misaligned buffer");
+  if (faces) {
+    if (!grad_verts || grad_tri9 || ((uintptr_t)faces & 3) || ((uintptr_t)grad_verts & 3))
+      return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: faces need grad_verts (and no grad_tri9)");
+    if (n_faces < s->prim_slot.size())
+      return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: fewer faces than input triangles");
+    if (n_verts >= (1ull << 32))
+      return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: 2^32 vertices or more");
+  } else if (!grad_tri9 || grad_verts) {
+    return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: grad_tri9 without faces");
+  }
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  {
+    std::lock_guard<std::mutex> lock(s->staging_mu);
+    if (!s->d_prim_slot) {
+      int rc = upload(&s->d_prim_slot, s->prim_slot);
+      if (rc) return rc;
+    }
+  }
+  dev::AdjointArgs a{rays, n, reinterpret_cast<const float4*>(grad_hits), grad_tri9, grad_rays,
+                     stack_cap(s)};
+  a.faces = faces;
+  a.grad_verts = grad_verts;
+  a.n_verts = (uint32_t)n_verts;
+  a.hits = reinterpret_cast<const float4*>(hits);
+  a.prim_slot = s->d_prim_slot;
+  a.n_prims = (uint32_t)s->prim_slot.size();
+  e = dev::launch_adjoint(s->dev_view(), s->layout.node_stride, a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "adjoint launch");
+  return BVHGPU_OK;
+}
+
 }  // extern "C"
 
 namespace bvhgpu {
@@ -1056,8 +1097,12 @@ int bvhgpu_scene_status(bvhgpu_scene_t s, void* stream) {
   if (code != 0) {
     cudaMemsetAsync(s->d_status, 0, sizeof(int), (cudaStream_t)stream);
     cudaStreamSynchronize((cudaStream_t)stream);
-    return set_error(code, code == BVHGPU_ERR_STACK_OVERFLOW ? "device: traversal stack overflow"
-                                                            : "device: bounded wait timed out");
+    const char* what = code == BVHGPU_ERR_STACK_OVERFLOW ? "device: traversal stack overflow"
+                       : code == BVHGPU_ERR_TIMEOUT     ? "device: bounded wait timed out"
+                       : code == BVHGPU_ERR_BAD_ARG     ? "device: vertex or triangle id out of range"
+                       : code == BVHGPU_ERR_UNSUPPORTED ? "device: node encoding failed"
+                                                        : "device: error";
+    return set_error(code, what);
   }
   return BVHGPU_OK;
 }

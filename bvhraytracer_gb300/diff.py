@@ -5,8 +5,8 @@ The visibility set is fixed: the forward pass finds each ray's closest
 triangle in a BVH built for the current vertex positions, and gradients flow
 through the hit triangle's Moller-Trumbore distance and barycentrics (the
 formulas of the reference's triIntersect{L}, rayTracerTemplate.ispc:35-76),
-not through changes of which triangle is hit. The backward kernel re-traces
-the rays instead of reading stored hits.
+not through changes of which triangle is hit. The backward kernel reads the
+forward pass's stored hits (16 bytes per ray) and runs only the reverse pass.
 """
 from __future__ import annotations
 
@@ -25,14 +25,14 @@ class _RayHit(torch.autograd.Function):
         ctx.scene = scene
         ctx.n_verts = verts.shape[0]
         faces32 = faces.to(torch.int32).contiguous()
-        ctx.save_for_backward(rays, faces32)
+        ctx.save_for_backward(rays, faces32, res)
         prim = res.view(torch.int32)[:, 0].clone()
         ctx.mark_non_differentiable(prim)
         return res[:, 1].clone(), res[:, 2].clone(), res[:, 3].clone(), prim
 
     @staticmethod
     def backward(ctx, gt, gu, gv, _gprim):
-        rays, faces = ctx.saved_tensors
+        rays, faces, hits = ctx.saved_tensors
         n = rays.shape[0]
         dev = rays.device
         z = torch.zeros(n, dtype=torch.float32, device=dev)
@@ -46,10 +46,10 @@ class _RayHit(torch.autograd.Function):
         stream = torch.cuda.current_stream(dev)
         # The kernel adds each hit triangle's vertex gradients straight into
         # grad_verts through the face indices.
-        N.check(N.lib().bvhgpu_adjoint_vertices(
-            ctx.scene.handle, rays.data_ptr(), n, grad_hits.data_ptr(), faces.data_ptr(),
-            faces.shape[0], ctx.n_verts, grad_verts.data_ptr(), grad_rays.data_ptr(),
-            C.c_void_p(stream.cuda_stream)))
+        N.check(N.lib().bvhgpu_adjoint_hits(
+            ctx.scene.handle, rays.data_ptr(), hits.data_ptr(), n, grad_hits.data_ptr(),
+            faces.data_ptr(), faces.shape[0], ctx.n_verts, grad_verts.data_ptr(), None,
+            grad_rays.data_ptr(), C.c_void_p(stream.cuda_stream)))
         return grad_verts, grad_rays, None, None
 
 

@@ -27,8 +27,8 @@
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
  *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
- *   bvhgpu_adjoint[_vertices] no reference counterpart: reverse pass of triIntersect{L}'s
- *                             Moller-Trumbore (rayTracerTemplate.ispc:35-76)
+ *   bvhgpu_adjoint[_vertices|_hits] no reference counterpart: reverse pass of
+ *                             triIntersect{L}'s Moller-Trumbore (rayTracerTemplate.ispc:35-76)
  *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
  *                             structure, fastNodeManager.h:92-156, across scenes)
  *   bvhgpu_camera_rays        Camera::getRayTargetPosition + FastRay (camera.h:82-98)
@@ -313,6 +313,20 @@ int bvhgpu_adjoint_vertices(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint
                             const float* grad_hits, const int32_t* faces, uint64_t n_faces,
                             uint64_t n_verts, float* grad_verts, float* grad_rays,
                             void* stream);
+
+/* The same backward passes from the forward pass's closest hits instead of a
+ * re-trace (no traversal: one thread per ray reads its hit, the triangle and
+ * the ray). hits[i] is bvhgpu_trace's record of ray i (fast profile for the
+ * forward pass's hits to be the ones the gradients describe); its prim selects
+ * the triangle, prim -1 gives zero gradients, an id the scene does not hold
+ * gives zero gradients and is recorded as BVHGPU_ERR_BAD_ARG. With faces, the
+ * vertex gradients go to grad_verts as in bvhgpu_adjoint_vertices (grad_tri9
+ * NULL); without, to grad_tri9 as in bvhgpu_adjoint (grad_verts NULL). Any
+ * node format. The first call uploads the scene's id -> leaf slot map. */
+int bvhgpu_adjoint_hits(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
+                        uint64_t n, const float* grad_hits, const int32_t* faces,
+                        uint64_t n_faces, uint64_t n_verts, float* grad_verts, float* grad_tri9,
+                        float* grad_rays, void* stream);
 
 /* ---- tracing without allocation --------------------------------------- */
 /* No counterpart in the reference (its renderer allocates nothing on a GPU).

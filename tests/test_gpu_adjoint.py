@@ -208,3 +208,71 @@ def test_per_triangle_and_per_vertex_entry_points_agree():
     with pytest.raises(Exception):
         scene.status()
     assert torch.count_nonzero(gv3) == 0
+
+
+def test_adjoint_from_stored_hits_equals_retrace():
+    """bvhgpu_adjoint_hits (the forward pass's hits, no traversal) gives the
+    re-tracing entry points' ray gradients bit for bit and their triangle /
+    vertex gradients up to the order of the atomic sums; misses and inactive
+    rays get zero gradients; a triangle id the scene does not hold is
+    reported and skipped."""
+    import ctypes as C
+    from bvhraytracer_gb300 import _native as N
+    v, f, r, scene, t_tgt, p_tgt = _case(n=32, res=64, seed=3)
+    rays = r.detach().clone()
+    rays[::53, 0] = float("nan")
+    rays[7, 4:7] = torch.tensor([0.0, 1.0, 0.0], device="cuda")  # points away: a miss
+    rays = rays.contiguous()
+    n = rays.shape[0]
+    hits = scene.trace(rays, profile="fast")["hits"]
+    gh = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    gh[:, 1] = torch.linspace(-1, 1, n, device="cuda")
+    gh[:, 2] = 0.3
+    gh[:, 3] = -0.2
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    f32 = f.to(torch.int32).contiguous()
+    tri_a = torch.zeros((f.shape[0], 9), dtype=torch.float32, device="cuda")
+    tri_b = torch.zeros_like(tri_a)
+    gr_a = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    gr_b = torch.full_like(gr_a, 7.0)
+    N.check(N.lib().bvhgpu_adjoint(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
+                                   tri_a.data_ptr(), gr_a.data_ptr(), st))
+    N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
+                                        gh.data_ptr(), None, 0, 0, None, tri_b.data_ptr(),
+                                        gr_b.data_ptr(), st))
+    gv_a = torch.zeros((v.shape[0], 3), dtype=torch.float32, device="cuda")
+    gv_b = torch.zeros_like(gv_a)
+    gr_c = torch.empty_like(gr_a)
+    N.check(N.lib().bvhgpu_adjoint_vertices(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
+                                            f32.data_ptr(), f32.shape[0], v.shape[0],
+                                            gv_a.data_ptr(), gr_c.data_ptr(), st))
+    N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
+                                        gh.data_ptr(), f32.data_ptr(), f32.shape[0],
+                                        v.shape[0], gv_b.data_ptr(), None, gr_b.data_ptr(), st))
+    torch.cuda.synchronize()
+    scene.status()
+    assert torch.equal(gr_a, gr_b) and torch.equal(gr_a, gr_c)
+    assert (tri_a - tri_b).abs().max() <= 1e-5 * tri_a.abs().max()
+    assert (gv_a - gv_b).abs().max() <= 1e-5 * gv_a.abs().max()
+    miss = hits.view(torch.int32)[:, 0] < 0
+    assert bool(miss[7]) and bool(miss[::53].all())
+    assert torch.count_nonzero(gr_b[miss]) == 0
+    # An id the scene does not hold: zero gradients, reported.
+    i = int(torch.nonzero(~miss)[0])
+    bad = hits.clone()
+    bad.view(torch.int32)[i, 0] = f.shape[0] + 100
+    tri_c = torch.zeros_like(tri_a)
+    N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays[i:].data_ptr(), bad[i:].data_ptr(), 1,
+                                        gh[i:].data_ptr(), None, 0, 0, None, tri_c.data_ptr(),
+                                        gr_b[i:].data_ptr(), st))
+    with pytest.raises(Exception):
+        scene.status()
+    assert torch.count_nonzero(tri_c) == 0 and torch.count_nonzero(gr_b[i]) == 0
+    # faces and grad_tri9 together, or neither: rejected on the host
+    assert N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
+                                       gh.data_ptr(), f32.data_ptr(), f32.shape[0], v.shape[0],
+                                       gv_b.data_ptr(), tri_b.data_ptr(), gr_b.data_ptr(),
+                                       st) == N.ERR_BAD_ARG
+    assert N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
+                                       gh.data_ptr(), None, 0, 0, None, None, gr_b.data_ptr(),
+                                       st) == N.ERR_BAD_ARG
