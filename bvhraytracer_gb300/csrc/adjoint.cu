@@ -13,8 +13,9 @@
 // The reverse pass runs in double-float arithmetic (pairs of floats, see
 // below), so the FP32 gradients it returns are the correctly rounded values
 // of a ~48-bit evaluation even for grazing rays, where a float evaluation of
-// s1.e1 cancels. Vertex gradients are accumulated per triangle (9 floats)
-// with atomics; the caller scatters them to shared vertices.
+// s1.e1 cancels. Vertex gradients are summed per triangle within each warp,
+// then added with atomics per triangle (9 floats, scattered to shared
+// vertices by the caller) or per vertex through the face indices.
 #include "adjoint.cuh"
 
 namespace bvhgpu {
@@ -87,11 +88,15 @@ BVHGPU_DEV df3 cross3(df3 a, df3 b) {
 }
 BVHGPU_DEV float3 to_f3(df3 a) { return make_float3(df_float(a.x), df_float(a.y), df_float(a.z)); }
 
-// Reverse pass for ray rid whose closest hit is lane `lane` of leaf `leaf`
-// (input triangle `prim`); writes the ray gradients and adds the vertex
-// gradients.
-BVHGPU_DEV void adjoint_reverse(const SceneDev& sc, const AdjointArgs& a, uint64_t rid,
-                                const bvhgpu_ray_t& in, uint32_t leaf, int i, uint32_t prim) {
+// Gradients of one hit triangle's three vertices (dL/dp0, dL/dp1, dL/dp2).
+struct TriGrad {
+  float v[9];
+};
+
+// Reverse pass for ray rid whose closest hit is lane `i` of leaf `leaf`:
+// writes the ray gradients and returns the vertex gradients.
+BVHGPU_DEV TriGrad adjoint_reverse(const SceneDev& sc, const AdjointArgs& a, uint64_t rid,
+                                   const bvhgpu_ray_t& in, uint32_t leaf, int i) {
   float* gr = a.grad_rays + rid * 8;
   // Vertices of the hit triangle from its leaf block (original axes).
   const float* blk = sc.leaves + (size_t)leaf * 9 * sc.leaf_memory;
@@ -146,28 +151,9 @@ BVHGPU_DEV void adjoint_reverse(const SceneDev& sc, const AdjointArgs& a, uint64
   const float3 g_p0 = to_f3(df3{df_neg(df_add(df_add(g_s.x, g_e1.x), g_e2.x)),
                                 df_neg(df_add(df_add(g_s.y, g_e1.y), g_e2.y)),
                                 df_neg(df_add(df_add(g_s.z, g_e1.z), g_e2.z))});
-  if (a.faces) {
-    const int32_t* fv = a.faces + (size_t)prim * 3;
-    const uint32_t v0 = (uint32_t)__ldg(fv + 0), v1 = (uint32_t)__ldg(fv + 1);
-    const uint32_t v2 = (uint32_t)__ldg(fv + 2);
-    if (v0 >= a.n_verts || v1 >= a.n_verts || v2 >= a.n_verts) {
-      record_error(sc.status, BVHGPU_ERR_BAD_ARG);
-    } else {
-      float* g0 = a.grad_verts + (size_t)v0 * 3;
-      float* g1 = a.grad_verts + (size_t)v1 * 3;
-      float* g2 = a.grad_verts + (size_t)v2 * 3;
-      atomicAdd(g0 + 0, g_p0.x); atomicAdd(g0 + 1, g_p0.y); atomicAdd(g0 + 2, g_p0.z);
-      atomicAdd(g1 + 0, g_p1.x); atomicAdd(g1 + 1, g_p1.y); atomicAdd(g1 + 2, g_p1.z);
-      atomicAdd(g2 + 0, g_p2.x); atomicAdd(g2 + 1, g_p2.y); atomicAdd(g2 + 2, g_p2.z);
-    }
-  } else {
-    float* gt9 = a.grad_tri9 + (size_t)prim * 9;
-    atomicAdd(gt9 + 0, g_p0.x); atomicAdd(gt9 + 1, g_p0.y); atomicAdd(gt9 + 2, g_p0.z);
-    atomicAdd(gt9 + 3, g_p1.x); atomicAdd(gt9 + 4, g_p1.y); atomicAdd(gt9 + 5, g_p1.z);
-    atomicAdd(gt9 + 6, g_p2.x); atomicAdd(gt9 + 7, g_p2.y); atomicAdd(gt9 + 8, g_p2.z);
-  }
   reinterpret_cast<float4*>(gr)[0] = make_float4(g_o.x, g_o.y, g_o.z, 0.f);
   reinterpret_cast<float4*>(gr)[1] = make_float4(g_dd.x, g_dd.y, g_dd.z, 0.f);
+  return TriGrad{{g_p0.x, g_p0.y, g_p0.z, g_p1.x, g_p1.y, g_p1.z, g_p2.x, g_p2.y, g_p2.z}};
 }
 
 BVHGPU_DEV void zero_ray_grad(const AdjointArgs& a, uint64_t rid) {
@@ -176,48 +162,102 @@ BVHGPU_DEV void zero_ray_grad(const AdjointArgs& a, uint64_t rid) {
   gr[1] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// Re-trace, then the reverse pass.
+// Adds the vertex gradients of the warp's hits. Neighbouring rays often hit
+// the same triangle (a large triangle close to the camera takes thousands of
+// rays), so lanes with the same triangle first sum their gradients through
+// shuffles and one lane per triangle issues the atomics: same-address
+// atomics would serialise in L2. Every lane of the warp must call this
+// (valid = false: nothing to add).
+BVHGPU_DEV void scatter_grads(const SceneDev& sc, const AdjointArgs& a, bool valid,
+                              uint32_t prim, TriGrad g) {
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long key = valid ? (unsigned long long)prim : (1ull << 32) | lane;
+  const unsigned peers = __match_any_sync(FULL, key);
+  const int leader = __ffs(peers) - 1;
+  unsigned donors = __ballot_sync(FULL, valid && (int)lane != leader);
+  TriGrad sum = g;
+  while (donors) {
+    const int k = __ffs(donors) - 1;
+    donors &= donors - 1u;
+    const int to = __shfl_sync(FULL, leader, k);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      const float x = __shfl_sync(FULL, g.v[c], k);
+      if ((int)lane == to) sum.v[c] += x;
+    }
+  }
+  if (!valid || (int)lane != leader) return;
+  if (a.faces) {
+    const int32_t* fv = a.faces + (size_t)prim * 3;
+    const uint32_t v0 = (uint32_t)__ldg(fv + 0), v1 = (uint32_t)__ldg(fv + 1);
+    const uint32_t v2 = (uint32_t)__ldg(fv + 2);
+    if (v0 >= a.n_verts || v1 >= a.n_verts || v2 >= a.n_verts) {
+      record_error(sc.status, BVHGPU_ERR_BAD_ARG);
+      return;
+    }
+    const uint32_t vid[3] = {v0, v1, v2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float* gv = a.grad_verts + (size_t)vid[k] * 3;
+      atomicAdd(gv + 0, sum.v[3 * k + 0]);
+      atomicAdd(gv + 1, sum.v[3 * k + 1]);
+      atomicAdd(gv + 2, sum.v[3 * k + 2]);
+    }
+  } else {
+    float* gt9 = a.grad_tri9 + (size_t)prim * 9;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) atomicAdd(gt9 + c, sum.v[c]);
+  }
+}
+
+// Re-trace, then the reverse pass. Lanes past the end or without a hit stay
+// in the warp until the gradient scatter.
 template <int N>
 __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a) {
   extern __shared__ uint32_t smem[];
   const int stride = blockDim.x;
   uint32_t* stack = smem + threadIdx.x;
   const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (rid >= a.n) return;
-  const bvhgpu_ray_t in = load_ray(a.rays, rid);
-  if (isnan(in.ox)) {
-    zero_ray_grad(a, rid);
-    return;
-  }
-  // Re-trace: closest hit, fast profile, depth-first.
-  const Ray r = make_ray<BVHGPU_PROFILE_FAST>(in);
-  float tmax = r.tmax;
-  Best best;
-  Counters ctr;
-  int sp = 1;
-  stack[0] = sc.root_entry;
-  bool ok = true;
-  while (sp > 0) {
-    --sp;
-    const uint32_t e = stack[sp * stride];
-    if (e & kLeafBit) {
-      leaf_step<BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false>(sc, e, r, tmax, best, ctr);
-    } else {
-      int depth;
-      if (!node_step<N, BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false, kFmtFP32>(
-              sc, e, nullptr, 0u, r, tmax, stack, stride, sp, a.stack_cap, ctr, depth)) {
-        record_error(sc.status, kDevErrStackOverflow);
-        ok = false;
-        break;
+  bool valid = false;
+  uint32_t prim = 0;
+  TriGrad g{};
+  if (rid < a.n) {
+    const bvhgpu_ray_t in = load_ray(a.rays, rid);
+    Best best;
+    bool ok = !isnan(in.ox);
+    if (ok) {
+      // Re-trace: closest hit, fast profile, depth-first.
+      const Ray r = make_ray<BVHGPU_PROFILE_FAST>(in);
+      float tmax = r.tmax;
+      Counters ctr;
+      int sp = 1;
+      stack[0] = sc.root_entry;
+      while (sp > 0) {
+        --sp;
+        const uint32_t e = stack[sp * stride];
+        if (e & kLeafBit) {
+          leaf_step<BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false>(sc, e, r, tmax, best, ctr);
+        } else {
+          int depth;
+          if (!node_step<N, BVHGPU_PROFILE_FAST, BVHGPU_CLOSEST, false, kFmtFP32>(
+                  sc, e, nullptr, 0u, r, tmax, stack, stride, sp, a.stack_cap, ctr, depth)) {
+            record_error(sc.status, kDevErrStackOverflow);
+            ok = false;
+            break;
+          }
+        }
       }
     }
+    if (ok && best.lane >= 0) {
+      prim = __ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + best.lane);
+      g = adjoint_reverse(sc, a, rid, in, best.leaf, best.lane);
+      valid = true;
+    } else {
+      zero_ray_grad(a, rid);
+    }
   }
-  if (!ok || best.lane < 0) {
-    zero_ray_grad(a, rid);
-    return;
-  }
-  const uint32_t prim = __ldg(sc.leaf_prim + (size_t)best.leaf * sc.leaf_memory + best.lane);
-  adjoint_reverse(sc, a, rid, in, best.leaf, best.lane, prim);
+  scatter_grads(sc, a, valid, prim, g);
 }
 
 // The reverse pass from stored closest hits (the forward pass's records):
@@ -226,21 +266,26 @@ __global__ void __launch_bounds__(128) adjoint_kernel(SceneDev sc, AdjointArgs a
 // are recorded as a bad argument).
 __global__ void __launch_bounds__(128) adjoint_hits_kernel(SceneDev sc, AdjointArgs a) {
   const uint64_t rid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (rid >= a.n) return;
-  const bvhgpu_ray_t in = load_ray(a.rays, rid);
-  const uint32_t prim = __float_as_uint(__ldg(a.hits + rid).x);
-  if (isnan(in.ox) || prim == 0xFFFFFFFFu) {
-    zero_ray_grad(a, rid);
-    return;
+  bool valid = false;
+  uint32_t prim = 0;
+  TriGrad g{};
+  if (rid < a.n) {
+    const bvhgpu_ray_t in = load_ray(a.rays, rid);
+    prim = __float_as_uint(__ldg(a.hits + rid).x);
+    uint32_t slot = 0xFFFFFFFFu;
+    if (!isnan(in.ox) && prim != 0xFFFFFFFFu) {
+      slot = prim < a.n_prims ? __ldg(a.prim_slot + prim) : 0xFFFFFFFFu;
+      if (slot == 0xFFFFFFFFu) record_error(sc.status, BVHGPU_ERR_BAD_ARG);
+    }
+    if (slot != 0xFFFFFFFFu) {
+      const uint32_t lm = (uint32_t)sc.leaf_memory;
+      g = adjoint_reverse(sc, a, rid, in, slot / lm, (int)(slot % lm));
+      valid = true;
+    } else {
+      zero_ray_grad(a, rid);
+    }
   }
-  const uint32_t slot = prim < a.n_prims ? __ldg(a.prim_slot + prim) : 0xFFFFFFFFu;
-  if (slot == 0xFFFFFFFFu) {
-    record_error(sc.status, BVHGPU_ERR_BAD_ARG);
-    zero_ray_grad(a, rid);
-    return;
-  }
-  const uint32_t lm = (uint32_t)sc.leaf_memory;
-  adjoint_reverse(sc, a, rid, in, slot / lm, (int)(slot % lm), prim);
+  scatter_grads(sc, a, valid, prim, g);
 }
 
 cudaError_t launch_adjoint(const SceneDev& sc, int nm, const AdjointArgs& a, cudaStream_t s) {

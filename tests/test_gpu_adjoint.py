@@ -276,3 +276,58 @@ def test_adjoint_from_stored_hits_equals_retrace():
     assert N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
                                        gh.data_ptr(), None, 0, 0, None, None, gr_b.data_ptr(),
                                        st) == N.ERR_BAD_ARG
+
+
+def test_adjoint_many_rays_on_one_triangle():
+    """4,096 rays on one large triangle (every lane of every warp has the
+    same hit, so the gradients are summed within warps before the atomics):
+    the vertex gradients equal FP64 autograd of Moller-Trumbore."""
+    import ctypes as C
+    from bvhraytracer_gb300 import _native as N
+    verts = np.array([[-3, -3, 0], [5, -3, 0], [-3, 5, 0],
+                      [5, 5, 1], [6, 5, 1], [5, 6, 1]], np.float32)
+    faces = np.array([[0, 1, 2], [3, 4, 5]], np.int64)
+    v = torch.from_numpy(verts).cuda()
+    f = torch.from_numpy(faces).cuda()
+    scene = D.scene_for(v, f, branching=4, leaf_size=4)
+    g = np.linspace(-0.9, 0.9, 64, dtype=np.float32)
+    xs, ys = np.meshgrid(g, g)
+    n = xs.size
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0], rays[:, 1], rays[:, 2] = xs.ravel(), ys.ravel(), 2.0
+    rays[:, 3] = 100.0
+    rays[:, 4] = 0.05 * xs.ravel()
+    rays[:, 5] = -0.03
+    rays[:, 6] = -1.0
+    r = torch.from_numpy(rays).cuda()
+    hits = scene.trace(r, profile="fast")["hits"]
+    assert bool((hits.view(torch.int32)[:, 0] == 0).all())
+    w = torch.linspace(-1, 2, n, device="cuda")
+    gh = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    gh[:, 1] = w
+    gh[:, 2] = 0.25 * w
+    f32 = f.to(torch.int32).contiguous()
+    gv = torch.zeros((6, 3), dtype=torch.float32, device="cuda")
+    gr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, r.data_ptr(), hits.data_ptr(), n,
+                                        gh.data_ptr(), f32.data_ptr(), 2, 6, gv.data_ptr(),
+                                        None, gr.data_ptr(), st))
+    gv2 = torch.zeros_like(gv)
+    N.check(N.lib().bvhgpu_adjoint_vertices(scene.handle, r.data_ptr(), n, gh.data_ptr(),
+                                            f32.data_ptr(), 2, 6, gv2.data_ptr(),
+                                            gr.data_ptr(), st))
+    torch.cuda.synchronize()
+    scene.status()
+    p = torch.from_numpy(verts.astype(np.float64)).requires_grad_(True)
+    rd = torch.from_numpy(rays.astype(np.float64))
+    t, b1, _ = D.moller_trumbore_torch(rd[:, 0:3], rd[:, 4:7], p[0].expand(n, 3),
+                                       p[1].expand(n, 3), p[2].expand(n, 3))
+    wd = w.double().cpu()
+    (gp,) = torch.autograd.grad((t * wd).sum() + (b1 * 0.25 * wd).sum(), (p,))
+    ref = gp.numpy()
+    for got in (gv, gv2):
+        got = got.double().cpu().numpy()
+        # float sums of 4,096 terms (a lost term would be ~2.4e-4 of the total)
+        assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max(), (got, ref)
+        assert np.all(got[3:] == 0)
