@@ -833,7 +833,9 @@ def run_scale(a):
     for name, sc in scenes.items():
         best = None
         for o in ({"scheme": "per_ray"}, {"scheme": "persistent", "policy": 0, "refill": 16},
-                  {"scheme": "persistent", "policy": 2, "refill": 16}):
+                  {"scheme": "persistent", "policy": 2, "refill": 16},
+                  {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10,
+                   "any_order": True}):
             outs = []
             ms = []
             for rays, kind in ((primary, "closest"), (ao, "any")):

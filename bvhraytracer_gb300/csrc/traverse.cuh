@@ -122,13 +122,21 @@ BVHGPU_DEV void load_bytes(const uint8_t* p, uint64_t& lo, uint64_t& hi) {
 // 2^e for a normal exponent e (-126 <= e <= 127).
 BVHGPU_DEV float exp2i(int e) { return __int_as_float((e + 127) << 23); }
 
+// Byte k of w as a float, exactly: the byte placed in the mantissa of
+// 2^23 (one byte permute), minus 2^23. Full-rate ALU and FP32 instructions
+// instead of an integer-to-float conversion.
+template <int K>
+BVHGPU_DEV float byte_to_float(uint32_t w) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | K)) - 8388608.0f;
+}
+
 // Four children's Q8 coordinates of one row: origin + q * step, rounded
 // down (lower bounds) or up (upper bounds). q * step is exact (q < 256,
 // step a power of two), so the decoded box contains the original one.
 BVHGPU_DEV float4 q8_row(uint32_t w, float origin, float step, bool up) {
   float4 v;
-  const float a = (float)(w & 0xFFu) * step, b = (float)((w >> 8) & 0xFFu) * step;
-  const float c = (float)((w >> 16) & 0xFFu) * step, d = (float)(w >> 24) * step;
+  const float a = byte_to_float<0>(w) * step, b = byte_to_float<1>(w) * step;
+  const float c = byte_to_float<2>(w) * step, d = byte_to_float<3>(w) * step;
   if (up) {
     v.x = __fadd_ru(origin, a); v.y = __fadd_ru(origin, b);
     v.z = __fadd_ru(origin, c); v.w = __fadd_ru(origin, d);
