@@ -264,6 +264,38 @@ class Scene:
             C.c_void_p(sp)))
         return out
 
+    def trace_host_batches(self, batches, *, profile: str = "instrumented", stream=None) -> list:
+        """Several host batches in one pipelined call (bvhgpu_trace_host_batches).
+
+        ``batches``: list of ``(rays, kind, out, options)`` with host arrays
+        (``out`` may be None) and ``options`` a dict of :meth:`trace`'s
+        keyword options (scheme, policy, refill, reorder, any_order, stack,
+        block, workgroup). Returns the result arrays, one per batch.
+        """
+        keep, outs = [], []
+        arr = (N.HostBatch * max(1, len(batches)))()
+        for i, (rays, kind, out, opt) in enumerate(batches):
+            rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+            n = rays.shape[0]
+            k = _KIND[kind]
+            if out is None:
+                out = (np.empty((n, 4), np.float32) if k == N.CLOSEST else np.empty(n, np.uint8))
+            opt = dict(opt or {})
+            o = N.TraceOpts(k, _SCHEME[opt.get("scheme", "per_ray")], _PROFILE[profile],
+                            opt.get("workgroup", 16), opt.get("block", 128),
+                            opt.get("policy", 0), opt.get("refill", 0),
+                            int(opt.get("save_distance", False)), int(opt.get("reorder", 0)),
+                            int(opt.get("stack", "shared") == "local"),
+                            int(opt.get("any_order", False)))
+            keep += [rays, o]
+            arr[i] = N.HostBatch(_ptr(rays), n, C.pointer(o),
+                                 _ptr(out) if k == N.CLOSEST else None,
+                                 _ptr(out) if k == N.ANY else None)
+            outs.append(out)
+        sp = stream.cuda_stream if stream is not None else 0
+        N.check(N.lib().bvhgpu_trace_host_batches(self._h, arr, len(batches), C.c_void_p(sp)))
+        return outs
+
     def trace_batches_noalloc(self, batches, *, profile: str = "instrumented", policy: int = 0,
                               refill: int = 0, stream=None) -> None:
         """Traces up to 64 batches with no GPU allocation in the call.

@@ -61,6 +61,11 @@ class Batch(C.Structure):
                 ("hits", C.c_void_p), ("occluded", C.c_void_p)]
 
 
+class HostBatch(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("n", C.c_uint64), ("opts", C.POINTER(TraceOpts)),
+                ("hits", C.c_void_p), ("occluded", C.c_void_p)]
+
+
 class Job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("n", C.c_uint64),
                 ("kind", C.c_int32), ("reorder", C.c_int32), ("hits", C.c_void_p),
@@ -121,6 +126,7 @@ _SIGS = {
     "bvhgpu_adjoint_hits": (C.c_int, [_P, _P, _P, C.c_uint64, _P, _P, C.c_uint64, C.c_uint64,
                                       _P, _P, _P, _P]),
     "bvhgpu_trace_jobs": (C.c_int, [C.POINTER(Job), C.c_int32, C.POINTER(TraceOpts), _P]),
+    "bvhgpu_trace_host_batches": (C.c_int, [_P, C.POINTER(HostBatch), C.c_int32, _P]),
     "bvhgpu_intersect_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P, _P]),
     "bvhgpu_intersect_secondary_fastrays": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P]),
     "bvhgpu_trace_batches_noalloc": (C.c_int, [_P, C.POINTER(Batch), C.c_int32,

@@ -584,24 +584,27 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   return launch_reordered(s, a, cfg, (cudaStream_t)stream);
 }
 
-int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
-                      const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
-                      void* stream) {
-  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+}  // extern "C"
+
+namespace {
+// One batch of a host-buffer trace: host rays in, host results out.
+struct HostBatch {
+  const bvhgpu_ray_t* rays;
+  uint64_t n;
   dev::LaunchCfg cfg;
-  int rc = check_opts(opts, cfg);
-  if (rc) return rc;
-  if (n == 0) return BVHGPU_OK;
-  if (!rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
-  const bool closest = cfg.kind == BVHGPU_CLOSEST;
-  if (closest ? !hits : !occluded) return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
-  cudaStream_t st = (cudaStream_t)stream;
+  bvhgpu_hit_t* hits;
+  uint8_t* occluded;
+};
+}  // namespace
+
+// Pipeline of host-buffer traces: the rays of every batch go in chunks over
+// two internal streams, so the copy of one chunk in, the trace of another and
+// the copy of a third out run at the same time, across batch boundaries too.
+// Both streams wait for `st` first; `st` waits for both at the end, and the
+// call returns with the results on the host.
+static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cudaStream_t st) {
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  // Pipeline: the rays go in chunks over two internal streams, so the copy
-  // of one chunk in, the trace of another and the copy of a third out run at
-  // the same time. Both streams wait for `stream` first; `stream` waits for
-  // both at the end, and the call returns with the results on the host.
   std::lock_guard<std::mutex> lock(s->staging_mu);
   constexpr int NS = bvhgpu_scene::kHostStreams;
   for (int i = 0; i < NS; ++i) {
@@ -616,16 +619,22 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
       if (e != cudaSuccess) return cuda_error(e, "create pipeline event");
     }
   }
-  // Chunks of an eighth of the batch, between 256 Ki and 2 Mi rays: small
+  // Chunks of an eighth of each batch, between 256 Ki and 2 Mi rays: small
   // enough that the first copy in and the last copy out (the parts that do
   // not overlap a trace) are short, large enough to fill the GPU.
-  uint64_t chunk = (n + 7) / 8;
-  chunk = std::max<uint64_t>(chunk, 256ull << 10);
-  chunk = std::min<uint64_t>(chunk, 2ull << 20);
-  chunk = std::min<uint64_t>(chunk, n);
-  const size_t out_rec = closest ? sizeof(bvhgpu_hit_t) : 1;
-  const size_t ray_bytes = align256(chunk * sizeof(bvhgpu_ray_t));
-  const size_t per_stream = ray_bytes + align256(chunk * out_rec);
+  std::vector<uint64_t> chunk(nb);
+  uint64_t max_chunk = 0;
+  for (int k = 0; k < nb; ++k) {
+    uint64_t c = (b[k].n + 7) / 8;
+    c = std::max<uint64_t>(c, 256ull << 10);
+    c = std::min<uint64_t>(c, 2ull << 20);
+    c = std::min<uint64_t>(c, b[k].n);
+    chunk[k] = c;
+    max_chunk = std::max(max_chunk, c);
+  }
+  if (max_chunk == 0) return BVHGPU_OK;
+  const size_t ray_bytes = align256(max_chunk * sizeof(bvhgpu_ray_t));
+  const size_t per_stream = ray_bytes + align256(max_chunk * sizeof(bvhgpu_hit_t));
   const size_t need = per_stream * NS;
   if (need > s->stage_bytes) {
     cudaStreamSynchronize(st);
@@ -643,34 +652,39 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
     e = cudaStreamWaitEvent(s->host_stream[i], s->host_event[NS], 0);
     if (e != cudaSuccess) return cuda_error(e, "pipeline wait");
   }
-  rc = BVHGPU_OK;
-  uint64_t k = 0;
-  for (uint64_t first = 0; first < n && rc == BVHGPU_OK; first += chunk, ++k) {
-    const uint64_t m = std::min<uint64_t>(chunk, n - first);
-    const int si = (int)(k % NS);
-    cudaStream_t cs = s->host_stream[si];
-    uint8_t* base = static_cast<uint8_t*>(s->d_stage) + per_stream * si;
-    auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(base);
-    uint8_t* d_out = base + ray_bytes;
-    e = cudaMemcpyAsync(d_rays, rays + first, m * sizeof(bvhgpu_ray_t), cudaMemcpyHostToDevice,
-                        cs);
-    if (e != cudaSuccess) {
-      rc = cuda_error(e, "copy rays in");
-      break;
+  int rc = BVHGPU_OK;
+  uint64_t k = 0;  // chunk counter over all batches: picks the stream
+  for (int bi = 0; bi < nb && rc == BVHGPU_OK; ++bi) {
+    const HostBatch& B = b[bi];
+    const bool closest = B.cfg.kind == BVHGPU_CLOSEST;
+    const size_t out_rec = closest ? sizeof(bvhgpu_hit_t) : 1;
+    for (uint64_t first = 0; first < B.n && rc == BVHGPU_OK; first += chunk[bi], ++k) {
+      const uint64_t m = std::min<uint64_t>(chunk[bi], B.n - first);
+      const int si = (int)(k % NS);
+      cudaStream_t cs = s->host_stream[si];
+      uint8_t* base = static_cast<uint8_t*>(s->d_stage) + per_stream * si;
+      auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(base);
+      uint8_t* d_out = base + ray_bytes;
+      e = cudaMemcpyAsync(d_rays, B.rays + first, m * sizeof(bvhgpu_ray_t),
+                          cudaMemcpyHostToDevice, cs);
+      if (e != cudaSuccess) {
+        rc = cuda_error(e, "copy rays in");
+        break;
+      }
+      dev::TraceArgs a;
+      a.rays = d_rays;
+      a.n = m;
+      a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
+      a.occluded = closest ? nullptr : d_out;
+      a.counters = nullptr;
+      a.depth_hist = nullptr;
+      a.stack_cap = stack_cap(s);
+      rc = launch_reordered(s, a, B.cfg, cs);
+      if (rc) break;
+      void* dst = closest ? (void*)(B.hits + first) : (void*)(B.occluded + first);
+      e = cudaMemcpyAsync(dst, d_out, m * out_rec, cudaMemcpyDeviceToHost, cs);
+      if (e != cudaSuccess) rc = cuda_error(e, "copy results out");
     }
-    dev::TraceArgs a;
-    a.rays = d_rays;
-    a.n = m;
-    a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
-    a.occluded = closest ? nullptr : d_out;
-    a.counters = nullptr;
-    a.depth_hist = nullptr;
-    a.stack_cap = stack_cap(s);
-    rc = launch_reordered(s, a, cfg, cs);
-    if (rc) break;
-    void* dst = closest ? (void*)(hits + first) : (void*)(occluded + first);
-    e = cudaMemcpyAsync(dst, d_out, m * out_rec, cudaMemcpyDeviceToHost, cs);
-    if (e != cudaSuccess) rc = cuda_error(e, "copy results out");
   }
   for (int i = 0; i < NS; ++i) {
     cudaEventRecord(s->host_event[i], s->host_stream[i]);
@@ -680,6 +694,44 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_error(e, "synchronise");
   return BVHGPU_OK;
+}
+
+extern "C" {
+
+int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
+                      const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                      void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  HostBatch b{rays, n, {}, hits, occluded};
+  int rc = check_opts(opts, b.cfg);
+  if (rc) return rc;
+  if (n == 0) return BVHGPU_OK;
+  if (!rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
+  if (b.cfg.kind == BVHGPU_CLOSEST ? !hits : !occluded)
+    return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
+  return trace_host_pipeline(s, &b, 1, (cudaStream_t)stream);
+}
+
+int bvhgpu_trace_host_batches(bvhgpu_scene_t s, const bvhgpu_host_batch_t* batches,
+                              int32_t n_batches, void* stream) {
+  if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
+  if (n_batches < 0 || (n_batches > 0 && !batches))
+    return set_error(BVHGPU_ERR_BAD_ARG, "batches: null");
+  std::vector<HostBatch> b;
+  b.reserve((size_t)n_batches);
+  for (int i = 0; i < n_batches; ++i) {
+    const bvhgpu_host_batch_t& x = batches[i];
+    HostBatch h{x.rays, x.n, {}, x.hits, x.occluded};
+    int rc = check_opts(x.opts, h.cfg);
+    if (rc) return rc;
+    if (x.n == 0) continue;
+    if (!x.rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
+    if (h.cfg.kind == BVHGPU_CLOSEST ? !x.hits : !x.occluded)
+      return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
+    b.push_back(h);
+  }
+  if (b.empty()) return BVHGPU_OK;
+  return trace_host_pipeline(s, b.data(), (int)b.size(), (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -26,7 +26,7 @@
  *                             (fastNodeManager.h:1328-1493, 835-1230) and the
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
- *   bvhgpu_trace_host         the same, on host buffers (copies in the call)
+ *   bvhgpu_trace_host[_batches] the same, on host buffers (copies in the call)
  *   bvhgpu_adjoint[_vertices|_hits] no reference counterpart: reverse pass of
  *                             triIntersect{L}'s Moller-Trumbore (rayTracerTemplate.ispc:35-76)
  *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
@@ -243,6 +243,22 @@ int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
 int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                       const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                       void* stream);
+
+/* Several host-buffer batches of one scene (a frame's primary, shadow and
+ * ambient-occlusion rays), each with its own options, in one call: the
+ * chunked copies in, traces and copies out of all batches form one pipeline,
+ * so a batch's first copy overlaps the previous batch's last trace. Results
+ * equal bvhgpu_trace_host's per batch; synchronises `stream` once. */
+typedef struct {
+  const bvhgpu_ray_t* rays;         /* host */
+  uint64_t n;
+  const bvhgpu_trace_opts_t* opts;  /* kind, scheme, ... of this batch */
+  bvhgpu_hit_t* hits;               /* host, closest */
+  uint8_t* occluded;                /* host, any */
+} bvhgpu_host_batch_t;
+
+int bvhgpu_trace_host_batches(bvhgpu_scene_t scene, const bvhgpu_host_batch_t* batches,
+                              int32_t n_batches, void* stream);
 
 /* ---- many scenes in one launch ---------------------------------------- */
 /* A job: one ray batch traced in one scene. bvhgpu_trace_jobs traces up to

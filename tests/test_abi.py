@@ -139,6 +139,7 @@ def test_struct_layouts_match_the_c_header(tmp_path):
     pairs = [("bvhgpu_build_params_t", N.BuildParams), ("bvhgpu_bvh_info_t", N.BvhInfo),
              ("bvhgpu_scene_params_t", N.SceneParams), ("bvhgpu_trace_opts_t", N.TraceOpts),
              ("bvhgpu_batch_t", N.Batch), ("bvhgpu_job_t", N.Job),
+             ("bvhgpu_host_batch_t", N.HostBatch),
              ("bvhgpu_camera_t", N.Camera), ("bvhgpu_secondary_t", N.Secondary)]
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "bvhgpu.h"', "int main(void) {"]
     for cname, py in pairs:

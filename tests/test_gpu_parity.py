@@ -195,6 +195,33 @@ def test_host_entry_point_matches_device(terrain):
     assert np.array_equal(occ, O.trace_instrumented(cv, sh, shadow=True)["occluded"])
 
 
+def test_host_batches_in_one_pipeline(terrain):
+    """bvhgpu_trace_host_batches: primary, shadow and AO batches with their
+    own options in one pipelined call (ragged sizes, an empty batch, more
+    than one chunk for the largest) equal the oracle."""
+    tris, b, cv, rays, scene = terrain
+    ref = O.trace_instrumented(cv, rays, shadow=False)
+    prims = pkg.hit_prims(ref["hits"])
+    sh, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=8)
+    big = np.concatenate([ao] * 24)  # > 256 Ki rays: several chunks
+    outs = scene.trace_host_batches([
+        (rays[:-3], "closest", None, {"scheme": "per_ray", "stack": "local"}),
+        (sh, "any", None, {"scheme": "persistent", "policy": 2, "refill": 16}),
+        (rays[:0], "closest", None, {}),
+        (big, "any", None, {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10,
+                            "any_order": True}),
+        (ao, "any", None, {"scheme": "stream"})])
+    assert np.array_equal(bits(outs[0]), bits(ref["hits"][:-3]))
+    occ_sh = O.trace_instrumented(cv, sh, shadow=True)["occluded"]
+    occ_ao = O.trace_instrumented(cv, ao, shadow=True)["occluded"]
+    assert np.array_equal(outs[1], occ_sh)
+    assert outs[2].shape == (0, 4)
+    assert np.array_equal(outs[3], np.concatenate([occ_ao] * 24))
+    assert np.array_equal(outs[4], occ_ao)
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace_host_batches([(sh, "any", None, {"reorder": 40})])
+
+
 def test_wrappers_mirror_reference_names(terrain):
     tris, b, cv, rays, scene = terrain
     fm = pkg.FastNodeManager(b)
