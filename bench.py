@@ -978,8 +978,9 @@ def run_terrain(a):
 
 def run_sweep(a):
     """The 1M-triangle clutter frame for every N, L in {4, 8, 12, 16}^2:
-    plain per-ray against ray-stream traversal (and the persistent kernel),
-    Mrays/s of the whole frame (primary + shadow + 8 AO per hit)."""
+    plain per-ray against ray-stream traversal, the persistent kernel and the
+    default bench's per-batch plan, Mrays/s of the whole frame (primary +
+    shadow + 8 AO per hit)."""
     import torch
     import bvhraytracer_gb300 as pkg
     dev = torch.device("cuda", 0)
@@ -999,14 +1000,22 @@ def run_sweep(a):
             sc = pkg.Scene(bvh)
             row = {}
             ref = None
+            # "this_method": the default bench's usual plan per batch (primary
+            # per-ray; shadow persistent policy 2; AO persistent policy 2,
+            # refill 24, direction bins K = 10, child-index push order).
+            plan = [{"scheme": "per_ray"}, {"scheme": "persistent", "policy": 2, "refill": 16},
+                    {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10,
+                     "any_order": True}]
             for name, o in (("per_ray", {"scheme": "per_ray"}),
                             ("stream_wg16", {"scheme": "stream"}),
-                            ("persistent", {"scheme": "persistent", "policy": 2, "refill": 16})):
+                            ("persistent", {"scheme": "persistent", "policy": 2, "refill": 16}),
+                            ("this_method", plan)):
                 ms = 0.0
                 outs = []
                 try:
-                    for r, k in batches:
-                        t, out = _time_trace(sc, r, k, o, max(1, a.steps // 2), stream)
+                    for bi, (r, k) in enumerate(batches):
+                        ob = o[bi] if isinstance(o, list) else o
+                        t, out = _time_trace(sc, r, k, ob, max(1, a.steps // 2), stream)
                         ms += t
                         outs.append(out["hits" if k == "closest" else "occluded"].view(torch.uint8))
                 except pkg.BvhgpuError as e:
@@ -1020,10 +1029,10 @@ def run_sweep(a):
             sc.status()
             table[f"N{n}L{l}"] = row
             del sc, bvh
-    best = max(table, key=lambda k: table[k]["persistent"]["mrays_per_s"])
+    best = max(table, key=lambda k: table[k]["this_method"]["mrays_per_s"])
     line = {
-        "metric": METRIC, "value": table[best]["persistent"]["mrays_per_s"], "unit": METRIC,
-        "n_gpus": 1, "steps": a.steps, "warmup": 1, "ms_per_step": table[best]["persistent"]["ms"],
+        "metric": METRIC, "value": table[best]["this_method"]["mrays_per_s"], "unit": METRIC,
+        "n_gpus": 1, "steps": a.steps, "warmup": 1, "ms_per_step": table[best]["this_method"]["ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded clutter scene standing in for the reference's glTF scenes)",
         "config": {"workload": workload_name(a).replace(f"N{a.branching}L{a.leaf}", "N,L sweep"),
