@@ -455,6 +455,55 @@ def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: 
     N.check(N.lib().bvhgpu_trace_jobs(arr, len(jobs), C.byref(o), C.c_void_p(s.cuda_stream)))
 
 
+# ---- the reference's ISPC kernels, batched (rayTracerTemplate.ispc) -------
+
+def gang_size() -> int:
+    """getGangSize: the fast profile's default gang (4)."""
+    return int(N.lib().bvhgpu_gang_size())
+
+
+def _stream_ptr(t, stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream(t.device)
+    return C.c_void_p(s.cuda_stream)
+
+
+def aabb_intersect(n: int, bounds, offsets, fastrays, distances, stream=None):
+    """aabbIntersect{n} for every (offset, FastRay) pair, on device tensors:
+    ``bounds`` float32 (node bounds rows of width n), ``offsets`` int32
+    ``[count]`` float offsets, ``fastrays`` ``[count, 10]`` float32;
+    writes t0 into ``distances`` ``[count, n]`` at hit lanes and returns the
+    per-call any-hit flags (uint8)."""
+    import torch
+    count = offsets.shape[0]
+    res = torch.empty(count, dtype=torch.uint8, device=offsets.device)
+    N.check(N.lib().bvhgpu_aabb_intersect(n, _ptr(bounds), _ptr(offsets), _ptr(fastrays),
+                                          _ptr(distances), _ptr(res), count,
+                                          _stream_ptr(offsets, stream)))
+    return res
+
+
+def tri_intersect(l: int, gang: int, tri, tri_ids, fastrays, stream=None):
+    """triIntersect{l} for every (leaf offset, FastRay) pair: returns the
+    in-leaf index or -1 (int32) and lowers tMax of ``fastrays`` in place."""
+    import torch
+    count = tri_ids.shape[0]
+    res = torch.empty(count, dtype=torch.int32, device=tri_ids.device)
+    N.check(N.lib().bvhgpu_tri_intersect(l, gang, _ptr(tri), _ptr(tri_ids), _ptr(fastrays),
+                                         _ptr(res), count, _stream_ptr(tri_ids, stream)))
+    return res
+
+
+def tri_any_hit(l: int, tri, tri_ids, fastrays, stream=None):
+    """triAnyHit{l} for every (leaf offset, FastRay) pair (uint8)."""
+    import torch
+    count = tri_ids.shape[0]
+    res = torch.empty(count, dtype=torch.uint8, device=tri_ids.device)
+    N.check(N.lib().bvhgpu_tri_any_hit(l, _ptr(tri), _ptr(tri_ids), _ptr(fastrays), _ptr(res),
+                                       count, _stream_ptr(tri_ids, stream)))
+    return res
+
+
 def hit_prims(hits) -> "np.ndarray":
     """Primitive ids (int32) of a ``[n, 4]`` hit record tensor or array."""
     if isinstance(hits, np.ndarray):

@@ -739,8 +739,62 @@ int bvhgpu_trace_host_batches(bvhgpu_scene_t s, const bvhgpu_host_batch_t* batch
 namespace bvhgpu {
 namespace dev {
 cudaError_t launch_batched(const JobTable& t, int profile, int sm_count, cudaStream_t s);
+cudaError_t launch_aabb_calls(int n, const float* bounds, const uint32_t* offset,
+                              const float* fastrays, float* distances, uint8_t* result,
+                              uint64_t count, cudaStream_t s);
+cudaError_t launch_tri_calls(int l, int gang, const float* tri, const uint32_t* tri_id,
+                             float* fastrays, int32_t* result, uint64_t count, cudaStream_t s);
+cudaError_t launch_any_calls(int l, const float* tri, const uint32_t* tri_id,
+                             const float* fastrays, uint8_t* result, uint64_t count,
+                             cudaStream_t s);
 }  // namespace dev
 }  // namespace bvhgpu
+
+static bool ispc_width(int32_t w) { return w == 4 || w == 8 || w == 12 || w == 16; }
+
+extern "C" {
+
+int bvhgpu_gang_size(void) { return 4; }
+
+int bvhgpu_aabb_intersect(int32_t n, const float* bounds, const uint32_t* offset,
+                          const float* fastrays, float* distances, uint8_t* result,
+                          uint64_t count, void* stream) {
+  if (!ispc_width(n)) return set_error(BVHGPU_ERR_BAD_ARG, "aabbIntersect: n must be 4, 8, 12 or 16");
+  if (count == 0) return BVHGPU_OK;
+  if (!bounds || !offset || !fastrays || !distances || !result)
+    return set_error(BVHGPU_ERR_BAD_ARG, "aabbIntersect: null buffer");
+  cudaError_t e = dev::launch_aabb_calls(n, bounds, offset, fastrays, distances, result, count,
+                                         (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "aabbIntersect launch");
+  return BVHGPU_OK;
+}
+
+int bvhgpu_tri_intersect(int32_t l, int32_t gang, const float* tri, const uint32_t* tri_id,
+                         float* fastrays, int32_t* result, uint64_t count, void* stream) {
+  if (!ispc_width(l)) return set_error(BVHGPU_ERR_BAD_ARG, "triIntersect: l must be 4, 8, 12 or 16");
+  if (gang != 4 && gang != 8) return set_error(BVHGPU_ERR_BAD_ARG, "triIntersect: gang 4 or 8");
+  if (count == 0) return BVHGPU_OK;
+  if (!tri || !tri_id || !fastrays || !result)
+    return set_error(BVHGPU_ERR_BAD_ARG, "triIntersect: null buffer");
+  cudaError_t e = dev::launch_tri_calls(l, gang, tri, tri_id, fastrays, result, count,
+                                        (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "triIntersect launch");
+  return BVHGPU_OK;
+}
+
+int bvhgpu_tri_any_hit(int32_t l, const float* tri, const uint32_t* tri_id,
+                       const float* fastrays, uint8_t* result, uint64_t count, void* stream) {
+  if (!ispc_width(l)) return set_error(BVHGPU_ERR_BAD_ARG, "triAnyHit: l must be 4, 8, 12 or 16");
+  if (count == 0) return BVHGPU_OK;
+  if (!tri || !tri_id || !fastrays || !result)
+    return set_error(BVHGPU_ERR_BAD_ARG, "triAnyHit: null buffer");
+  cudaError_t e = dev::launch_any_calls(l, tri, tri_id, fastrays, result, count,
+                                        (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "triAnyHit launch");
+  return BVHGPU_OK;
+}
+
+}  // extern "C"
 
 extern "C" {
 

@@ -36,6 +36,9 @@
  *                             (fastNodeManager.h:1700-1713, cameraFast.h:366-381, 513-552,
  *                             camera.cpp:21-52)
  *   bvhgpu_ao_factor          the AO term of cameraData.h:403-406
+ *   bvhgpu_gang_size / bvhgpu_aabb_intersect / bvhgpu_tri_intersect / bvhgpu_tri_any_hit
+ *                             getGangSize / aabbIntersect{N} / triIntersect{L} / triAnyHit{L},
+ *                             the ISPC C ABI (src/ISPC/rayTracerTemplate.ispc:3-233), batched
  *   bvhgpu_intersect_fastrays FastNodeManager::intersectWideAlternative on FastRay
  *                             records (fastNodeManager.h:835-1049; FastRay: src/fastRay.h:14-29)
  *   bvhgpu_intersect_secondary_fastrays
@@ -289,6 +292,44 @@ typedef struct {
 
 int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_trace_opts_t* opts,
                       void* stream);
+
+/* ---- the reference's ISPC kernels, batched ----------------------------- */
+/* The extern "C" functions the ISPC compiler generates from
+ * src/ISPC/rayTracerTemplate.ispc and fastNodeManager.h binds
+ * (fastNodeManager.h:247-257), as batches of independent calls, one GPU
+ * thread per call: where the reference calls aabbIntersect{N}(bounds,
+ * distances, rayInfo) once per node visit, bvhgpu_aabb_intersect takes count
+ * such calls. Device pointers; stream-ordered. `fastrays` are the reference's
+ * FastRay records (10 floats: tMax, pos[3], invDirection[3], direction[3];
+ * src/fastRay.h:14-29) used as given; rows of the node bounds and leaf blocks
+ * are `width` floats long (padding 1), as in the FastNode / trianglePoints
+ * arrays of bvhgpu_bvh_export_fast. */
+
+/* getGangSize (rayTracerTemplate.ispc:3-6): the gang the fast profile uses
+ * by default (4, the SSE4 build's programCount; scenes may use 8). */
+int bvhgpu_gang_size(void);
+
+/* aabbIntersect{N} (rayTracerTemplate.ispc:171-233), N = n in {4, 8, 12, 16}:
+ * call i slab-tests fastrays[i] against the n boxes of bounds + offset[i]
+ * (rows min x, min y, min z, max x, max y, max z); writes distances[i * n +
+ * lane] = t0 for every hit lane (the other entries are left as they are) and
+ * result[i] = 1 if any lane is hit. */
+int bvhgpu_aabb_intersect(int32_t n, const float* bounds, const uint32_t* offset,
+                          const float* fastrays, float* distances, uint8_t* result,
+                          uint64_t count, void* stream);
+
+/* triIntersect{L} (rayTracerTemplate.ispc:28-108), L = l in {4, 8, 12, 16}:
+ * call i tests fastrays[i] against the l triangles of the leaf block at
+ * tri + tri_id[i] (tri_id: the primIdBegin float offset) with the gang-lane
+ * tie rule of a `gang`-wide ISPC gang (4 or 8); result[i] = the in-leaf index
+ * of the hit or -1, and a hit lowers fastrays[i * 10] (tMax) to its t. */
+int bvhgpu_tri_intersect(int32_t l, int32_t gang, const float* tri, const uint32_t* tri_id,
+                         float* fastrays, int32_t* result, uint64_t count, void* stream);
+
+/* triAnyHit{L} (rayTracerTemplate.ispc:112-168): result[i] = 1 if any of the
+ * l triangles at tri + tri_id[i] is hit within tMax. */
+int bvhgpu_tri_any_hit(int32_t l, const float* tri, const uint32_t* tri_id,
+                       const float* fastrays, uint8_t* result, uint64_t count, void* stream);
 
 /* ---- FastRay drop-in -------------------------------------------------- */
 /* Host arrays of the reference's FastRay records (40 bytes each: tMax,

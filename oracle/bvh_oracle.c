@@ -23,6 +23,7 @@
  *     intersectSaveDistance ............... fastNodeManager.h:1232-1326
  *     intersectWideAlternative /
  *     intersectSecondaryWideAlternative ... fastNodeManager.h:835-1230
+ *   the ISPC kernels as single calls (oracle_*_calls) .. rayTracerTemplate.ispc:26-233
  *
  * Parity status: UNPINNED at the reference level. The reference ships no
  * golden vectors or known-answer tests for this path and cannot be built here
@@ -881,6 +882,83 @@ void oracle_fp64_pairs(const float* rays, const float* tri9, uint64_t n, int nor
     o3[0] = tt;
     o3[1] = b1;
     o3[2] = b2;
+  }
+}
+
+/* --------------------------------------------- ISPC calls, one by one -- */
+/* The reference's exported ISPC kernels as independent calls, for the
+ * batched GPU entry points. FastRay records (10 floats: tMax, pos[3],
+ * invDirection[3], direction[3]; fastRay.h:14-29) are used as given: the
+ * slab test reads invDirection, Moller-Trumbore reads pos and direction.
+ * Rows are `width` long (padding 1, raytracerTemplateGen.py:10). */
+static void fastray_state(const float* fr, oray_t* r) {
+  r->tmax = fr[0];
+  for (int a = 0; a < 3; ++a) {
+    r->o[a] = fr[1 + a];
+    r->inv[a] = fr[4 + a];
+    r->d[a] = fr[7 + a];
+  }
+  r->code = max_abs_dim(r->d);
+  r->reverse = r->d[r->code] <= 0;
+}
+
+/* aabbIntersect{N} (rayTracerTemplate.ispc:171-233) over all `n` lanes of
+ * bounds + offset[i]: distances[i * n + lane] = t0 for each hit lane (other
+ * entries untouched), result[i] = 1 if any lane is hit. */
+void oracle_aabb_intersect_calls(int32_t n, const float* bounds, const uint32_t* offset,
+                                 const float* fastrays, float* distances, uint8_t* result,
+                                 uint64_t count) {
+  for (uint64_t i = 0; i < count; ++i) {
+    oray_t r;
+    fastray_state(fastrays + i * 10, &r);
+    const float* bd = bounds + offset[i];
+    int any = 0;
+    for (int j = 0; j < n; ++j) {
+      float lo[3] = {bd[j], bd[j + n], bd[j + n * 2]};
+      float hi[3] = {bd[j + n * 3], bd[j + n * 4], bd[j + n * 5]};
+      float t0 = 0;
+      if (slab_dist(lo, hi, &r, r.tmax, &t0)) {
+        any = 1;
+        distances[i * n + j] = t0;
+      }
+    }
+    result[i] = (uint8_t)any;
+  }
+}
+
+/* triIntersect{L} (rayTracerTemplate.ispc:28-108) on the leaf block at
+ * tri + tri_id[i] with `l` lanes of a `gang`-wide ISPC gang: result[i] = the
+ * in-leaf index of the hit (or -1); a hit lowers fastrays[i * 10] (tMax). */
+void oracle_tri_intersect_calls(int32_t l, int32_t gang, const float* tri,
+                                const uint32_t* tri_id, float* fastrays, int32_t* result,
+                                uint64_t count) {
+  oracle_fast_t f;
+  memset(&f, 0, sizeof f);
+  f.gang = gang;
+  f.leaf_memory = l;
+  f.tri_points = tri;
+  for (uint64_t i = 0; i < count; ++i) {
+    oray_t r;
+    fastray_state(fastrays + i * 10, &r);
+    float u, v;
+    result[i] = tri_intersect(&f, tri_id[i], l, l, &r, &u, &v, NULL);
+    fastrays[i * 10] = r.tmax;
+  }
+}
+
+/* triAnyHit{L} (rayTracerTemplate.ispc:112-168): result[i] = 1 if any of
+ * the `l` triangles at tri + tri_id[i] is hit within tMax. */
+void oracle_tri_any_hit_calls(int32_t l, const float* tri, const uint32_t* tri_id,
+                              const float* fastrays, uint8_t* result, uint64_t count) {
+  oracle_fast_t f;
+  memset(&f, 0, sizeof f);
+  f.gang = 4;
+  f.leaf_memory = l;
+  f.tri_points = tri;
+  for (uint64_t i = 0; i < count; ++i) {
+    oray_t r;
+    fastray_state(fastrays + i * 10, &r);
+    result[i] = (uint8_t)tri_any_hit(&f, tri_id[i], l, l, &r, NULL);
   }
 }
 

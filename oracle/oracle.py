@@ -50,6 +50,13 @@ def lib() -> C.CDLL:
                                             C.c_int]
             L.oracle_fp64_pairs.restype = None
             L.oracle_fp64_pairs.argtypes = [_P, _P, C.c_uint64, C.c_int, _P]
+            L.oracle_aabb_intersect_calls.restype = None
+            L.oracle_aabb_intersect_calls.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.c_uint64]
+            L.oracle_tri_intersect_calls.restype = None
+            L.oracle_tri_intersect_calls.argtypes = [C.c_int32, C.c_int32, _P, _P, _P, _P,
+                                                     C.c_uint64]
+            L.oracle_tri_any_hit_calls.restype = None
+            L.oracle_tri_any_hit_calls.argtypes = [C.c_int32, _P, _P, _P, _P, C.c_uint64]
             _lib = L
     return _lib
 
@@ -130,3 +137,40 @@ def fp64_pairs(rays: np.ndarray, tri9: np.ndarray, normalise: bool) -> np.ndarra
     out = np.zeros((rays.shape[0], 3), np.float64)
     lib().oracle_fp64_pairs(_p(rays), _p(tri9), rays.shape[0], int(normalise), _p(out))
     return out
+
+
+def aabb_intersect_calls(n: int, bounds: np.ndarray, offsets: np.ndarray, fastrays: np.ndarray,
+                         distances: np.ndarray):
+    """aabbIntersect{n} per call (bvh_oracle.c: oracle_aabb_intersect_calls):
+    returns (result [count] u8, distances [count, n] with t0 written at hit
+    lanes of the given array)."""
+    bounds = np.ascontiguousarray(bounds, np.float32)
+    offsets = np.ascontiguousarray(offsets, np.uint32)
+    fastrays = np.ascontiguousarray(fastrays, np.float32)
+    dist = np.array(distances, np.float32, copy=True, order="C")
+    res = np.zeros(offsets.shape[0], np.uint8)
+    lib().oracle_aabb_intersect_calls(n, _p(bounds), _p(offsets), _p(fastrays), _p(dist),
+                                      _p(res), offsets.shape[0])
+    return res, dist
+
+
+def tri_intersect_calls(l: int, gang: int, tri: np.ndarray, ids: np.ndarray,
+                        fastrays: np.ndarray):
+    """triIntersect{l} per call: returns (in-leaf index or -1, the FastRay
+    records with tMax lowered on hits)."""
+    tri = np.ascontiguousarray(tri, np.float32)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    fr = np.array(fastrays, np.float32, copy=True, order="C")
+    res = np.zeros(ids.shape[0], np.int32)
+    lib().oracle_tri_intersect_calls(l, gang, _p(tri), _p(ids), _p(fr), _p(res), ids.shape[0])
+    return res, fr
+
+
+def tri_any_hit_calls(l: int, tri: np.ndarray, ids: np.ndarray, fastrays: np.ndarray):
+    """triAnyHit{l} per call: returns [count] u8."""
+    tri = np.ascontiguousarray(tri, np.float32)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    fr = np.ascontiguousarray(fastrays, np.float32)
+    res = np.zeros(ids.shape[0], np.uint8)
+    lib().oracle_tri_any_hit_calls(l, _p(tri), _p(ids), _p(fr), _p(res), ids.shape[0])
+    return res
