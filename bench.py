@@ -938,9 +938,14 @@ def run_terrain(a):
     stream = torch.cuda.current_stream(dev)
     res = {}
     for name, o in (("per_ray", {"scheme": "per_ray"}), ("stream_wg16", {"scheme": "stream"}),
-                    ("persistent", {"scheme": "persistent", "policy": 0, "refill": 16})):
-        ms_p, hp = _time_trace(sc, d_p, "closest", o, a.steps, stream)
-        ms_s, hs = _time_trace(sc, d_s, "any", o, a.steps, stream)
+                    ("persistent", {"scheme": "persistent", "policy": 0, "refill": 16}),
+                    ("per_ray_local", {"scheme": "per_ray", "stack": "local"}),
+                    # primary per-ray with local stacks, shadow persistent policy 2
+                    ("mixed", [{"scheme": "per_ray", "stack": "local"},
+                               {"scheme": "persistent", "policy": 2, "refill": 16}])):
+        op, os_ = (o[0], o[1]) if isinstance(o, list) else (o, o)
+        ms_p, hp = _time_trace(sc, d_p, "closest", op, a.steps, stream)
+        ms_s, hs = _time_trace(sc, d_s, "any", os_, a.steps, stream)
         ok = (np.array_equal(hp["hits"].cpu().numpy().view(np.uint32), ref["hits"].view(np.uint32))
               and np.array_equal(hs["occluded"].cpu().numpy(), ref_s))
         res[name] = {"ms_primary": ms_p, "ms_shadow": ms_s,

@@ -174,6 +174,80 @@ def test_edge_cases():
     assert e["hits"].shape == (0, 4)
 
 
+@pytest.mark.parametrize("profile", ["instrumented", "fast"])
+def test_non_finite_and_extreme_rays(profile):
+    """Rays the renderer never makes but a caller may pass: infinite and
+    zero tMax, NaN or infinite direction components, a zero direction,
+    signed zeros, subnormal and huge components, origins far outside the
+    scene. Every scheme returns the oracle's results (the reference's
+    comparison forms decide what a NaN does): bit for bit, except that a NaN
+    result matches any NaN (the GPU's canonical NaN is 0x7fffffff, an x86
+    host's default NaN 0xffc00000)."""
+
+    def nan_bits(hits):
+        # (prim, t, u, v): prim compared as is, t / u / v with one NaN pattern
+        u = np.ascontiguousarray(hits, np.float32).view(np.uint32).copy()
+        f = np.ascontiguousarray(hits, np.float32)
+        u[:, 1:][np.isnan(f[:, 1:])] = 0x7FC00000
+        return u
+    tris, b, cv = TS.bvh("clutter120", 8, 4)
+    fv = O.FastView(b.export_fast()) if profile == "fast" else None
+    base = TS.clutter_rays(tris)[:64].copy()
+    rows = []
+    inf, nan = np.float32(np.inf), np.float32(np.nan)
+    for k, r in enumerate(base):
+        r = r.copy()
+        v = k % 16
+        if v == 0: r[3] = inf
+        elif v == 1: r[3] = 0.0
+        elif v == 2: r[5] = nan
+        elif v == 3: r[4:7] = 0.0
+        elif v == 4: r[4] = -0.0; r[5] = 0.0
+        elif v == 5: r[6] = inf
+        elif v == 6: r[4:7] *= np.float32(1e-40)
+        elif v == 7: r[4:7] *= np.float32(1e30)
+        elif v == 8: r[0:3] = np.float32(1e30)
+        elif v == 9: r[0:3] = -r[0:3] * 100
+        elif v == 10: r[3] = nan
+        elif v == 11: r[1] = inf
+        elif v == 12: r[3] = -1.0
+        elif v == 13: r[4] = np.float32(1e-45)
+        rows.append(r)
+    rays = np.stack(rows).astype(np.float32)
+    scene = pkg.Scene(b)
+    for kind in ("closest", "any"):
+        if profile == "instrumented":
+            ref = O.trace_instrumented(cv, rays, shadow=kind == "any", counters=False)
+        else:
+            ref = O.trace_fast(fv, cv, rays, any_hit=kind == "any", counters=False)
+        for scheme, kw in SCHEMES:
+            got = scene.trace(dev(rays), kind=kind, scheme=scheme, profile=profile, **kw)
+            if kind == "closest":
+                assert np.array_equal(nan_bits(got["hits"].cpu().numpy()),
+                                      nan_bits(ref["hits"])), scheme
+            else:
+                assert np.array_equal(got["occluded"].cpu().numpy(), ref["occluded"]), scheme
+        extra = [{"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 8}]
+        if kind == "any":
+            extra.append({"scheme": "persistent", "policy": 2, "refill": 24, "any_order": True})
+        for o in extra:
+            got = scene.trace(dev(rays), kind=kind, profile=profile, **o)
+            if kind == "closest":
+                assert np.array_equal(nan_bits(got["hits"].cpu().numpy()),
+                                      nan_bits(ref["hits"])), o
+            else:
+                assert np.array_equal(got["occluded"].cpu().numpy(), ref["occluded"]), o
+    if profile == "instrumented":
+        got = scene.trace(dev(rays), counters=True, depth_hist=True)
+        ref = O.trace_instrumented(cv, rays, shadow=False)
+        assert np.array_equal(nan_bits(got["hits"].cpu().numpy()), nan_bits(ref["hits"]))
+        assert np.array_equal(got["counters"].cpu().numpy().astype(np.uint32)[:, :7],
+                              ref["counters"][:, :7])
+        assert np.array_equal(got["depth_hist"].cpu().numpy().astype(np.uint64),
+                              ref["depth_hist"])
+    scene.status()
+
+
 @pytest.mark.parametrize("n", [1, 31, 127, 129, 255, 257, 1000])
 def test_ragged_ray_counts(n, terrain):
     tris, b, cv, rays, scene = terrain
