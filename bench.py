@@ -84,12 +84,14 @@ def parse():
     p.add_argument("--report", default="",
                    help="clutter: write the reference's _Info.txt / _Perf.txt into this folder")
     p.add_argument("--workload", default="clutter",
-                   choices=["clutter", "batch64", "adjoint", "scale8m", "terrain", "sweep"],
+                   choices=["clutter", "batch64", "adjoint", "scale8m", "terrain", "sweep",
+                            "gpuframe"],
                    help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch; "
                         "adjoint: forward + backward of the hit distance; scale8m: 8M "
                         "triangles FP32 vs Q8 nodes; terrain: the 32k-triangle terrain, N4L4, "
                         "512x512 + shadow rays; sweep: the clutter frame for every N, L in "
-                        "{4,8,12,16}^2, per-ray vs ray-stream")
+                        "{4,8,12,16}^2, per-ray vs ray-stream; gpuframe: the clutter frame with "
+                        "every ray generated on the GPU, AO image read back")
     p.add_argument("--scenes", type=int, default=64)
     p.add_argument("--job-reorder", type=int, default=8,
                    help="batch64: direction bins per cube face side for the AO jobs (0 = off)")
@@ -981,6 +983,119 @@ def run_terrain(a):
     print(json.dumps(line))
 
 
+def run_gpuframe(a):
+    """The clutter frame rendered on the GPU end to end: camera rays
+    (bvhgpu_camera_rays), primary closest hits, shadow and 8 cosine AO rays
+    per hit generated from the hits (bvhgpu_secondary_rays), the shadow and
+    AO traces, and the per-pixel AO factor (bvhgpu_ao_factor); the AO image
+    is read back to the host each step. No rays cross the host boundary."""
+    import torch
+    import bvhraytracer_gb300 as pkg
+    from bvhraytracer_gb300 import scenes as S
+    from oracle import oracle as O
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    t_setup = time.time()
+    tris = S.clutter(a.objects, seed=1)
+    bvh = pkg.Bvh(tris, a.branching, a.leaf)
+    sc = pkg.Scene(bvh)
+    cam, target, light = S.clutter_viewpoints(a.objects, seed=1)
+    ao_len = float(0.1 * S.scene_diagonal(tris))
+    w, h, spp = a.width, a.height, a.ao
+    img = torch.empty(w * h, dtype=torch.float32).pin_memory()
+
+    def frame():
+        prim = pkg.camera_rays(cam, target, w, h)
+        hits = sc.trace(prim, scheme="per_ray", stack="local")["hits"]
+        sh, ao = sc.secondary_rays(prim, hits, light=light, ao_samples=spp, ao_length=ao_len,
+                                   sampling="cosine", seed=0)
+        occ_s = sc.trace(sh, kind="any", scheme="persistent", policy=2, refill=16)["occluded"]
+        occ_a = sc.trace(ao, kind="any", scheme="persistent", policy=2, refill=24, reorder=10,
+                         any_order=True)["occluded"]
+        return prim, hits, sh, ao, occ_s, occ_a, pkg.ao_factor(occ_a, spp)
+
+    prim, hits, sh, ao, occ_s, occ_a, fac = frame()
+    torch.cuda.synchronize(dev)
+    setup_s = time.time() - t_setup
+    active = lambda r: int((~torch.isnan(r[:, 0])).sum().item())
+    n_prim, n_sh, n_ao = prim.shape[0], active(sh), active(ao)
+    n_rays = n_prim + n_sh + n_ao
+    # Parity on samples of the GPU-made rays: the oracle traces the same rays.
+    cv = O.CompactView(bvh.export_compact())
+    rng = np.random.default_rng(5)
+    checks = {}
+    for name, rays, kind, out in (("primary", prim, "closest", hits), ("shadow", sh, "any", occ_s),
+                                  ("ao", ao, "any", occ_a)):
+        idx = np.sort(rng.choice(rays.shape[0], min(20000, rays.shape[0]), replace=False))
+        r = rays.cpu().numpy()[idx]
+        ref = O.trace_instrumented(cv, r, shadow=kind == "any", counters=False)
+        got = out.cpu().numpy()[idx]
+        want = ref["hits"] if kind == "closest" else ref["occluded"]
+        checks[name] = bool(np.array_equal(got.view(np.uint8), want.view(np.uint8)))
+    sc.status()
+
+    def timed(fn):
+        for _ in range(a.warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / a.steps
+
+    ms_eager = timed(frame)
+    outs = {}
+
+    def capture_body():
+        outs["f"] = frame()[-1]
+    capture_body()
+    torch.cuda.synchronize(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        capture_body()
+    with ClockSampler(0) as clk:
+        ms_graph = timed(g.replay)
+    clocks = clk.summary()
+    graph_ok = bool(torch.equal(outs["f"], fac))
+
+    def e2e_step():
+        g.replay()
+        img.copy_(outs["f"], non_blocking=True)
+        torch.cuda.synchronize(dev)
+    for _ in range(a.warmup):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / a.steps
+    ms = min(ms_eager, ms_graph)
+    line = {
+        "metric": METRIC, "value": n_rays / (ms / 1e3) / 1e6, "unit": METRIC, "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded clutter scene; rays generated on the GPU)",
+        "config": {"workload": f"clutter-{a.objects}obj N{a.branching}L{a.leaf} {w}x{h} frame on the "
+                               f"GPU: camera rays, primary, shadow + {spp} cosine AO rays per hit "
+                               "generated from the hits, AO factor",
+                   "rays_per_step": n_rays, "primary": n_prim, "shadow": n_sh, "ao": n_ao,
+                   "ms_eager": ms_eager, "ms_graph": ms_graph, "graph_equals_eager": graph_ok,
+                   "oracle_equal_on_20k_samples": checks, "setup_s": round(setup_s, 1),
+                   "plan": "primary per-ray (local stacks); shadow persistent policy 2, refill 16; "
+                           "AO persistent policy 2, refill 24, 6x10x10 direction bins, "
+                           "child-index push order"},
+        "e2e": {"value": n_rays / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(w * h * 4)},
+        "clocks": clocks,
+        # camera rays, primary trace, secondary rays, shadow trace (+ queue clear
+        # is a memset), four reorder passes + AO trace, AO factor
+        "gpu_launches": 10 * a.steps,
+    }
+    print(json.dumps(line))
+
+
 def run_sweep(a):
     """The 1M-triangle clutter frame for every N, L in {4, 8, 12, 16}^2:
     plain per-ray against ray-stream traversal, the persistent kernel and the
@@ -1060,6 +1175,8 @@ def main():
         run_terrain(a)
     elif a.workload == "sweep":
         run_sweep(a)
+    elif a.workload == "gpuframe":
+        run_gpuframe(a)
     else:
         run_ours(a)
 
