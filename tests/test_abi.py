@@ -161,3 +161,28 @@ def test_struct_layouts_match_the_c_header(tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for f in py._fields_:
             assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+def test_new_entry_points_validate_arguments_without_a_gpu():
+    """Argument checks of the batched ISPC calls, the multi-batch host trace
+    and the stored-hit adjoint run before any device work."""
+    lib = N.lib()
+    assert lib.bvhgpu_gang_size() == 4
+    buf = np.zeros(64, np.float32)
+    ids = np.zeros(1, np.uint32)
+    res = np.zeros(4, np.uint8)
+    assert lib.bvhgpu_aabb_intersect(5, buf.ctypes.data, ids.ctypes.data, buf.ctypes.data,
+                                     buf.ctypes.data, res.ctypes.data, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_aabb_intersect(8, None, None, None, None, None, 0, None) == N.OK
+    assert lib.bvhgpu_aabb_intersect(8, None, ids.ctypes.data, buf.ctypes.data,
+                                     buf.ctypes.data, res.ctypes.data, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_tri_intersect(8, 3, buf.ctypes.data, ids.ctypes.data, buf.ctypes.data,
+                                    res.ctypes.data, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_tri_intersect(7, 4, buf.ctypes.data, ids.ctypes.data, buf.ctypes.data,
+                                    res.ctypes.data, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_tri_any_hit(20, buf.ctypes.data, ids.ctypes.data, buf.ctypes.data,
+                                  res.ctypes.data, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_trace_host_batches(None, None, 1, None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_adjoint_hits(None, None, None, 1, None, None, 0, 0, None, None, None,
+                                   None) == N.ERR_BAD_ARG
+    assert b"null" in lib.bvhgpu_last_error()
