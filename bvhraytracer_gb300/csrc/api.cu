@@ -164,6 +164,19 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   return BVHGPU_OK;
 }
 
+// The traversal stacks of a launch must fit the 227 KB of shared memory a
+// block may use (the stream scheme keeps a whole packet's state there).
+static int check_smem_fit(const dev::LaunchCfg& cfg, int cap) {
+  if (cfg.scheme == BVHGPU_STREAM &&
+      dev::stream_smem_bytes(cfg.packet, cap, cfg.count) > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED,
+                     "stream packet does not fit shared memory for this tree depth");
+  if (cfg.scheme != BVHGPU_STREAM &&
+      (size_t)cap * 128 * 4 * (cfg.save_distance ? 2 : 1) > 227 * 1024)
+    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  return BVHGPU_OK;
+}
+
 // Shared memory per block for the persistent kernel's copy of the top levels;
 // small enough to keep six blocks per SM next to the traversal stacks.
 constexpr uint32_t kTopStageBytes = 8192;
@@ -573,12 +586,7 @@ int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   a.counters = counters;
   a.depth_hist = reinterpret_cast<unsigned long long*>(depth_hist);
   a.stack_cap = stack_cap(s);
-  if (cfg.scheme == BVHGPU_STREAM &&
-      dev::stream_smem_bytes(cfg.packet, a.stack_cap, cfg.count) > 227 * 1024)
-    return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet does not fit shared memory for this tree depth");
-  if (cfg.scheme != BVHGPU_STREAM &&
-      (size_t)a.stack_cap * 128 * 4 * (cfg.save_distance ? 2 : 1) > 227 * 1024)
-    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  if ((rc = check_smem_fit(cfg, a.stack_cap))) return rc;
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   return launch_reordered(s, a, cfg, (cudaStream_t)stream);
@@ -706,6 +714,7 @@ int bvhgpu_trace_host(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   int rc = check_opts(opts, b.cfg);
   if (rc) return rc;
   if (n == 0) return BVHGPU_OK;
+  if ((rc = check_smem_fit(b.cfg, stack_cap(s)))) return rc;
   if (!rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
   if (b.cfg.kind == BVHGPU_CLOSEST ? !hits : !occluded)
     return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
@@ -725,6 +734,7 @@ int bvhgpu_trace_host_batches(bvhgpu_scene_t s, const bvhgpu_host_batch_t* batch
     int rc = check_opts(x.opts, h.cfg);
     if (rc) return rc;
     if (x.n == 0) continue;
+    if ((rc = check_smem_fit(h.cfg, stack_cap(s)))) return rc;
     if (!x.rays) return set_error(BVHGPU_ERR_BAD_ARG, "rays: null");
     if (h.cfg.kind == BVHGPU_CLOSEST ? !x.hits : !x.occluded)
       return set_error(BVHGPU_ERR_BAD_ARG, "result buffer: null");
