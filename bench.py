@@ -42,11 +42,12 @@ METRIC = "Mrays/s"
 # is the ray stream plus cold misses (the BVH stays in L2), so it grows with
 # the ray count and is scaled by it.
 # Source: profiles/trace_persistent_p2_ao_clutter250k_N8L8.md
-# With reorder = 8 the launch is the four reorder passes plus the trace (the
+# With reordering the launch is the four reorder passes plus the trace (the
 # rays read once to bin them and once, gathered in bin order, by the trace;
-# the bins and the index permutation).
-# Source: profiles/reorder_k8_persistent_p2_ao_clutter250k_N8L8.md
-NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, 8: 445689088 / 4147200}
+# the bins and the index permutation): the bench's plan, 6 x 10 x 10 bins and
+# child-index push order.
+# Source: profiles/traffic_ao_reorder_k10_anyorder_clutter250k_N8L8.md
+NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, "reorder": 457373696 / 4147200}
 
 
 def parse():
@@ -459,8 +460,7 @@ def run_ours(a):
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
             and dom_opts.get("policy") == 2 and chosen[dom][0].node_format == "fp32"):
-        # The reorder passes' bytes per ray do not depend on the bin count K.
-        key = 8 if dom_opts.get("reorder", 0) else 0
+        key = "reorder" if dom_opts.get("reorder", 0) else 0
         traffic = NCU_TRAFFIC_PER_AO_RAY[key] * int(batches[dom][0].shape[0])
 
     compare = {}
@@ -509,8 +509,9 @@ def run_ours(a):
                 else "fallback",
                 "traffic": traffic,
                 "traffic_source": ("ncu DRAM bytes per AO ray of a 4.1M-ray capture on the "
-                                   "251k-triangle scene (reorder K=8 when the plan reorders), "
-                                   "scaled by rays" if traffic else None),
+                                   "251k-triangle scene (with the reorder passes, K=10 and "
+                                   "child-index order, when the plan reorders), scaled by rays"
+                                   if traffic else None),
                 "algorithmic_bytes_per_launch": alg[dom]["bytes"],
                 "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
             },
