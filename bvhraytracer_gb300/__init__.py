@@ -195,7 +195,8 @@ class Scene:
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
               policy: int = 0, refill: int = 0, counters: bool = False,
               depth_hist: bool = False, save_distance: bool = False, reorder: int = 0,
-              stack: str = "shared", any_order: bool = False, out=None, stream=None) -> dict:
+              stack: str = "shared", any_order: bool = False, steps: int = 0, out=None,
+              stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -208,7 +209,11 @@ class Scene:
         ``"shared"`` or ``"local"`` memory for the traversal stacks.
         ``any_order``: any-hit rays without counters push hit children in
         child-index order in both profiles (same results; faster for short
-        rays such as ambient occlusion).
+        rays such as ambient occlusion). ``steps`` = S > 0 (stream scheme,
+        with ``counters``): also returns ``"step_stats"`` ``[packets, S, 5]``
+        (node work, unique nodes, leaf work, unique leaves, terminations per
+        step, step 0 the set-up) and ``"step_count"`` ``[packets]``
+        (bvhgpu_trace_steps).
         """
         import torch
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
@@ -236,6 +241,15 @@ class Scene:
                         int(save_distance), int(reorder), int(stack == "local"),
                         int(any_order))
         s = stream if stream is not None else torch.cuda.current_stream(dev)
+        if steps:
+            packets = -(-n // (workgroup * workgroup))
+            res["step_stats"] = torch.zeros((packets, steps, 5), dtype=torch.int32, device=dev)
+            res["step_count"] = torch.zeros(packets, dtype=torch.int32, device=dev)
+            N.check(N.lib().bvhgpu_trace_steps(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
+                                               steps, _ptr(res["step_stats"]),
+                                               _ptr(res["step_count"]),
+                                               C.c_void_p(s.cuda_stream)))
+            return res
         N.check(N.lib().bvhgpu_trace(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
                                      C.c_void_p(s.cuda_stream)))
         return res

@@ -84,7 +84,7 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
   } else {
     if (FMT != kFmtFP32) return cudaErrorNotSupported;
     const int p = cfg.packet;
-    const size_t smem = stream_smem_bytes(p, a.stack_cap, COUNT);
+    const size_t smem = stream_smem_bytes(p, a.stack_cap, COUNT, COUNT && a.step_stats);
     auto k = trace_stream_kernel<NM, PROFILE, KIND, COUNT>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;

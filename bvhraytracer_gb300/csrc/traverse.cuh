@@ -57,6 +57,13 @@ struct TraceArgs {
   // Reordered traces: the i-th ray the kernel takes is input ray
   // out_index[i] (null: i), and its results go to that input slot.
   const uint32_t* out_index = nullptr;
+  // Stream scheme with counters: per packet and step, (node work, unique
+  // nodes, leaf work, unique leaves, terminations) into
+  // step_stats[(packet * step_cap + step) * 5 ..] for steps < step_cap, and
+  // the packet's step count (with step 0, the set-up) into step_count[packet].
+  uint32_t* step_stats = nullptr;
+  uint32_t* step_count = nullptr;
+  int step_cap = 0;
 };
 
 BVHGPU_DEV uint64_t out_slot(const TraceArgs& a, uint64_t rid) {
@@ -630,18 +637,36 @@ BVHGPU_DEV Ray unpack_ray(const StreamRay& s) {
 
 struct StreamShared {
   int node_rays, leaf_rays, next_node, next_leaf;
+  int unique_nodes, unique_leaves, terminations, pad;  // step log
 };
 
-// Shared-memory bytes of the stream kernel for a packet of p rays.
-inline size_t stream_smem_bytes(int p, int stack_cap, bool count) {
+// Shared-memory bytes of the stream kernel for a packet of p rays (with the
+// step log: a hash set of 2p entries for the unique node / leaf counts).
+inline size_t stream_smem_bytes(int p, int stack_cap, bool count, bool steps = false) {
   size_t b = sizeof(StreamShared);
   b = (b + 15) / 16 * 16;
+  if (steps) b += (size_t)p * 2 * 4;
   b += (size_t)p * sizeof(StreamRay);
   b += (size_t)p * stack_cap * 4;        // stacks
   b += (size_t)p * 4 * 4;                // best: leaf, lane|hit|sp, u, v
   b += (size_t)p * 2 * 2;                // two work lists
   if (count) b += (size_t)p * 8 * 4;     // counters
   return b;
+}
+
+// Insert into an open-addressing set in shared memory (linear probing,
+// atomicCAS); true if the key was not there yet. At most size / 2 keys go
+// into a set, so a free slot is always found within `size` probes.
+constexpr uint32_t kSetEmpty = 0x7FFFFFFFu;  // no node index or leaf entry has this value
+BVHGPU_DEV bool set_insert(uint32_t* tbl, int size, uint32_t key) {
+  uint32_t h = (key * 2654435761u) % (uint32_t)size;
+  for (int probe = 0; probe < size; ++probe) {
+    const uint32_t old = atomicCAS(tbl + h, kSetEmpty, key);
+    if (old == kSetEmpty) return true;
+    if (old == key) return false;
+    h = (h + 1 == (uint32_t)size) ? 0u : h + 1u;
+  }
+  return false;
 }
 
 template <int N, int PROFILE, int KIND, bool COUNT>
@@ -651,7 +676,17 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   StreamShared* ctl = reinterpret_cast<StreamShared*>(smem_raw);
-  uint8_t* base = smem_raw + 16;
+  uint8_t* base = smem_raw + (sizeof(StreamShared) + 15) / 16 * 16;
+  // Step log (workgroup analysis of CameraData, cameraData.h:660-1109): per
+  // step the node and leaf work, the unique nodes and leaves among them and
+  // the rays that terminate, as intersectWideAlternative collects them
+  // (compactNode.cpp:357-601).
+  const bool log = COUNT && a.step_stats != nullptr;
+  uint32_t* set = nullptr;
+  if (log) {
+    set = reinterpret_cast<uint32_t*>(base);
+    base += (size_t)P * 2 * 4;
+  }
   StreamRay* rays = reinterpret_cast<StreamRay*>(base);
   base += (size_t)P * sizeof(StreamRay);
   uint32_t* stacks = reinterpret_cast<uint32_t*>(base);  // stacks[slot * P + ray]
@@ -669,7 +704,10 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
   const uint64_t rid = first + tid;
   const int cap = a.stack_cap;
 
-  if (tid == 0) { ctl->node_rays = 0; ctl->leaf_rays = 0; ctl->next_node = 0; ctl->next_leaf = 0; }
+  if (tid == 0) {
+    ctl->node_rays = 0; ctl->leaf_rays = 0; ctl->next_node = 0; ctl->next_leaf = 0;
+    ctl->unique_nodes = 0; ctl->unique_leaves = 0; ctl->terminations = 0;
+  }
   __syncthreads();
   // Set-up: active rays go to the node part of list 0 (the root entry is an
   // inner node unless the whole tree is one leaf).
@@ -708,11 +746,28 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
     }
   }
   __syncthreads();
+  // Step 0, the state before the loop: the active rays at the root, the
+  // inactive ones terminated (compactNode.cpp:410-415).
+  int step = 1;
+  if (log && tid == 0 && a.step_cap > 0) {
+    const uint32_t wide = (uint32_t)(a.n - first < (uint64_t)P ? a.n - first : (uint64_t)P);
+    const uint32_t act = (uint32_t)(ctl->node_rays + ctl->leaf_rays);
+    uint32_t* rec = a.step_stats + (size_t)blockIdx.x * a.step_cap * 5;
+    rec[0] = root_leaf ? 0u : act;
+    rec[1] = root_leaf ? 0u : 1u;
+    rec[2] = root_leaf ? act : 0u;
+    rec[3] = root_leaf ? (act ? 1u : 0u) : 0u;
+    rec[4] = wide - act;
+  }
 
   int cur = 0;
   while (true) {
     const int node_rays = ctl->node_rays, leaf_rays = ctl->leaf_rays;
     if (node_rays == 0 && leaf_rays == 0) break;
+    if (log) {
+      for (int i = tid; i < 2 * P; i += P) set[i] = kSetEmpty;
+      __syncthreads();
+    }
     int ray = -1;
     bool is_node = false;
     const uint16_t* wcur = work0 + cur * P;
@@ -728,6 +783,8 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       Counters ctr;
       --sp;
       const uint32_t e = stacks[sp * P + ray];
+      if (log && set_insert(set, 2 * P, e))
+        atomicAdd(is_node ? &ctl->unique_nodes : &ctl->unique_leaves, 1);
       if (is_node) {
         int depth;
         if (!node_step<N, PROFILE, KIND, COUNT, kFmtFP32>(sc, e, nullptr, 0u, r, tmax, stacks + ray,
@@ -775,6 +832,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
         else want_node = true;
       }
       if (done) sp = 0;
+      if (log && sp == 0) atomicAdd(&ctl->terminations, 1);
       misc = (misc & ~(0x7FFF << 8)) | (sp << 8);
       best_misc[ray] = misc;
     }
@@ -796,14 +854,27 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
     }
     __syncthreads();
     if (tid == 0) {
+      if (log && step < a.step_cap) {
+        uint32_t* rec = a.step_stats + ((size_t)blockIdx.x * a.step_cap + step) * 5;
+        rec[0] = (uint32_t)node_rays;
+        rec[1] = (uint32_t)ctl->unique_nodes;
+        rec[2] = (uint32_t)leaf_rays;
+        rec[3] = (uint32_t)ctl->unique_leaves;
+        rec[4] = (uint32_t)ctl->terminations;
+      }
+      ctl->unique_nodes = 0;
+      ctl->unique_leaves = 0;
+      ctl->terminations = 0;
       ctl->node_rays = ctl->next_node;
       ctl->leaf_rays = ctl->next_leaf;
       ctl->next_node = 0;
       ctl->next_leaf = 0;
     }
+    ++step;
     cur = nxt;
     __syncthreads();
   }
+  if (log && tid == 0) a.step_count[blockIdx.x] = (uint32_t)step;
 
   // Results of this thread's own ray slot.
   if (rid < a.n) {

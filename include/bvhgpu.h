@@ -241,6 +241,21 @@ int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                  const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                  uint32_t* counters, uint64_t* depth_hist, void* stream);
 
+/* The stream scheme with counters and a step log, for CameraData's workgroup
+ * analysis (cameraData.h:660-1109): for each packet (workgroup) p and step s
+ * (step 0 = the state before the loop, compactNode.cpp:410-415), writes
+ * step_stats[(p * step_cap + s) * 5 ..] = (rays doing node work, unique nodes
+ * among them, rays doing leaf work, unique leaves among them, rays that
+ * terminate) as intersectWideAlternative collects them
+ * (compactNode.cpp:357-601), and step_count[p] = the packet's number of steps;
+ * steps at or beyond step_cap are counted but not written. opts: scheme
+ * BVHGPU_STREAM, no reorder; counters non-null; packets of opts->workgroup^2
+ * rays in ray order. Results and counters equal bvhgpu_trace's. */
+int bvhgpu_trace_steps(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
+                       const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
+                       uint32_t* counters, uint64_t* depth_hist, int32_t step_cap,
+                       uint32_t* step_stats, uint32_t* step_count, void* stream);
+
 /* Host pointers: copies rays in, traces, copies results out, synchronises
  * `stream`. Device staging buffers are owned by the scene and reused. */
 int bvhgpu_trace_host(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,

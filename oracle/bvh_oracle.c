@@ -411,9 +411,29 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
 
 /* intersectWideAlternative (compactNode.cpp:357-601) over packets of
  * `packet` consecutive rays. Per-ray results equal the per-ray traversal. */
-int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* rays, uint64_t n,
-                                     int shadow, int packet, ohit_t* hits, uint8_t* occluded,
-                                     octr_t* ctrs, uint64_t* hist) {
+static int cmp_i32(const void* x, const void* y) {
+  int32_t a = *(const int32_t*)x, c = *(const int32_t*)y;
+  return (a > c) - (a < c);
+}
+
+/* Number of distinct values among ids[0..k) (sorts ids). */
+static uint32_t distinct(int32_t* ids, int k) {
+  if (k == 0) return 0;
+  qsort(ids, (size_t)k, sizeof(int32_t), cmp_i32);
+  uint32_t d = 1;
+  for (int i = 1; i < k; ++i) d += ids[i] != ids[i - 1];
+  return d;
+}
+
+/* intersectWideAlternative with counters; with `steps`, also the per-step
+ * data it collects for CameraData's workgroup analysis
+ * (compactNode.cpp:357-601): per packet p and step s, steps[(p * step_cap
+ * + s) * 5 ..] = node work, unique nodes, leaf work, unique leaves,
+ * terminations (step 0: the state before the loop, compactNode.cpp:410-415;
+ * a root that is a leaf starts as leaf work), step_count[p] = steps used. */
+static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n, int shadow,
+                       int packet, ohit_t* hits, uint8_t* occluded, octr_t* ctrs,
+                       uint64_t* hist, int step_cap, uint32_t* steps, uint32_t* step_count) {
   int cap = stack_need(b);
   if (packet <= 0 || packet > 65535) return 1;
   int64_t npk = (int64_t)((n + (uint64_t)packet - 1) / (uint64_t)packet);
@@ -425,6 +445,7 @@ int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* ray
     ostate_t* st = (ostate_t*)malloc(sizeof(ostate_t) * (size_t)packet);
     uint16_t* w1 = (uint16_t*)malloc(2 * (size_t)packet);
     uint16_t* w2 = (uint16_t*)malloc(2 * (size_t)packet);
+    int32_t* ids = (int32_t*)malloc(sizeof(int32_t) * (size_t)packet);
     uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 4)
     for (int64_t pk = 0; pk < npk; ++pk) {
@@ -451,33 +472,61 @@ int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* ray
         }
       }
       int next_node = 0, next_leaf = 0;
+      int step = 1;
+      if (steps && step_cap > 0) {
+        uint32_t act = (uint32_t)(node_rays + leaf_rays);
+        uint32_t* rec = steps + (size_t)pk * (size_t)step_cap * 5;
+        rec[0] = root_leaf ? 0u : act;
+        rec[1] = root_leaf ? 0u : 1u;
+        rec[2] = root_leaf ? act : 0u;
+        rec[3] = root_leaf ? (act ? 1u : 0u) : 0u;
+        rec[4] = (uint32_t)wide - act;
+      }
       while (node_rays != 0 || leaf_rays != 0) {
+        uint32_t term = 0, un = 0, ul = 0;
         for (int i = 0; i < node_rays; ++i) {
           int j = cur[i];
           ostate_t* s = &st[j];
           int32_t* stk = stacks + (size_t)j * cap;
           int32_t id = stk[--sps[j]];
+          ids[i] = id;
           node_visit(b, (uint32_t)id, s, stk, &sps[j], 1, NULL);
           if (sps[j] >= cap - 32) rc = 4;
           if (sps[j] != 0) {
             if (stk[sps[j] - 1] >= 0) nxt[next_node++] = (uint16_t)j;
             else nxt[wide - 1 - (next_leaf++)] = (uint16_t)j;
+          } else {
+            term++;
           }
         }
+        if (steps) un = distinct(ids, node_rays);
         for (int i = 0; i < leaf_rays; ++i) {
           int j = cur[wide - 1 - i];
           ostate_t* s = &st[j];
           int32_t* stk = stacks + (size_t)j * cap;
           int32_t id = -stk[--sps[j]];
+          ids[i] = id;
           if (leaf_visit(b, (uint32_t)id, s)) {
             s->hit = 1;
-            if (shadow) { sps[j] = 0; continue; }
+            if (shadow) { sps[j] = 0; term++; continue; }
           }
           if (sps[j] != 0) {
             if (stk[sps[j] - 1] >= 0) nxt[next_node++] = (uint16_t)j;
             else nxt[wide - 1 - (next_leaf++)] = (uint16_t)j;
+          } else {
+            term++;
           }
         }
+        if (steps) ul = distinct(ids, leaf_rays);
+        if (steps && step < step_cap) {
+          uint32_t* rec = steps + ((size_t)pk * (size_t)step_cap + (size_t)step) * 5;
+          rec[0] = (uint32_t)node_rays;
+          rec[1] = un;
+          rec[2] = (uint32_t)leaf_rays;
+          rec[3] = ul;
+          rec[4] = term;
+        }
+        ++step;
         leaf_rays = next_leaf;
         next_leaf = 0;
         node_rays = next_node;
@@ -489,15 +538,30 @@ int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* ray
         finish(b, &st[j], hits ? hits + i : NULL, occluded ? occluded + i : NULL);
         if (ctrs) ctrs[i] = st[j].c;
       }
+      if (step_count) step_count[pk] = (uint32_t)step;
     }
     if (hist) {
 #pragma omp critical
       for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
       free(h);
     }
-    free(stacks); free(sps); free(st); free(w1); free(w2);
+    free(stacks); free(sps); free(st); free(w1); free(w2); free(ids);
   }
   return rc;
+}
+
+int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* rays, uint64_t n,
+                                     int shadow, int packet, ohit_t* hits, uint8_t* occluded,
+                                     octr_t* ctrs, uint64_t* hist) {
+  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, 0, NULL, NULL);
+}
+
+int oracle_trace_instrumented_stream_steps(const oracle_compact_t* b, const float* rays,
+                                           uint64_t n, int shadow, int packet, ohit_t* hits,
+                                           uint8_t* occluded, octr_t* ctrs, uint64_t* hist,
+                                           int step_cap, uint32_t* steps, uint32_t* step_count) {
+  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, step_cap, steps,
+                     step_count);
 }
 
 /* ------------------------------------------------------------ fast path -- */

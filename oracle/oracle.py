@@ -44,6 +44,10 @@ def lib() -> C.CDLL:
             L.oracle_trace_instrumented_stream.restype = C.c_int
             L.oracle_trace_instrumented_stream.argtypes = [C.POINTER(_Compact), _P, C.c_uint64,
                                                            C.c_int, C.c_int, _P, _P, _P, _P]
+            L.oracle_trace_instrumented_stream_steps.restype = C.c_int
+            L.oracle_trace_instrumented_stream_steps.argtypes = [
+                C.POINTER(_Compact), _P, C.c_uint64, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int,
+                _P, _P]
             L.oracle_trace_fast.restype = C.c_int
             L.oracle_trace_fast.argtypes = [C.POINTER(_Fast), C.POINTER(_Compact), _P, C.c_uint64,
                                             C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
@@ -128,6 +132,31 @@ def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: b
         raise RuntimeError(f"oracle error {rc}")
     return {"hits": hits, "occluded": occ, "leaf_index": li, "tri_index": ti, "counters": ctr,
             "depth_hist": hist}
+
+
+def trace_instrumented_steps(view: CompactView, rays: np.ndarray, shadow: bool, packet: int,
+                             step_cap: int) -> dict:
+    """intersectWideAlternative over packets of ``packet`` rays with the
+    per-step workgroup data (bvh_oracle.c: stream_impl): ``steps`` [packets,
+    step_cap, 5] (node work, unique nodes, leaf work, unique leaves,
+    terminations) and ``step_count`` [packets], plus hits / occlusion and
+    counters."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = rays.shape[0]
+    npk = -(-n // packet)
+    hits = None if shadow else np.zeros((n, 4), np.float32)
+    occ = np.zeros(n, np.uint8) if shadow else None
+    ctr = np.zeros((n, 8), np.uint32)
+    hist = np.zeros((2, 64), np.uint64)
+    steps = np.zeros((npk, step_cap, 5), np.uint32)
+    count = np.zeros(npk, np.uint32)
+    rc = lib().oracle_trace_instrumented_stream_steps(
+        C.byref(view.c), _p(rays), n, int(shadow), packet, _p(hits), _p(occ), _p(ctr), _p(hist),
+        step_cap, _p(steps), _p(count))
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist, "steps": steps,
+            "step_count": count}
 
 
 def fp64_pairs(rays: np.ndarray, tri9: np.ndarray, normalise: bool) -> np.ndarray:

@@ -248,6 +248,46 @@ def test_non_finite_and_extreme_rays(profile):
     scene.status()
 
 
+@pytest.mark.parametrize("kind,n,l", [("terrain", 4, 4), ("clutter120", 8, 4),
+                                      ("clutter120", 16, 16)])
+def test_stream_step_log(kind, n, l):
+    """bvhgpu_trace_steps: per packet and step the node work, unique nodes,
+    leaf work, unique leaves and terminations of intersectWideAlternative
+    equal the oracle's, for primary and shadow rays (inactive rays, a ragged
+    last packet, a step log shorter than the traversal)."""
+    tris, b, cv = TS.bvh(kind, n, l)
+    rays = (TS.terrain_case()[1] if kind == "terrain" else TS.clutter_rays(tris))[:-77]
+    scene = pkg.Scene(b)
+    prims = pkg.hit_prims(scene.trace(dev(rays))["hits"].cpu().numpy())
+    sh, _ = TS.secondary(tris, rays, prims, LIGHT)
+    cap = 400
+    for shadow, r in ((False, rays), (True, sh)):
+        ref = O.trace_instrumented_steps(cv, r, shadow, 256, cap)
+        assert int(ref["step_count"].max()) < cap
+        got = scene.trace(dev(r), kind="any" if shadow else "closest", scheme="stream",
+                          counters=True, depth_hist=True, steps=cap)
+        assert np.array_equal(got["step_count"].cpu().numpy().astype(np.uint32),
+                              ref["step_count"])
+        assert np.array_equal(got["step_stats"].cpu().numpy().astype(np.uint32), ref["steps"])
+        assert np.array_equal(got["counters"].cpu().numpy().astype(np.uint32)[:, :7],
+                              ref["counters"][:, :7])
+        if shadow:
+            assert np.array_equal(got["occluded"].cpu().numpy(), ref["occluded"])
+        else:
+            assert np.array_equal(bits(got["hits"].cpu().numpy()), bits(ref["hits"]))
+        short = scene.trace(dev(r), kind="any" if shadow else "closest", scheme="stream",
+                            counters=True, steps=3)
+        assert np.array_equal(short["step_count"].cpu().numpy().astype(np.uint32),
+                              ref["step_count"])
+        assert np.array_equal(short["step_stats"].cpu().numpy().astype(np.uint32),
+                              ref["steps"][:, :3])
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace(dev(rays), scheme="per_ray", counters=True, steps=8)
+    with pytest.raises(pkg.BvhgpuError):
+        scene.trace(dev(rays), scheme="stream", steps=8)
+    scene.status()
+
+
 @pytest.mark.parametrize("n", [1, 31, 127, 129, 255, 257, 1000])
 def test_ragged_ray_counts(n, terrain):
     tris, b, cv, rays, scene = terrain
