@@ -178,3 +178,117 @@ def write_workgroup_whisker(path: str, name: str, problem: str, camera_name: str
                 fh.write(f"{r[0]}, {r[1]}, {r[2]}, {_fmt(r[3])}, {_fmt(r[4])}\n")
         out.append(fn)
     return out
+
+
+def _f32(x) -> np.float32:
+    return np.float32(x)
+
+
+def write_workgroup_data(path: str, name: str, problem: str, camera_name: str, workgroup: int,
+                         wide_alternative: int, n_groups: int, primary_steps, primary_step_count,
+                         secondary_steps, secondary_step_count, primary_counters,
+                         secondary_counters) -> list[str]:
+    """Writes ``WorkGroupSize_<wg>_Version_<v>/<name><problem><camera>_
+    WorkGroupData.txt`` and ``..._WorkGroupUniqueWork.txt`` like
+    CameraData::workGroupAnalysisPerImage (cameraData.h:809-1105), from the
+    step logs of ``Scene.trace(..., scheme="stream", counters=True,
+    steps=S)`` (``[packets, S, 5]`` and ``[packets]``) and the per-ray
+    counters, for the first ``n_groups`` packets (the reference's
+    (width / workGroupSize) * (height / workGroupSize) full workgroups, which
+    come first when the width is a multiple of the workgroup size).
+
+    The reference's quirks are kept: the step range is the longest primary
+    log (its second size check reads the primary log again), averages are
+    float sums in workgroup order, unique-count averages run over workgroups
+    that touched at least one node (leaf), terminations are averaged over
+    all workgroups and accumulated over steps."""
+    wsq = workgroup * workgroup
+
+    def logs(steps, count):
+        st = np.asarray(_host(steps), np.int64)
+        ct = np.asarray(_host(count), np.int64)
+        if np.any(ct[:n_groups] > st.shape[1]):
+            raise ValueError("step log shorter than a workgroup's traversal: trace with more steps")
+        return st[:n_groups], ct[:n_groups]
+
+    ps, pc = logs(primary_steps, primary_step_count)
+    ss, scnt = logs(secondary_steps, secondary_step_count)
+    max_size = int(pc.max()) if n_groups else 0
+    folder = os.path.join(path, f"WorkGroupSize_{workgroup}_Version_{wide_alternative}")
+    os.makedirs(folder, exist_ok=True)
+    header = ("stepId, avgPrimaryNodeWork, avgPrimaryNodeUnique, avgPrimaryLeafWork, "
+              "avgPrimaryLeafUnique, avgPrimaryRayTermination, primaryNodeWorkMax, "
+              "primaryNodeWorkMin, primaryLeafWorkMax, primaryLeafWorkMin, avgSecondaryNodeWork, "
+              "avgSecondaryNodeUnique, avgSecondaryLeafWork, avgSecondaryLeafUnique, "
+              "avgSecondaryRayTermination, secondaryNodeWorkMax, secondaryNodeWorkMin, "
+              "secondaryLeafWorkMax, secondaryLeafWorkMin")
+    lines = [header]
+    term_prev = [_f32(0), _f32(0)]
+    groups = _f32(n_groups)
+    for j in range(max_size):
+        row = [str(j)]
+        for side, (st, ct) in enumerate(((ps, pc), (ss, scnt))):
+            nw = lw = un = ul = tr = _f32(0)
+            cnt = ucn = ucl = 0
+            umax_n = umax_l = 0
+            umin_n = umin_l = wsq + 1
+            for i in range(n_groups):
+                if ct[i] <= j:
+                    continue
+                cnt += 1
+                rec = st[i, j]
+                nw = _f32(nw + _f32(rec[0]))
+                lw = _f32(lw + _f32(rec[2]))
+                un = _f32(un + _f32(rec[1]))
+                ul = _f32(ul + _f32(rec[3]))
+                tr = _f32(tr + _f32(rec[4]))
+                if rec[1] != 0:
+                    ucn += 1
+                    umax_n, umin_n = max(int(rec[1]), umax_n), min(int(rec[1]), umin_n)
+                if rec[3] != 0:
+                    ucl += 1
+                    umax_l, umin_l = max(int(rec[3]), umax_l), min(int(rec[3]), umin_l)
+            cnt, ucn, ucl = max(cnt, 1), max(ucn, 1), max(ucl, 1)
+            umin_n = 0 if umin_n == wsq + 1 else umin_n
+            umin_l = 0 if umin_l == wsq + 1 else umin_l
+            tr = _f32(tr / groups)
+            if j != 0:
+                tr = _f32(tr + term_prev[side])
+            term_prev[side] = tr
+            row += [_fmt(float(_f32(nw / _f32(cnt)))), _fmt(float(_f32(un / _f32(ucn)))),
+                    _fmt(float(_f32(lw / _f32(cnt)))), _fmt(float(_f32(ul / _f32(ucl)))),
+                    _fmt(float(tr)), str(umax_n), str(umin_n), str(umax_l), str(umin_l)]
+        lines.append(", ".join(row))
+    fn_data = os.path.join(folder, f"{name}{problem}{camera_name}_WorkGroupData.txt")
+    with open(fn_data, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    # Per workgroup: node / leaf visits summed over its rays (with their max
+    # and min) and the unique nodes / leaves summed over its steps.
+    pcn = np.asarray(_host(primary_counters), np.int64).reshape(-1, 8)
+    scn = np.asarray(_host(secondary_counters), np.int64).reshape(-1, 8)
+    lines = ["loadedPrimaryNodes, loadedPrimaryLeafs, loadedPrimaryNodesMax, loadedPrimaryLeafsMax, "
+             "loadedPrimaryNodesMin, loadedPrimaryLeafsMin, loadedSecondaryNodes, "
+             "loadedSecondaryLeafs, loadedSecondaryNodesMax, loadedSecondaryLeafsMax, "
+             "loadedSecondaryNodesMin, loadedSecondaryLeafsMin, loadedWidePrimaryNodes, "
+             "loadedWidePrimaryLeafs, loadedWideSecondaryNodes, loadedWideSecondaryLeafs"]
+    for i in range(n_groups):
+        row = []
+        for c in (pcn, scn):
+            g = c[i * wsq:(i + 1) * wsq]
+            nodes = leaves = _f32(0)
+            for k in range(g.shape[0]):
+                nodes = _f32(nodes + _f32(g[k, 0]))
+                leaves = _f32(leaves + _f32(g[k, 1]))
+            # minima start at 1000 and read 0 when no ray went below it
+            mn = [int(g[:, a].min(initial=1000)) for a in (0, 1)]
+            mn = [0 if m == 1000 else m for m in mn]
+            row += [_fmt(float(nodes)), _fmt(float(leaves)), str(int(g[:, 0].max(initial=0))),
+                    str(int(g[:, 1].max(initial=0))), str(mn[0]), str(mn[1])]
+        for st, ct in ((ps, pc), (ss, scnt)):
+            k = int(ct[i])
+            row += [_fmt(float(int(st[i, :k, 1].sum()))), _fmt(float(int(st[i, :k, 3].sum())))]
+        lines.append(", ".join(row))
+    fn_unique = os.path.join(folder, f"{name}{problem}{camera_name}_WorkGroupUniqueWork.txt")
+    with open(fn_unique, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return [fn_data, fn_unique]

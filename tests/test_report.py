@@ -2,6 +2,7 @@
 analysis script reads (the first number after its key) is present and
 equals the statistic computed from the counters."""
 import numpy as np
+import pytest
 
 from bvhraytracer_gb300 import report as R
 
@@ -76,3 +77,39 @@ def test_whisker_file(tmp_path):
     assert lines[0] == "median, min, max, lowerStdDeviation, upperStdDeviation"
     # groups: [4,2,3,6] -> median 4 (index 2 of sorted 2,3,4,6), [9,10,11,12] -> 11
     assert lines[1].startswith("4, 2, 6, 3.75") and lines[2].startswith("11, 9, 12, 10.5")
+
+
+def test_workgroup_data_files(tmp_path):
+    """_WorkGroupData.txt / _WorkGroupUniqueWork.txt from step logs of two
+    2x2 workgroups, against values worked out by hand from
+    cameraData.h:809-1105 (averages over active workgroups, unique averages
+    over workgroups that touched a node / leaf, terminations averaged over
+    all workgroups and accumulated, step range of the primary logs)."""
+    from bvhraytracer_gb300 import report as R
+    P = np.zeros((2, 4, 5), np.int32)
+    P[0, :3] = [[4, 1, 0, 0, 0], [4, 2, 0, 0, 1], [3, 1, 0, 0, 3]]
+    P[1, :2] = [[4, 1, 0, 0, 0], [0, 0, 4, 3, 4]]
+    S = np.zeros((2, 4, 5), np.int32)
+    S[0, :2] = [[2, 1, 0, 0, 2], [2, 1, 0, 0, 2]]
+    S[1, :4] = [[4, 1, 0, 0, 0], [4, 2, 0, 0, 0], [0, 0, 4, 2, 2], [2, 1, 0, 0, 2]]
+    pc = np.zeros((8, 8), np.int32)
+    pc[:, 0] = [3, 2, 2, 1, 1, 1, 1, 1]
+    pc[:, 1] = [0, 1, 0, 2, 1, 1, 1, 1]
+    sc = np.zeros((8, 8), np.int32)
+    sc[:, 0] = [2, 2, 0, 0, 3, 2, 1, 2]
+    sc[:, 1] = [0, 0, 0, 0, 1, 1, 0, 0]
+    data, unique = R.write_workgroup_data(str(tmp_path), "scene", "_p", "_cam", 2, 1, 2, P,
+                                          np.array([3, 2]), S, np.array([2, 4]), pc, sc)
+    assert data.endswith("WorkGroupSize_2_Version_1/scene_p_cam_WorkGroupData.txt")
+    lines = open(data).read().splitlines()
+    assert lines[0].startswith("stepId, avgPrimaryNodeWork, avgPrimaryNodeUnique")
+    assert lines[1:] == ["0, 4, 1, 0, 0, 0, 1, 1, 0, 0, 3, 1, 0, 0, 1, 1, 1, 0, 0",
+                         "1, 2, 2, 2, 3, 2.5, 2, 2, 3, 3, 3, 1.5, 0, 0, 2, 2, 1, 0, 0",
+                         "2, 3, 1, 0, 0, 4, 1, 1, 0, 0, 0, 0, 4, 2, 3, 0, 0, 2, 2"]
+    lines = open(unique).read().splitlines()
+    assert lines[0].startswith("loadedPrimaryNodes, loadedPrimaryLeafs")
+    assert lines[1:] == ["8, 3, 3, 2, 1, 0, 4, 0, 2, 0, 0, 0, 4, 0, 2, 0",
+                         "4, 4, 1, 1, 1, 1, 8, 2, 3, 1, 1, 0, 1, 3, 4, 2"]
+    with pytest.raises(ValueError):
+        R.write_workgroup_data(str(tmp_path), "s", "", "", 2, 1, 2, P, np.array([5, 2]), S,
+                               np.array([2, 4]), pc, sc)
