@@ -11,6 +11,14 @@ value as the first number after a fixed key) can consume GPU results.
   child fullness = box tests / node visits and average leaf fullness =
   triangle tests / leaf visits); the per-count fullness lines of the
   reference are not written because the kernels do not histogram them.
+* ``WorkGroupSize_<wg>_Version_<v>/...`` — CameraData::workGroupAnalysisPerImage
+  (cameraData.h:660-1105): the primary / secondary whisker plots of the
+  termination steps per workgroup, ``_WorkGroupData.txt`` (per step: average
+  node and leaf work, unique nodes and leaves, accumulated terminations) and
+  ``_WorkGroupUniqueWork.txt`` (per workgroup: node and leaf visits of its
+  rays, unique nodes and leaves summed over its steps), from the stream
+  kernel's step log (``Scene.trace(..., scheme="stream", counters=True,
+  steps=S)``).
 * ``<name><problem>_Perf.txt`` — CameraFast::renderImage's timing summary
   (src/cameraFast.h:147-161) with the device time of the frame. The GPU does
   not time rays and triangle tests separately, so those lines read ``n/a``
