@@ -622,6 +622,17 @@ int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 
 }  // extern "C"
 
+// Host-buffer pipeline: chunks per batch and the largest chunk (Mi rays).
+// Measured on the 1M-triangle frame (20.7M rays in three batches): 4 / 4 Mi
+// 9.24 ms, 8 / 2 Mi 9.54, 8 / 4 Mi 9.55, 3 / 8 Mi 9.37, 2 / 8 Mi 9.75,
+// 16 / 1 Mi 9.68.
+#ifndef BVHGPU_HOST_CHUNKS
+#define BVHGPU_HOST_CHUNKS 4
+#endif
+#ifndef BVHGPU_HOST_CHUNK_MAX
+#define BVHGPU_HOST_CHUNK_MAX 4
+#endif
+
 namespace {
 // One batch of a host-buffer trace: host rays in, host results out.
 struct HostBatch {
@@ -655,15 +666,16 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
       if (e != cudaSuccess) return cuda_error(e, "create pipeline event");
     }
   }
-  // Chunks of an eighth of each batch, between 256 Ki and 2 Mi rays: small
+  // Chunks of a quarter of each batch, between 256 Ki and 4 Mi rays: small
   // enough that the first copy in and the last copy out (the parts that do
-  // not overlap a trace) are short, large enough to fill the GPU.
+  // not overlap a trace) are short, large enough to fill the GPU and keep
+  // the per-chunk launch tails and reorder passes few.
   std::vector<uint64_t> chunk(nb);
   uint64_t max_chunk = 0;
   for (int k = 0; k < nb; ++k) {
-    uint64_t c = (b[k].n + 7) / 8;
+    uint64_t c = (b[k].n + BVHGPU_HOST_CHUNKS - 1) / BVHGPU_HOST_CHUNKS;
     c = std::max<uint64_t>(c, 256ull << 10);
-    c = std::min<uint64_t>(c, 2ull << 20);
+    c = std::min<uint64_t>(c, (uint64_t)BVHGPU_HOST_CHUNK_MAX << 20);
     c = std::min<uint64_t>(c, b[k].n);
     chunk[k] = c;
     max_chunk = std::max(max_chunk, c);
