@@ -26,6 +26,9 @@
  *                             (fastNodeManager.h:1328-1493, 835-1230) and the
  *                             instrumented CompactNodeManager::intersectImmediately /
  *                             intersectWideAlternative (compactNode.cpp:604-814, 357-601)
+ *   bvhgpu_trace_steps        intersectWideAlternative with the per-step data of
+ *                             CameraData's workgroup analysis (compactNode.cpp:357-601,
+ *                             cameraData.h:660-1105)
  *   bvhgpu_trace_host[_batches] the same, on host buffers (copies in the call)
  *   bvhgpu_adjoint[_vertices|_hits] no reference counterpart: reverse pass of
  *                             triIntersect{L}'s Moller-Trumbore (rayTracerTemplate.ispc:35-76)
