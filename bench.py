@@ -695,19 +695,22 @@ def run_batch(a):
             "workload": f"{a.scenes} scenes in one persistent launch, triangles log-uniform "
                         f"1k-500k, rays log-uniform 4k-2M (primary:shadow:AO 1:1:4)",
             "triangles_total": n_tris, "rays_per_step": n_rays, "jobs": len(jobs_plain),
-            "method": "bvhgpu_trace_jobs (speculative any-hit policy, AO jobs grouped into "
+            "method": "bvhgpu_trace_jobs (one persistent launch per ray kind over all scenes; "
+                      "speculative any-hit policy, AO jobs grouped into "
                       f"6x{a.job_reorder}x{a.job_reorder} direction bins"
                       + (", child-index push order" if a.job_any_order else "")
                       + ") in a CUDA graph"
                       if a.job_reorder else
-                      "bvhgpu_trace_jobs (speculative any-hit policy) in a CUDA graph",
+                      "bvhgpu_trace_jobs (one persistent launch per ray kind over all scenes; "
+                      "speculative any-hit policy) in a CUDA graph",
             "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,
             "ms_sequential_plain_launches": ms_seq,
             "speedup_vs_sequential": ms_seq / ms_graph, "results_identical": bool(same),
             "autotuned_nl": bool(a.tune_nl), "scenes": scenes, "setup_s": round(setup_s, 1),
         },
-        # one batched launch per step, plus the four segmented reorder passes
-        "clocks": clocks, "gpu_launches": a.steps * (5 if a.job_reorder else 1),
+        # per step one batched launch per ray kind (closest-hit jobs, any-hit
+        # jobs), plus the four segmented reorder passes
+        "clocks": clocks, "gpu_launches": a.steps * (6 if a.job_reorder else 2),
     }
     print(json.dumps(line))
 

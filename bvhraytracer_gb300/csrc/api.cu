@@ -788,7 +788,8 @@ int bvhgpu_trace_host_batches(bvhgpu_scene_t s, const bvhgpu_host_batch_t* batch
 
 namespace bvhgpu {
 namespace dev {
-cudaError_t launch_batched(const JobTable& t, int profile, int sm_count, cudaStream_t s);
+cudaError_t launch_batched(const JobTable& t, int profile, int kmode, int sm_count,
+                           cudaStream_t s);
 cudaError_t launch_aabb_calls(int n, const float* bounds, const uint32_t* offset,
                               const float* fastrays, float* distances, uint8_t* result,
                               uint64_t count, cudaStream_t s);
@@ -847,6 +848,10 @@ int bvhgpu_tri_any_hit(int32_t l, const float* tri, const uint32_t* tri_id,
 }  // extern "C"
 
 extern "C" {
+
+#ifndef BVHGPU_JOBS_SPLIT
+#define BVHGPU_JOBS_SPLIT 1
+#endif
 
 int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_trace_opts_t* opts,
                       void* stream) {
@@ -951,7 +956,38 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
       return cuda_error(e, "job reorder");
     }
   }
-  e = dev::launch_batched(*t, cfg.profile, sms, st);
+  // Jobs of one ray kind run in a kernel compiled for that kind. Mixed
+  // batches are split into a closest-hit and an any-hit launch (same
+  // stream), unless BVHGPU_JOBS_SPLIT is 0 (one launch, kind per lane).
+  int kinds = 0;
+  for (int i = 0; i < nj; ++i) kinds |= t->jobs[i].kind == BVHGPU_ANY ? 2 : 1;
+  if (kinds != 3) {
+    e = dev::launch_batched(*t, cfg.profile, kinds, sms, st);
+  } else if (!BVHGPU_JOBS_SPLIT) {
+    e = dev::launch_batched(*t, cfg.profile, 0, sms, st);
+  } else {
+    std::unique_ptr<dev::JobTable> part(new (std::nothrow) dev::JobTable());
+    if (!part) {
+      e = cudaErrorMemoryAllocation;
+    } else {
+      for (int kind = BVHGPU_CLOSEST; kind <= BVHGPU_ANY && e == cudaSuccess; ++kind) {
+        *part = *t;
+        int m = 0;
+        uint64_t begin = 0;
+        for (int i = 0; i < nj; ++i) {
+          if (t->jobs[i].kind != kind) continue;
+          part->jobs[m] = t->jobs[i];
+          part->jobs[m].ray_begin = begin;
+          begin += t->jobs[i].n;
+          ++m;
+        }
+        part->n_jobs = m;
+        part->total = begin;
+        part->head = first->d_queue + (first->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
+        e = dev::launch_batched(*part, cfg.profile, kind == BVHGPU_ANY ? 2 : 1, sms, st);
+      }
+    }
+  }
   if (scratch) {
     cudaError_t f = cudaFreeAsync(scratch, st);
     if (e == cudaSuccess) e = f;

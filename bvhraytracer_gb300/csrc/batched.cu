@@ -8,11 +8,16 @@ namespace dev {
 
 size_t batched_param_bytes() { return sizeof(JobTable); }
 
-cudaError_t launch_batched(const JobTable& t, int profile, int sm_count, cudaStream_t s) {
+cudaError_t launch_batched(const JobTable& t, int profile, int kmode, int sm_count,
+                           cudaStream_t s) {
   const int bs = 128;
   const size_t smem = (size_t)t.stack_cap * bs * 4;
-  auto k = profile == BVHGPU_PROFILE_FAST ? trace_batched_kernel<BVHGPU_PROFILE_FAST>
-                                          : trace_batched_kernel<BVHGPU_PROFILE_INSTRUMENTED>;
+  constexpr int F = BVHGPU_PROFILE_FAST, I = BVHGPU_PROFILE_INSTRUMENTED;
+  void (*k)(const JobTable) =
+      profile == F ? (kmode == 1 ? trace_batched_kernel<F, 1>
+                                 : kmode == 2 ? trace_batched_kernel<F, 2> : trace_batched_kernel<F, 0>)
+                   : (kmode == 1 ? trace_batched_kernel<I, 1>
+                                 : kmode == 2 ? trace_batched_kernel<I, 2> : trace_batched_kernel<I, 0>);
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024)
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

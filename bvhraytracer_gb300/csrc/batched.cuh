@@ -75,7 +75,9 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
 #ifndef BVHGPU_BATCHED_MIN_BLOCKS
 #define BVHGPU_BATCHED_MIN_BLOCKS 5
 #endif
-template <int PROFILE>
+// KMODE 0: every lane takes its job's ray kind; 1: closest-hit jobs only;
+// 2: any-hit jobs only (the other kind's code is compiled out).
+template <int PROFILE, int KMODE>
 __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
     trace_batched_kernel(const __grid_constant__ JobTable t) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -97,7 +99,8 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
   SceneDev sc;
   sc.leaf_depth = nullptr;
   sc.top_nodes = 0;
-  int nm = 8, fmt = 0, kind = 0;
+  int nm = 8, fmt = 0;
+  int kind = KMODE == 2 ? BVHGPU_ANY : BVHGPU_CLOSEST;
   bool drained = false;
   uint32_t postponed = NONE;
 
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
           sc.any_index_order = J.any_index_order;
           nm = J.nm;
           fmt = J.fmt;
-          kind = J.kind;
+          if (KMODE == 0) kind = J.kind;
           const bvhgpu_ray_t in = load_ray(J.rays, local);
           best = Best();
           hit = false;

@@ -32,7 +32,7 @@
  *   bvhgpu_trace_host[_batches] the same, on host buffers (copies in the call)
  *   bvhgpu_adjoint[_vertices|_hits] no reference counterpart: reverse pass of
  *                             triIntersect{L}'s Moller-Trumbore (rayTracerTemplate.ispc:35-76)
- *   bvhgpu_trace_jobs         many scenes in one persistent launch (the refill
+ *   bvhgpu_trace_jobs         many scenes in one persistent launch per ray kind (the refill
  *                             structure, fastNodeManager.h:92-156, across scenes)
  *   bvhgpu_camera_rays        Camera::getRayTargetPosition + FastRay (camera.h:82-98)
  *   bvhgpu_secondary_rays     getSurfaceNormalPosition + shadow / AO set-up
@@ -284,9 +284,11 @@ int bvhgpu_trace_host_batches(bvhgpu_scene_t scene, const bvhgpu_host_batch_t* b
 /* ---- many scenes in one launch ---------------------------------------- */
 /* A job: one ray batch traced in one scene. bvhgpu_trace_jobs traces up to
  * BVHGPU_MAX_JOBS jobs (scenes of any N, L and node format, closest or any
- * hit, uneven sizes) in ONE persistent launch that pulls rays from a global
- * queue spanning all jobs (the GPU form of the reference's workgroup refill,
- * fastNodeManager.h:92-156, 277-450, extended across scenes). Results per ray
+ * hit, uneven sizes) in one persistent launch per ray kind (closest-hit jobs,
+ * then any-hit jobs, each kernel compiled for its kind) that pulls rays from
+ * a global queue spanning all its jobs (the GPU form of the reference's
+ * workgroup refill, fastNodeManager.h:92-156, 277-450, extended across
+ * scenes). Results per ray
  * equal bvhgpu_trace's. All scenes must live on the stream's device; the
  * options' profile and policy (0 or 2) apply to every job. Stream-ordered, no
  * synchronisation (so it can be recorded in a CUDA graph); no allocation
