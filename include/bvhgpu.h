@@ -284,9 +284,10 @@ int bvhgpu_trace_host_batches(bvhgpu_scene_t scene, const bvhgpu_host_batch_t* b
 /* ---- many scenes in one launch ---------------------------------------- */
 /* A job: one ray batch traced in one scene. bvhgpu_trace_jobs traces up to
  * BVHGPU_MAX_JOBS jobs (scenes of any N, L and node format, closest or any
- * hit, uneven sizes) in one persistent launch per ray kind (closest-hit jobs,
- * then any-hit jobs, each kernel compiled for its kind) that pulls rays from
- * a global queue spanning all its jobs (the GPU form of the reference's
+ * hit, uneven sizes) in one persistent launch per group of jobs with the same
+ * ray kind, node width and node format (each kernel compiled for its kind)
+ * that pulls rays from a global queue spanning the group's jobs, scenes of
+ * any size mixed (the GPU form of the reference's
  * workgroup refill, fastNodeManager.h:92-156, 277-450, extended across
  * scenes). Results per ray
  * equal bvhgpu_trace's. All scenes must live on the stream's device; the
