@@ -70,8 +70,8 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
 
 // Five blocks per SM (up to 102 registers per thread): the kernel carries
 // every node width, format and ray kind, and at six blocks (80 registers)
-// it spills more (batch of 64 scenes: 11.23 ms at six blocks, 10.96 at five,
-// 11.70 at four).
+// it spills more (batch of 64 scenes, one launch per ray kind: 7.23 ms at
+// six blocks, 6.11 at five, 6.87 at four).
 #ifndef BVHGPU_BATCHED_MIN_BLOCKS
 #define BVHGPU_BATCHED_MIN_BLOCKS 5
 #endif
