@@ -440,7 +440,7 @@ def ao_factor(occluded, samples: int, stream=None):
 
 def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: int = 16,
                stream=None) -> None:
-    """Traces many (scene, rays) jobs in one persistent launch.
+    """Traces many (scene, rays) jobs in one persistent launch per ray kind.
 
     ``jobs``: list of ``(scene, rays, kind, out)``, ``(scene, rays, kind,
     out, reorder)`` or ``(scene, rays, kind, out, reorder, any_order)`` with
