@@ -391,30 +391,34 @@ def run_ours(a):
                           a.branching, a.leaf, stats[0], sec)
         # Workgroup analysis (CameraData::workGroupAnalysisPerImage) of the
         # ray-stream scheme over 16 x 16 packets: primary and shadow rays.
-        logs = []
         sh_px = d_shadow  # one shadow ray per pixel, inactive where the primary missed
         if d_shadow.shape[0] != d_primary.shape[0]:
             hit_px = torch.from_numpy(pkg.hit_prims(hits0.cpu().numpy()) >= 0).to(dev)
             sh_px = torch.full_like(d_primary, float("nan"))
             sh_px[hit_px] = d_shadow
-        for r, kind in ((d_primary, "closest"), (sh_px, "any")):
-            cap = 1024
-            while True:
-                t = plain.trace(r, kind=kind, scheme="stream", counters=True, steps=cap,
-                                profile=a.profile)
-                need = int(t["step_count"].max().item())
-                if need <= cap:
-                    break
-                cap = need
-            logs.append(t)
         wg_name, wg_problem = f"clutter{a.objects}", f"_b{a.branching}_l{a.leaf}"
-        report.write_workgroup_whisker(a.report, wg_name, wg_problem, "", 16, 1,
-                                       logs[0]["counters"], logs[1]["counters"])
-        report.write_workgroup_data(a.report, wg_name, wg_problem, "", 16, 1,
-                                    (a.width // 16) * (a.height // 16),
-                                    logs[0]["step_stats"], logs[0]["step_count"],
-                                    logs[1]["step_stats"], logs[1]["step_count"],
-                                    logs[0]["counters"], logs[1]["counters"])
+        for version in (1, 0):  # intersectWideAlternative, intersectWide
+            logs = []
+            for r, kind in ((d_primary, "closest"), (sh_px, "any")):
+                cap = 1024
+                while True:
+                    t = plain.trace(r, kind=kind, scheme="stream", counters=True, steps=cap,
+                                    wide_alternative=bool(version), profile=a.profile)
+                    need = int(t["step_count"].max().item())
+                    if need <= cap:
+                        break
+                    cap = need
+                logs.append(t)
+            n_groups = (a.width // 16) * (a.height // 16)
+            report.write_workgroup_whisker(
+                a.report, wg_name, wg_problem, "", 16, version,
+                (logs[0]["step_stats"], logs[0]["step_count"]),
+                (logs[1]["step_stats"], logs[1]["step_count"]), n_groups)
+            report.write_workgroup_data(a.report, wg_name, wg_problem, "", 16, version,
+                                        (a.width // 16) * (a.height // 16),
+                                        logs[0]["step_stats"], logs[0]["step_count"],
+                                        logs[1]["step_stats"], logs[1]["step_count"],
+                                        logs[0]["counters"], logs[1]["counters"])
     setup_s = time.time() - t_setup
 
     for _ in range(a.warmup):

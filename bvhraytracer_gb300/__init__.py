@@ -195,8 +195,8 @@ class Scene:
               profile: str = "instrumented", workgroup: int = 16, block: int = 128,
               policy: int = 0, refill: int = 0, counters: bool = False,
               depth_hist: bool = False, save_distance: bool = False, reorder: int = 0,
-              stack: str = "shared", any_order: bool = False, steps: int = 0, out=None,
-              stream=None) -> dict:
+              stack: str = "shared", any_order: bool = False, steps: int = 0,
+              wide_alternative: bool = True, out=None, stream=None) -> dict:
         """Traces device rays (torch CUDA tensor ``[n, 8]`` float32).
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
@@ -213,7 +213,8 @@ class Scene:
         with ``counters``): also returns ``"step_stats"`` ``[packets, S, 5]``
         (node work, unique nodes, leaf work, unique leaves, terminations per
         step, step 0 the set-up) and ``"step_count"`` ``[packets]``
-        (bvhgpu_trace_steps).
+        (bvhgpu_trace_steps), of intersectWideAlternative's schedule or,
+        with ``wide_alternative=False``, intersectWide's.
         """
         import torch
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[-1] == 8
@@ -246,7 +247,8 @@ class Scene:
             res["step_stats"] = torch.zeros((packets, steps, 5), dtype=torch.int32, device=dev)
             res["step_count"] = torch.zeros(packets, dtype=torch.int32, device=dev)
             N.check(N.lib().bvhgpu_trace_steps(self._h, _ptr(rays), n, C.byref(o), hp, op, cp, hh,
-                                               steps, _ptr(res["step_stats"]),
+                                               steps, int(wide_alternative),
+                                               _ptr(res["step_stats"]),
                                                _ptr(res["step_count"]),
                                                C.c_void_p(s.cuda_stream)))
             return res

@@ -129,7 +129,7 @@ _SIGS = {
     "bvhgpu_trace_host_batches": (C.c_int, [_P, C.POINTER(HostBatch), C.c_int32, _P]),
     "bvhgpu_gang_size": (C.c_int, []),
     "bvhgpu_trace_steps": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P, _P,
-                                     C.c_int32, _P, _P, _P]),
+                                     C.c_int32, C.c_int32, _P, _P, _P]),
     "bvhgpu_aabb_intersect": (C.c_int, [C.c_int32, _P, _P, _P, _P, _P, C.c_uint64, _P]),
     "bvhgpu_tri_intersect": (C.c_int, [C.c_int32, C.c_int32, _P, _P, _P, _P, C.c_uint64, _P]),
     "bvhgpu_tri_any_hit": (C.c_int, [C.c_int32, _P, _P, _P, _P, C.c_uint64, _P]),

@@ -567,7 +567,8 @@ int bvhgpu_scene_bytes(bvhgpu_scene_t s, uint64_t* node_bytes, uint64_t* leaf_by
 static int trace_device(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
                         const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                         uint32_t* counters, uint64_t* depth_hist, int32_t step_cap,
-                        uint32_t* step_stats, uint32_t* step_count, void* stream) {
+                        int32_t wide_alternative, uint32_t* step_stats, uint32_t* step_count,
+                        void* stream) {
   if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
   dev::LaunchCfg cfg;
   int rc = check_opts(opts, cfg);
@@ -594,6 +595,7 @@ static int trace_device(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
     a.step_stats = step_stats;
     a.step_count = step_count;
     a.step_cap = step_cap;
+    a.step_wide = wide_alternative == 0;
     if (dev::stream_smem_bytes(cfg.packet, a.stack_cap, true, true) > 227 * 1024)
       return set_error(BVHGPU_ERR_UNSUPPORTED, "stream packet with step log does not fit shared memory");
   }
@@ -606,18 +608,19 @@ static int trace_device(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 int bvhgpu_trace(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
                  const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                  uint32_t* counters, uint64_t* depth_hist, void* stream) {
-  return trace_device(s, rays, n, opts, hits, occluded, counters, depth_hist, 0, nullptr, nullptr,
-                      stream);
+  return trace_device(s, rays, n, opts, hits, occluded, counters, depth_hist, 0, 1, nullptr,
+                      nullptr, stream);
 }
 
 int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
                        const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                        uint32_t* counters, uint64_t* depth_hist, int32_t step_cap,
-                       uint32_t* step_stats, uint32_t* step_count, void* stream) {
+                       int32_t wide_alternative, uint32_t* step_stats, uint32_t* step_count,
+                       void* stream) {
   if (n > 0 && (!step_stats || !step_count))
     return set_error(BVHGPU_ERR_BAD_ARG, "step log: null step_stats or step_count");
   return trace_device(s, rays, n, opts, hits, occluded, counters, depth_hist, step_cap,
-                      step_stats, step_count, stream);
+                      wide_alternative, step_stats, step_count, stream);
 }
 
 }  // extern "C"

@@ -64,6 +64,9 @@ struct TraceArgs {
   uint32_t* step_stats = nullptr;
   uint32_t* step_count = nullptr;
   int step_cap = 0;
+  // Step log of intersectWide's schedule (a node visit followed by a leaf
+  // visit counts as one step) instead of intersectWideAlternative's.
+  bool step_wide = false;
 };
 
 BVHGPU_DEV uint64_t out_slot(const TraceArgs& a, uint64_t rid) {
@@ -637,7 +640,7 @@ BVHGPU_DEV Ray unpack_ray(const StreamRay& s) {
 
 struct StreamShared {
   int node_rays, leaf_rays, next_node, next_leaf;
-  int unique_nodes, unique_leaves, terminations, pad;  // step log
+  int unique_nodes, unique_leaves, terminations, extra_leaf_work;  // step log
 };
 
 // Shared-memory bytes of the stream kernel for a packet of p rays (with the
@@ -707,6 +710,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
   if (tid == 0) {
     ctl->node_rays = 0; ctl->leaf_rays = 0; ctl->next_node = 0; ctl->next_leaf = 0;
     ctl->unique_nodes = 0; ctl->unique_leaves = 0; ctl->terminations = 0;
+    ctl->extra_leaf_work = 0;
   }
   __syncthreads();
   // Set-up: active rays go to the node part of list 0 (the root entry is an
@@ -785,26 +789,15 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       const uint32_t e = stacks[sp * P + ray];
       if (log && set_insert(set, 2 * P, e))
         atomicAdd(is_node ? &ctl->unique_nodes : &ctl->unique_leaves, 1);
-      if (is_node) {
-        int depth;
-        if (!node_step<N, PROFILE, KIND, COUNT, kFmtFP32>(sc, e, nullptr, 0u, r, tmax, stacks + ray,
-                                                          P, sp, cap, ctr, depth)) {
-          record_error(sc.status, kDevErrStackOverflow);
-          best_leaf[ray] = 0xFFFFFFFFu;
-          misc = 0xFF;
-          done = true;
-          sp = 0;
-        }
-        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
-      } else {
+      auto leaf_visit = [&](uint32_t le) {
         if (COUNT && a.depth_hist)
-          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[le & kLeafIndexMask], 63), 1ull);
         Best best;
         best.leaf = best_leaf[ray];
         best.lane = (int)(int8_t)(misc & 0xFF);
         best.u = best_u[ray];
         best.v = best_v[ray];
-        bool h = leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
+        bool h = leaf_step<PROFILE, KIND, COUNT>(sc, le, r, tmax, best, ctr);
         if (h) {
           misc |= (int32_t)0x80000000;
           if (KIND == BVHGPU_ANY) done = true;
@@ -816,6 +809,30 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
             best_v[ray] = best.v;
           }
         }
+      };
+      if (is_node) {
+        int depth;
+        if (!node_step<N, PROFILE, KIND, COUNT, kFmtFP32>(sc, e, nullptr, 0u, r, tmax, stacks + ray,
+                                                          P, sp, cap, ctr, depth)) {
+          record_error(sc.status, kDevErrStackOverflow);
+          best_leaf[ray] = 0xFFFFFFFFu;
+          misc = 0xFF;
+          done = true;
+          sp = 0;
+        }
+        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+        // intersectWide's schedule (compactNode.cpp:118-356, step log only):
+        // a ray whose next entry is a leaf visits it in the same step.
+        if (log && a.step_wide && !done && sp > 0 && (stacks[(sp - 1) * P + ray] & kLeafBit)) {
+          ctrs[6 * P + ray] = max(ctrs[6 * P + ray], (uint32_t)sp);
+          --sp;
+          const uint32_t le = stacks[sp * P + ray];
+          if (set_insert(set, 2 * P, le)) atomicAdd(&ctl->unique_leaves, 1);
+          atomicAdd(&ctl->extra_leaf_work, 1);
+          leaf_visit(le);
+        }
+      } else {
+        leaf_visit(e);
       }
       if (COUNT) {
         ctrs[0 * P + ray] += ctr.node_visits;
@@ -858,13 +875,14 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
         uint32_t* rec = a.step_stats + ((size_t)blockIdx.x * a.step_cap + step) * 5;
         rec[0] = (uint32_t)node_rays;
         rec[1] = (uint32_t)ctl->unique_nodes;
-        rec[2] = (uint32_t)leaf_rays;
+        rec[2] = (uint32_t)(leaf_rays + ctl->extra_leaf_work);
         rec[3] = (uint32_t)ctl->unique_leaves;
         rec[4] = (uint32_t)ctl->terminations;
       }
       ctl->unique_nodes = 0;
       ctl->unique_leaves = 0;
       ctl->terminations = 0;
+      ctl->extra_leaf_work = 0;
       ctl->node_rays = ctl->next_node;
       ctl->leaf_rays = ctl->next_leaf;
       ctl->next_node = 0;

@@ -167,18 +167,39 @@ def _whisker_rows(steps: np.ndarray, group: int):
     return rows
 
 
+def termination_steps_from_log(step_stats, step_count, n_groups: int) -> np.ndarray:
+    """Termination step of every ray of the first ``n_groups`` packets from
+    the stream kernel's step log: step s repeated terminations[s] times per
+    packet, as workGroupAnalysisPerImage expands terminationsPerStep
+    (cameraData.h:727-741). Valid for either wide schedule."""
+    st = np.asarray(_host(step_stats), np.int64)
+    ct = np.asarray(_host(step_count), np.int64)
+    out = []
+    for i in range(n_groups):
+        k = int(ct[i])
+        if k > st.shape[1]:
+            raise ValueError("step log shorter than a workgroup's traversal: trace with more steps")
+        out.append(np.repeat(np.arange(k), st[i, :k, 4]))
+    return np.concatenate(out) if out else np.zeros(0, np.int64)
+
+
 def write_workgroup_whisker(path: str, name: str, problem: str, camera_name: str,
-                            workgroup: int, wide_alternative: int, primary_counters,
-                            secondary_counters) -> list[str]:
+                            workgroup: int, wide_alternative: int, primary, secondary,
+                            n_groups: int = 0) -> list[str]:
     """Writes ``WorkGroupSize_<wg>_Version_<v>/<name><problem><camera>_
-    {Primary,Secondary}WorkGroupWiskerPlot.txt`` from per-ray counters of rays
-    in workgroup order (workgroup^2 consecutive rays per workgroup, one
-    secondary ray per pixel)."""
+    {Primary,Secondary}WorkGroupWiskerPlot.txt``. ``primary`` / ``secondary``:
+    per-ray counters of rays in workgroup order (workgroup^2 consecutive rays
+    per workgroup, one secondary ray per pixel; a ray terminates at step node
+    visits + leaf visits, the intersectWideAlternative schedule), or a
+    ``(step_stats, step_count)`` step log of either schedule with the number
+    of workgroups ``n_groups``."""
     folder = os.path.join(path, f"WorkGroupSize_{workgroup}_Version_{wide_alternative}")
     os.makedirs(folder, exist_ok=True)
     out = []
-    for kind, c in (("Primary", primary_counters), ("Secondary", secondary_counters)):
-        rows = _whisker_rows(termination_steps(c), workgroup * workgroup)
+    for kind, c in (("Primary", primary), ("Secondary", secondary)):
+        steps = (termination_steps_from_log(c[0], c[1], n_groups) if isinstance(c, tuple)
+                 else termination_steps(c))
+        rows = _whisker_rows(steps, workgroup * workgroup)
         fn = os.path.join(folder, f"{name}{problem}{camera_name}_{kind}WorkGroupWiskerPlot.txt")
         with open(fn, "w") as fh:
             fh.write("median, min, max, lowerStdDeviation, upperStdDeviation\n")

@@ -251,13 +251,17 @@ int bvhgpu_trace(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
  * among them, rays doing leaf work, unique leaves among them, rays that
  * terminate) as intersectWideAlternative collects them
  * (compactNode.cpp:357-601), and step_count[p] = the packet's number of steps;
- * steps at or beyond step_cap are counted but not written. opts: scheme
- * BVHGPU_STREAM, no reorder; counters non-null; packets of opts->workgroup^2
- * rays in ray order. Results and counters equal bvhgpu_trace's. */
+ * steps at or beyond step_cap are counted but not written. wide_alternative
+ * 0 logs intersectWide's schedule instead (compactNode.cpp:118-356: a ray
+ * whose node visit leaves a leaf on top visits that leaf in the same step).
+ * opts: scheme BVHGPU_STREAM, no reorder; counters non-null; packets of
+ * opts->workgroup^2 rays in ray order. Results and counters equal
+ * bvhgpu_trace's. */
 int bvhgpu_trace_steps(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint64_t n,
                        const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                        uint32_t* counters, uint64_t* depth_hist, int32_t step_cap,
-                       uint32_t* step_stats, uint32_t* step_count, void* stream);
+                       int32_t wide_alternative, uint32_t* step_stats, uint32_t* step_count,
+                       void* stream);
 
 /* Host pointers: copies rays in, traces, copies results out, synchronises
  * `stream`. Device staging buffers are owned by the scene and reused. */

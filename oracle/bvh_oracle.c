@@ -427,13 +427,16 @@ static uint32_t distinct(int32_t* ids, int k) {
 
 /* intersectWideAlternative with counters; with `steps`, also the per-step
  * data it collects for CameraData's workgroup analysis
- * (compactNode.cpp:357-601): per packet p and step s, steps[(p * step_cap
+ * (compactNode.cpp:357-601; wide_alt 0: the schedule of intersectWide,
+ * compactNode.cpp:118-356, where a ray whose node visit leaves a leaf on
+ * top visits that leaf in the same step's leaf loop): per packet p and step s, steps[(p * step_cap
  * + s) * 5 ..] = node work, unique nodes, leaf work, unique leaves,
  * terminations (step 0: the state before the loop, compactNode.cpp:410-415;
  * a root that is a leaf starts as leaf work), step_count[p] = steps used. */
 static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n, int shadow,
                        int packet, ohit_t* hits, uint8_t* occluded, octr_t* ctrs,
-                       uint64_t* hist, int step_cap, uint32_t* steps, uint32_t* step_count) {
+                       uint64_t* hist, int step_cap, uint32_t* steps, uint32_t* step_count,
+                       int wide_alt) {
   int cap = stack_need(b);
   if (packet <= 0 || packet > 65535) return 1;
   int64_t npk = (int64_t)((n + (uint64_t)packet - 1) / (uint64_t)packet);
@@ -446,6 +449,7 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
     uint16_t* w1 = (uint16_t*)malloc(2 * (size_t)packet);
     uint16_t* w2 = (uint16_t*)malloc(2 * (size_t)packet);
     int32_t* ids = (int32_t*)malloc(sizeof(int32_t) * (size_t)packet);
+    uint16_t* ext = (uint16_t*)malloc(2 * (size_t)packet);
     uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 4)
     for (int64_t pk = 0; pk < npk; ++pk) {
@@ -484,6 +488,7 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
       }
       while (node_rays != 0 || leaf_rays != 0) {
         uint32_t term = 0, un = 0, ul = 0;
+        int n_ext = 0;
         for (int i = 0; i < node_rays; ++i) {
           int j = cur[i];
           ostate_t* s = &st[j];
@@ -494,14 +499,15 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
           if (sps[j] >= cap - 32) rc = 4;
           if (sps[j] != 0) {
             if (stk[sps[j] - 1] >= 0) nxt[next_node++] = (uint16_t)j;
+            else if (!wide_alt) ext[n_ext++] = (uint16_t)j;  /* intersectWide: leaf this step */
             else nxt[wide - 1 - (next_leaf++)] = (uint16_t)j;
           } else {
             term++;
           }
         }
         if (steps) un = distinct(ids, node_rays);
-        for (int i = 0; i < leaf_rays; ++i) {
-          int j = cur[wide - 1 - i];
+        for (int i = 0; i < leaf_rays + n_ext; ++i) {
+          int j = i < leaf_rays ? cur[wide - 1 - i] : ext[i - leaf_rays];
           ostate_t* s = &st[j];
           int32_t* stk = stacks + (size_t)j * cap;
           int32_t id = -stk[--sps[j]];
@@ -517,12 +523,12 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
             term++;
           }
         }
-        if (steps) ul = distinct(ids, leaf_rays);
+        if (steps) ul = distinct(ids, leaf_rays + n_ext);
         if (steps && step < step_cap) {
           uint32_t* rec = steps + ((size_t)pk * (size_t)step_cap + (size_t)step) * 5;
           rec[0] = (uint32_t)node_rays;
           rec[1] = un;
-          rec[2] = (uint32_t)leaf_rays;
+          rec[2] = (uint32_t)(leaf_rays + n_ext);
           rec[3] = ul;
           rec[4] = term;
         }
@@ -545,7 +551,7 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
       for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
       free(h);
     }
-    free(stacks); free(sps); free(st); free(w1); free(w2); free(ids);
+    free(stacks); free(sps); free(st); free(w1); free(w2); free(ids); free(ext);
   }
   return rc;
 }
@@ -553,15 +559,16 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
 int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* rays, uint64_t n,
                                      int shadow, int packet, ohit_t* hits, uint8_t* occluded,
                                      octr_t* ctrs, uint64_t* hist) {
-  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, 0, NULL, NULL);
+  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, 0, NULL, NULL, 1);
 }
 
 int oracle_trace_instrumented_stream_steps(const oracle_compact_t* b, const float* rays,
                                            uint64_t n, int shadow, int packet, ohit_t* hits,
                                            uint8_t* occluded, octr_t* ctrs, uint64_t* hist,
-                                           int step_cap, uint32_t* steps, uint32_t* step_count) {
+                                           int step_cap, uint32_t* steps, uint32_t* step_count,
+                                           int wide_alternative) {
   return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, step_cap, steps,
-                     step_count);
+                     step_count, wide_alternative);
 }
 
 /* ------------------------------------------------------------ fast path -- */

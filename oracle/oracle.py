@@ -47,7 +47,7 @@ def lib() -> C.CDLL:
             L.oracle_trace_instrumented_stream_steps.restype = C.c_int
             L.oracle_trace_instrumented_stream_steps.argtypes = [
                 C.POINTER(_Compact), _P, C.c_uint64, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int,
-                _P, _P]
+                _P, _P, C.c_int]
             L.oracle_trace_fast.restype = C.c_int
             L.oracle_trace_fast.argtypes = [C.POINTER(_Fast), C.POINTER(_Compact), _P, C.c_uint64,
                                             C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
@@ -135,7 +135,7 @@ def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: b
 
 
 def trace_instrumented_steps(view: CompactView, rays: np.ndarray, shadow: bool, packet: int,
-                             step_cap: int) -> dict:
+                             step_cap: int, wide_alternative: bool = True) -> dict:
     """intersectWideAlternative over packets of ``packet`` rays with the
     per-step workgroup data (bvh_oracle.c: stream_impl): ``steps`` [packets,
     step_cap, 5] (node work, unique nodes, leaf work, unique leaves,
@@ -152,7 +152,7 @@ def trace_instrumented_steps(view: CompactView, rays: np.ndarray, shadow: bool, 
     count = np.zeros(npk, np.uint32)
     rc = lib().oracle_trace_instrumented_stream_steps(
         C.byref(view.c), _p(rays), n, int(shadow), packet, _p(hits), _p(occ), _p(ctr), _p(hist),
-        step_cap, _p(steps), _p(count))
+        step_cap, _p(steps), _p(count), int(wide_alternative))
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist, "steps": steps,

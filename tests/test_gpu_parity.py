@@ -253,19 +253,20 @@ def test_non_finite_and_extreme_rays(profile):
 def test_stream_step_log(kind, n, l):
     """bvhgpu_trace_steps: per packet and step the node work, unique nodes,
     leaf work, unique leaves and terminations of intersectWideAlternative
-    equal the oracle's, for primary and shadow rays (inactive rays, a ragged
-    last packet, a step log shorter than the traversal)."""
+    (and of intersectWide's schedule) equal the oracle's, for primary and
+    shadow rays (inactive rays, a ragged last packet, a step log shorter than
+    the traversal)."""
     tris, b, cv = TS.bvh(kind, n, l)
     rays = (TS.terrain_case()[1] if kind == "terrain" else TS.clutter_rays(tris))[:-77]
     scene = pkg.Scene(b)
     prims = pkg.hit_prims(scene.trace(dev(rays))["hits"].cpu().numpy())
     sh, _ = TS.secondary(tris, rays, prims, LIGHT)
     cap = 400
-    for shadow, r in ((False, rays), (True, sh)):
-        ref = O.trace_instrumented_steps(cv, r, shadow, 256, cap)
+    for (shadow, r), alt in [(x, y) for x in ((False, rays), (True, sh)) for y in (True, False)]:
+        ref = O.trace_instrumented_steps(cv, r, shadow, 256, cap, wide_alternative=alt)
         assert int(ref["step_count"].max()) < cap
         got = scene.trace(dev(r), kind="any" if shadow else "closest", scheme="stream",
-                          counters=True, depth_hist=True, steps=cap)
+                          counters=True, depth_hist=True, steps=cap, wide_alternative=alt)
         assert np.array_equal(got["step_count"].cpu().numpy().astype(np.uint32),
                               ref["step_count"])
         assert np.array_equal(got["step_stats"].cpu().numpy().astype(np.uint32), ref["steps"])
@@ -276,7 +277,7 @@ def test_stream_step_log(kind, n, l):
         else:
             assert np.array_equal(bits(got["hits"].cpu().numpy()), bits(ref["hits"]))
         short = scene.trace(dev(r), kind="any" if shadow else "closest", scheme="stream",
-                            counters=True, steps=3)
+                            counters=True, steps=3, wide_alternative=alt)
         assert np.array_equal(short["step_count"].cpu().numpy().astype(np.uint32),
                               ref["step_count"])
         assert np.array_equal(short["step_stats"].cpu().numpy().astype(np.uint32),

@@ -113,3 +113,25 @@ def test_workgroup_data_files(tmp_path):
     with pytest.raises(ValueError):
         R.write_workgroup_data(str(tmp_path), "s", "", "", 2, 1, 2, P, np.array([5, 2]), S,
                                np.array([2, 4]), pc, sc)
+
+
+def test_whisker_from_step_log_matches_counters():
+    """Termination steps expanded from a step log equal node + leaf visits
+    per ray for the alternative schedule (here a synthetic log built from
+    per-ray visit counts of two 2x2 workgroups)."""
+    from bvhraytracer_gb300 import report as R
+    visits = np.array([[3, 1], [2, 0], [0, 0], [4, 2], [1, 1], [2, 2], [5, 0], [3, 3]])
+    c = np.zeros((8, 8), np.int32)
+    c[:, 0], c[:, 1] = visits[:, 0], visits[:, 1]
+    steps = c[:, 0] + c[:, 1]
+    log = np.zeros((2, 12, 5), np.int32)
+    count = np.zeros(2, np.int32)
+    for g in range(2):
+        s = steps[g * 4:(g + 1) * 4]
+        count[g] = s.max() + 1
+        for v in s:
+            log[g, v, 4] += 1
+    from_log = R.termination_steps_from_log(log, count, 2)
+    want = np.concatenate([np.sort(steps[:4]), np.sort(steps[4:])])
+    assert np.array_equal(from_log, want)
+    assert R._whisker_rows(from_log, 4) == R._whisker_rows(steps, 4)
