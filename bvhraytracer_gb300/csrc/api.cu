@@ -564,6 +564,8 @@ int bvhgpu_scene_bytes(bvhgpu_scene_t s, uint64_t* node_bytes, uint64_t* leaf_by
   return BVHGPU_OK;
 }
 
+// bvhgpu_trace and bvhgpu_trace_steps: a trace of device rays, with the
+// stream kernel's step log when step_stats is given.
 static int trace_device(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
                         const bvhgpu_trace_opts_t* opts, bvhgpu_hit_t* hits, uint8_t* occluded,
                         uint32_t* counters, uint64_t* depth_hist, int32_t step_cap,
