@@ -164,3 +164,20 @@ def test_jobs_any_order(profile):
             assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
         else:
             assert torch.equal(out, ref)
+
+
+@pytest.mark.parametrize("kind", ["closest", "any"])
+def test_jobs_of_one_kind(kind):
+    """A job list of one ray kind (one launch, kernel compiled for that
+    kind) and of one kind and node width (one group) equal the per-scene
+    traces."""
+    items = _scenes()
+    jobs, refs = _jobs(items, "instrumented")
+    sel = [(j, r) for j, r in zip(jobs, refs) if j[2] == kind]
+    for subset in (sel, [x for x in sel if x[0][0].node_format == "fp32"][:2]):
+        for j, _ in subset:
+            j[3].fill_(9)
+        pkg.trace_jobs([j for j, _ in subset], policy=2, refill=16)
+        torch.cuda.synchronize()
+        for (scene, rays, k, out), ref in subset:
+            assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
