@@ -805,7 +805,7 @@ def run_adjoint(a):
             cam, target, _ = S.clutter_viewpoints(a.objects, seed=1)
             rays = S.camera_rays(cam, target, 1024, 1024)
         v = torch.from_numpy(verts).to(dev).requires_grad_(True)
-        f = torch.from_numpy(faces).to(dev)
+        f = torch.from_numpy(faces.astype(np.int32)).to(dev)  # int32: no per-step conversion
         r = torch.from_numpy(rays).to(dev).requires_grad_(True)
         scene = D.scene_for(v, f)
         vt = torch.from_numpy(verts + rng.normal(0, 0.01, verts.shape).astype(np.float32)).to(dev)

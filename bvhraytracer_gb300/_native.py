@@ -123,8 +123,8 @@ _SIGS = {
     "bvhgpu_adjoint": (C.c_int, [_P, _P, C.c_uint64, _P, _P, _P, _P]),
     "bvhgpu_adjoint_vertices": (C.c_int, [_P, _P, C.c_uint64, _P, _P, C.c_uint64, C.c_uint64,
                                           _P, _P, _P]),
-    "bvhgpu_adjoint_hits": (C.c_int, [_P, _P, _P, C.c_uint64, _P, _P, C.c_uint64, C.c_uint64,
-                                      _P, _P, _P, _P]),
+    "bvhgpu_adjoint_hits": (C.c_int, [_P, _P, _P, C.c_uint64, _P, _P, _P, _P, C.c_uint64,
+                                      C.c_uint64, _P, _P, _P, _P]),
     "bvhgpu_trace_jobs": (C.c_int, [C.POINTER(Job), C.c_int32, C.POINTER(TraceOpts), _P]),
     "bvhgpu_trace_host_batches": (C.c_int, [_P, C.POINTER(HostBatch), C.c_int32, _P]),
     "bvhgpu_gang_size": (C.c_int, []),

@@ -127,7 +127,14 @@ BVHGPU_DEV TriGrad adjoint_reverse(const SceneDev& sc, const AdjointArgs& a, uin
   const df n3 = dot3(e2, s2);
 
   // Reverse pass.
-  const float4 g = a.grad_hits[rid];
+  float4 g;
+  if (a.grad_hits) {
+    g = a.grad_hits[rid];
+  } else {
+    // Separate per-ray arrays dL/dt, dL/du, dL/dv (null: zero).
+    g = make_float4(0.f, a.grad_t ? __ldg(a.grad_t + rid) : 0.f,
+                    a.grad_u ? __ldg(a.grad_u + rid) : 0.f, a.grad_v ? __ldg(a.grad_v + rid) : 0.f);
+  }
   const df gt = df_of(g.y), gb1 = df_of(g.z), gb2 = df_of(g.w);
   const df g_n1 = df_mul(gb1, inv), g_n2 = df_mul(gb2, inv), g_n3 = df_mul(gt, inv);
   const df g_inv = df_add(df_add(df_mul(gb1, n1), df_mul(gb2, n2)), df_mul(gt, n3));

@@ -1068,13 +1068,15 @@ int bvhgpu_adjoint_vertices(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t
 }
 
 int bvhgpu_adjoint_hits(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
-                        uint64_t n, const float* grad_hits, const int32_t* faces,
-                        uint64_t n_faces, uint64_t n_verts, float* grad_verts, float* grad_tri9,
-                        float* grad_rays, void* stream) {
+                        uint64_t n, const float* grad_t, const float* grad_u,
+                        const float* grad_v, const int32_t* faces, uint64_t n_faces,
+                        uint64_t n_verts, float* grad_verts, float* grad_tri9, float* grad_rays,
+                        void* stream) {
   if (!s) return set_error(BVHGPU_ERR_BAD_ARG, "null scene");
   if (n == 0) return BVHGPU_OK;
-  if (!rays || !hits || !grad_hits || !grad_rays || ((uintptr_t)rays & 15) ||
-      ((uintptr_t)hits & 15) || ((uintptr_t)grad_hits & 15) || ((uintptr_t)grad_rays & 15))
+  if (!rays || !hits || !grad_rays || ((uintptr_t)rays & 15) || ((uintptr_t)hits & 15) ||
+      ((uintptr_t)grad_rays & 15) || ((uintptr_t)grad_t & 3) || ((uintptr_t)grad_u & 3) ||
+      ((uintptr_t)grad_v & 3))
     return set_error(BVHGPU_ERR_BAD_ARG, "adjoint: null or misaligned buffer");
   if (faces) {
     if (!grad_verts || grad_tri9 || ((uintptr_t)faces & 3) || ((uintptr_t)grad_verts & 3))
@@ -1095,8 +1097,10 @@ int bvhgpu_adjoint_hits(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, const bvhgpu
       if (rc) return rc;
     }
   }
-  dev::AdjointArgs a{rays, n, reinterpret_cast<const float4*>(grad_hits), grad_tri9, grad_rays,
-                     stack_cap(s)};
+  dev::AdjointArgs a{rays, n, nullptr, grad_tri9, grad_rays, stack_cap(s)};
+  a.grad_t = grad_t;
+  a.grad_u = grad_u;
+  a.grad_v = grad_v;
   a.faces = faces;
   a.grad_verts = grad_verts;
   a.n_verts = (uint32_t)n_verts;

@@ -35,19 +35,20 @@ class _RayHit(torch.autograd.Function):
         rays, faces, hits = ctx.saved_tensors
         n = rays.shape[0]
         dev = rays.device
-        z = torch.zeros(n, dtype=torch.float32, device=dev)
 
         def g(x):
-            return z if x is None else x.to(torch.float32)
+            # incoming gradient of t, u or v as a contiguous float32 array (None: zero)
+            return None if x is None else x.to(torch.float32).contiguous()
 
-        grad_hits = torch.stack([z, g(gt), g(gu), g(gv)], dim=1).contiguous()
+        gt, gu, gv = g(gt), g(gu), g(gv)
         grad_rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
         grad_verts = torch.zeros((ctx.n_verts, 3), dtype=torch.float32, device=dev)
         stream = torch.cuda.current_stream(dev)
         # The kernel adds each hit triangle's vertex gradients straight into
         # grad_verts through the face indices.
         N.check(N.lib().bvhgpu_adjoint_hits(
-            ctx.scene.handle, rays.data_ptr(), hits.data_ptr(), n, grad_hits.data_ptr(),
+            ctx.scene.handle, rays.data_ptr(), hits.data_ptr(), n,
+            *[None if x is None else x.data_ptr() for x in (gt, gu, gv)],
             faces.data_ptr(), faces.shape[0], ctx.n_verts, grad_verts.data_ptr(), None,
             grad_rays.data_ptr(), C.c_void_p(stream.cuda_stream)))
         return grad_verts, grad_rays, None, None

@@ -398,7 +398,9 @@ int bvhgpu_adjoint_vertices(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint
 
 /* The same backward passes from the forward pass's closest hits instead of a
  * re-trace (no traversal: one thread per ray reads its hit, the triangle and
- * the ray). hits[i] is bvhgpu_trace's record of ray i (fast profile for the
+ * the ray), with the incoming gradients as separate per-ray arrays grad_t,
+ * grad_u, grad_v (dL/dt, dL/du, dL/dv; NULL: zero) instead of grad_hits
+ * records. hits[i] is bvhgpu_trace's record of ray i (fast profile for the
  * forward pass's hits to be the ones the gradients describe); its prim selects
  * the triangle, prim -1 gives zero gradients, an id the scene does not hold
  * gives zero gradients and is recorded as BVHGPU_ERR_BAD_ARG. With faces, the
@@ -406,9 +408,10 @@ int bvhgpu_adjoint_vertices(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, uint
  * NULL); without, to grad_tri9 as in bvhgpu_adjoint (grad_verts NULL). Any
  * node format. The first call uploads the scene's id -> leaf slot map. */
 int bvhgpu_adjoint_hits(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
-                        uint64_t n, const float* grad_hits, const int32_t* faces,
-                        uint64_t n_faces, uint64_t n_verts, float* grad_verts, float* grad_tri9,
-                        float* grad_rays, void* stream);
+                        uint64_t n, const float* grad_t, const float* grad_u,
+                        const float* grad_v, const int32_t* faces, uint64_t n_faces,
+                        uint64_t n_verts, float* grad_verts, float* grad_tri9, float* grad_rays,
+                        void* stream);
 
 /* ---- tracing without allocation --------------------------------------- */
 /* No counterpart in the reference (its renderer allocates nothing on a GPU).

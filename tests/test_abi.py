@@ -183,6 +183,6 @@ def test_new_entry_points_validate_arguments_without_a_gpu():
     assert lib.bvhgpu_tri_any_hit(20, buf.ctypes.data, ids.ctypes.data, buf.ctypes.data,
                                   res.ctypes.data, 1, None) == N.ERR_BAD_ARG
     assert lib.bvhgpu_trace_host_batches(None, None, 1, None) == N.ERR_BAD_ARG
-    assert lib.bvhgpu_adjoint_hits(None, None, None, 1, None, None, 0, 0, None, None, None,
-                                   None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_adjoint_hits(None, None, None, 1, None, None, None, None, 0, 0, None,
+                                   None, None, None) == N.ERR_BAD_ARG
     assert b"null" in lib.bvhgpu_last_error()

@@ -237,8 +237,11 @@ def test_adjoint_from_stored_hits_equals_retrace():
     gr_b = torch.full_like(gr_a, 7.0)
     N.check(N.lib().bvhgpu_adjoint(scene.handle, rays.data_ptr(), n, gh.data_ptr(),
                                    tri_a.data_ptr(), gr_a.data_ptr(), st))
+    # the incoming gradients as separate dL/dt, dL/du, dL/dv arrays
+    gtuv = [gh[:, k].contiguous() for k in (1, 2, 3)]
+    gp = [x.data_ptr() for x in gtuv]
     N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
-                                        gh.data_ptr(), None, 0, 0, None, tri_b.data_ptr(),
+                                        *gp, None, 0, 0, None, tri_b.data_ptr(),
                                         gr_b.data_ptr(), st))
     gv_a = torch.zeros((v.shape[0], 3), dtype=torch.float32, device="cuda")
     gv_b = torch.zeros_like(gv_a)
@@ -247,7 +250,7 @@ def test_adjoint_from_stored_hits_equals_retrace():
                                             f32.data_ptr(), f32.shape[0], v.shape[0],
                                             gv_a.data_ptr(), gr_c.data_ptr(), st))
     N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
-                                        gh.data_ptr(), f32.data_ptr(), f32.shape[0],
+                                        *gp, f32.data_ptr(), f32.shape[0],
                                         v.shape[0], gv_b.data_ptr(), None, gr_b.data_ptr(), st))
     torch.cuda.synchronize()
     scene.status()
@@ -263,18 +266,18 @@ def test_adjoint_from_stored_hits_equals_retrace():
     bad.view(torch.int32)[i, 0] = f.shape[0] + 100
     tri_c = torch.zeros_like(tri_a)
     N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, rays[i:].data_ptr(), bad[i:].data_ptr(), 1,
-                                        gh[i:].data_ptr(), None, 0, 0, None, tri_c.data_ptr(),
-                                        gr_b[i:].data_ptr(), st))
+                                        *[x[i:].data_ptr() for x in gtuv], None, 0, 0, None,
+                                        tri_c.data_ptr(), gr_b[i:].data_ptr(), st))
     with pytest.raises(Exception):
         scene.status()
     assert torch.count_nonzero(tri_c) == 0 and torch.count_nonzero(gr_b[i]) == 0
     # faces and grad_tri9 together, or neither: rejected on the host
     assert N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
-                                       gh.data_ptr(), f32.data_ptr(), f32.shape[0], v.shape[0],
+                                       *gp, f32.data_ptr(), f32.shape[0], v.shape[0],
                                        gv_b.data_ptr(), tri_b.data_ptr(), gr_b.data_ptr(),
                                        st) == N.ERR_BAD_ARG
     assert N.lib().bvhgpu_adjoint_hits(scene.handle, rays.data_ptr(), hits.data_ptr(), n,
-                                       gh.data_ptr(), None, 0, 0, None, None, gr_b.data_ptr(),
+                                       *gp, None, 0, 0, None, None, gr_b.data_ptr(),
                                        st) == N.ERR_BAD_ARG
 
 
@@ -310,9 +313,11 @@ def test_adjoint_many_rays_on_one_triangle():
     gv = torch.zeros((6, 3), dtype=torch.float32, device="cuda")
     gr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # dL/dt and dL/du only: dL/dv passed as NULL (zero)
+    gtw, guw = gh[:, 1].contiguous(), gh[:, 2].contiguous()
     N.check(N.lib().bvhgpu_adjoint_hits(scene.handle, r.data_ptr(), hits.data_ptr(), n,
-                                        gh.data_ptr(), f32.data_ptr(), 2, 6, gv.data_ptr(),
-                                        None, gr.data_ptr(), st))
+                                        gtw.data_ptr(), guw.data_ptr(), None, f32.data_ptr(), 2,
+                                        6, gv.data_ptr(), None, gr.data_ptr(), st))
     gv2 = torch.zeros_like(gv)
     N.check(N.lib().bvhgpu_adjoint_vertices(scene.handle, r.data_ptr(), n, gh.data_ptr(),
                                             f32.data_ptr(), 2, 6, gv2.data_ptr(),
