@@ -481,6 +481,11 @@ def run_ours(a):
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = statistics.median(e2e_times)
     e2e_mean_s = statistics.mean(e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+        te = torch.tensor([e2e_s, e2e_mean_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)  # the slowest rank sets both
+        e2e_s, e2e_mean_s = (float(x) for x in te.tolist())
     e2e_ok = (np.array_equal(h_out[0].numpy().view(np.uint32), out_h.cpu().numpy().view(np.uint32))
               and np.array_equal(h_out[2].numpy(), out_a.cpu().numpy()))
     h2d = sum(x.numel() * 4 for x in h_rays)
