@@ -17,7 +17,9 @@ def _scenes():
     out = []
     specs = [("terrain", 20, 4, 4, "fp32"), ("clutter", 30, 8, 8, "fp32"),
              ("terrain", 40, 16, 4, "q8"), ("clutter", 80, 4, 8, "q8"),
-             ("clutter", 50, 16, 16, "fp32"), ("terrain", 12, 12, 12, "fp32")]
+             ("clutter", 50, 16, 16, "fp32"), ("terrain", 12, 12, 12, "fp32"),
+             # widths off the gang multiples: padded node and leaf records
+             ("clutter", 25, 3, 2, "fp32"), ("terrain", 16, 5, 7, "q8")]
     for i, (kind, size, n, l, fmt) in enumerate(specs):
         if kind == "terrain":
             tris = S.terrain(size, seed=i)

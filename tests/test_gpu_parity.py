@@ -125,6 +125,47 @@ def test_sweep_all_widths(n, l):
                       refa, False)
 
 
+@pytest.mark.parametrize("n,l", [(2, 1), (3, 2), (5, 3), (7, 5), (9, 7), (13, 11), (2, 16),
+                                 (16, 1)])
+def test_odd_widths(n, l):
+    """Branching factors and leaf sizes off the gang multiples (the reference's
+    render-time sweeps run N = 2..16, LatexPlots/MatLibPlot/PerformancePlots.py:21-24):
+    node and leaf records are padded to the gang of 4 like
+    fastNodeManager.h:1556,1602, the padding lanes never hit. Every scheme,
+    both profiles, closest and any hit, counters included; Q8 nodes keep the
+    hits."""
+    tris, b, cv = TS.bvh("clutter120", n, l)
+    rays = TS.clutter_rays(tris, res=(64, 48))
+    scene = pkg.Scene(b)
+    fv = O.FastView(b.export_fast())
+    for profile in ("instrumented", "fast"):
+        if profile == "instrumented":
+            ref = O.trace_instrumented(cv, rays, shadow=False)
+        else:
+            ref = O.trace_fast(fv, cv, rays, any_hit=False)
+        prims = pkg.hit_prims(ref["hits"])
+        _, ao = TS.secondary(tris, rays, prims, LIGHT, ao_samples=2)
+        if profile == "instrumented":
+            refa = O.trace_instrumented(cv, ao, shadow=True)
+        else:
+            refa = O.trace_fast(fv, cv, ao, any_hit=True)
+        for scheme, kw in SCHEMES:
+            got = scene.trace(dev(rays), scheme=scheme, profile=profile, counters=True,
+                              depth_hist=True, **kw)
+            check_closest(got, ref)
+            g = scene.trace(dev(ao), kind="any", scheme=scheme, profile=profile, counters=True,
+                            depth_hist=True, **kw)
+            check_any(g, refa)
+        s8 = pkg.Scene(b, node_format="q8")
+        for scheme, kw in (("per_ray", {}), ("persistent", {"policy": 2, "refill": 16})):
+            got = s8.trace(dev(rays), scheme=scheme, profile=profile, **kw)
+            check_closest(got, ref, False)
+            check_any(s8.trace(dev(ao), kind="any", scheme=scheme, profile=profile, **kw), refa,
+                      False)
+        s8.status()
+    scene.status()
+
+
 @pytest.mark.parametrize("gang,leaf_memory", [(8, 0), (4, 16), (8, 16)])
 def test_gang_and_leaf_memory(gang, leaf_memory):
     tris, b, cv = TS.bvh("clutter120", 8, 4)
