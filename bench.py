@@ -825,31 +825,38 @@ def run_adjoint(a):
         vt = torch.from_numpy(verts + rng.normal(0, 0.01, verts.shape).astype(np.float32)).to(dev)
         t_tgt, _, _, p_tgt = D.ray_hit(vt, f, r.detach(), D.scene_for(vt, f))
 
-        def step():
-            t, u, w, prim = D.ray_hit(v, f, r, scene)
+        def step(recompute=False):
+            t, u, w, prim = D.ray_hit(v, f, r, scene, recompute=recompute)
             m = (prim >= 0) & (p_tgt >= 0)
             # masked by multiplication (no boolean indexing, so no host sync)
             loss = torch.where(m, (t - t_tgt) ** 2, torch.zeros_like(t)).sum()
             gv, gr = torch.autograd.grad(loss, (v, r))
             return loss, gv, gr, prim, m
 
-        for _ in range(a.warmup):
-            step()
-        torch.cuda.synchronize(dev)
         stream = torch.cuda.current_stream(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(a.steps):
-            loss, gv, gr, prim, m = step()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / a.steps
+
+        def timed(recompute):
+            for _ in range(a.warmup):
+                step(recompute)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(a.steps):
+                res = step(recompute)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            return e0.elapsed_time(e1) / a.steps, res
+
+        # the backward re-tracing each ray instead of reading the stored hits
+        ms_re, _ = timed(True)
+        ms, (loss, gv, gr, prim, m) = timed(False)
         fdr = fd_check(verts, faces, rays, prim.cpu().numpy(), m.cpu().numpy(),
                        t_tgt.cpu().numpy().astype(np.float64), gv.cpu().numpy())
         scene.status()
         results[name] = {"triangles": int(faces.shape[0]), "rays": int(rays.shape[0]),
                          "hits": int(m.sum().item()), "ms_forward_backward": ms,
                          "mrays_per_s_forward_backward": rays.shape[0] / (ms / 1e3) / 1e6,
+                         "ms_forward_backward_recompute": ms_re,
                          "fd_fp64_norm_relative_error": fdr,
                          "fd": "central, FP64, 512 sampled vertex coordinates"}
     line = {

@@ -57,6 +57,28 @@ def test_adjoint_matches_torch_autograd_moller_trumbore():
     assert rel_v < 1e-4 and rel_r < 1e-4, (rel_v.item(), rel_r.item())
 
 
+@pytest.mark.parametrize("which", ["t", "uv"])
+def test_recompute_backward_equals_stored_hits(which):
+    """ray_hit(recompute=True) re-traces in the backward pass instead of
+    keeping the forward's hits: the same per-ray gradients bit for bit, the
+    same vertex gradients up to the order of the atomic sums."""
+    v, f, r, scene, t_tgt, p_tgt = _case(n=48, res=80, seed=3)
+    out = []
+    for recompute in (False, True):
+        t, u, w, prim = D.ray_hit(v, f, r, scene, recompute=recompute)
+        m = (prim >= 0) & (p_tgt >= 0)
+        if which == "t":
+            loss = torch.where(m, (t - t_tgt) ** 2, torch.zeros_like(t)).sum()
+        else:
+            loss = torch.where(m, 0.7 * u - 1.3 * w, torch.zeros_like(u)).sum()
+        out.append(torch.autograd.grad(loss, (v, r)))
+    (gv0, gr0), (gv1, gr1) = out
+    scene.status()
+    assert torch.equal(gr0, gr1)
+    assert gv0.abs().max() > 0
+    assert (gv0 - gv1).abs().max() <= 1e-5 * gv0.abs().max()
+
+
 def test_adjoint_matches_fp64_chain_rule():
     """The reverse pass against float64 PyTorch autograd of Moller-Trumbore on
     the CPU, fed the same upstream gradient (from the FP32 forward t): with
