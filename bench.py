@@ -53,7 +53,7 @@ NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, "reorder": 457373696 / 4147200
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--objects", type=int, default=4000)
@@ -148,6 +148,13 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.before = 0  # samples taken before the timed region
+
+    def _lines(self):
+        try:
+            return Path(self.path).read_text().count("\n")
+        except OSError:
+            return 0
 
     def __enter__(self):
         try:
@@ -159,6 +166,14 @@ class ClockSampler:
                 stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        # Wait (at most 5 s) for the first sample, so that the sampler runs
+        # before the timed region starts; the samples taken until then are
+        # left out of the summary when later ones exist.
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None and self._lines() == 0:
+            time.sleep(0.005)
+        self.before = self._lines()
         return self
 
     def __exit__(self, *exc):
@@ -180,6 +195,8 @@ class ClockSampler:
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        if len(rows) > self.before:
+            rows = rows[self.before:]
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
