@@ -79,6 +79,26 @@ def test_recompute_backward_equals_stored_hits(which):
     assert (gv0 - gv1).abs().max() <= 1e-5 * gv0.abs().max()
 
 
+def test_non_contiguous_rays():
+    """Rays given as a strided view (8 of 11 columns): the same hits and
+    gradients as the contiguous copy, in both backward modes."""
+    v, f, r, scene, t_tgt, p_tgt = _case(n=32, res=48, seed=5)
+    wide = torch.zeros((r.shape[0], 11), dtype=torch.float32, device="cuda")
+    wide[:, 2:10] = r.detach()
+    rs = wide[:, 2:10].requires_grad_(True)
+    assert not rs.is_contiguous()
+    for recompute in (False, True):
+        got, want = [], []
+        for rays, out in ((rs, got), (r, want)):
+            t, u, w, prim = D.ray_hit(v, f, rays, scene, recompute=recompute)
+            loss = torch.where(prim >= 0, t + 0.5 * u, torch.zeros_like(t)).sum()
+            out.append((t.detach(), prim) + torch.autograd.grad(loss, (v, rays)))
+        assert torch.equal(got[0][0], want[0][0]) and torch.equal(got[0][1], want[0][1])
+        assert torch.equal(got[0][3], want[0][3])
+        assert (got[0][2] - want[0][2]).abs().max() <= 1e-5 * want[0][2].abs().max()
+    scene.status()
+
+
 def test_adjoint_matches_fp64_chain_rule():
     """The reverse pass against float64 PyTorch autograd of Moller-Trumbore on
     the CPU, fed the same upstream gradient (from the FP32 forward t): with
