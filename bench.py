@@ -245,6 +245,38 @@ def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=5):
             "seconds": med}
 
 
+def oracle_check(a, bvh, batches, device_outs, host_outs, rays_per_batch=24_000):
+    """CPU-baseline leg, as the checker: an evenly strided sample of each
+    timed batch (primary hits, shadow and AO occlusion, as the timed device
+    launches and the host entry point left them) against the oracle's
+    restatement of the reference on the same rays (instrumented profile:
+    CompactNodeManager::intersectImmediately; fast profile:
+    FastNodeManager::intersect / intersectSecondary). Returns per batch
+    whether both result sets equal the oracle bit for bit."""
+    from oracle import oracle as O
+    cv = O.CompactView(bvh.export_compact())
+    fv = O.FastView(bvh.export_fast(gang=4)) if a.profile == "fast" else None
+    res = {}
+    for name, (rays, kind), dev_out, host_out in zip(("primary", "shadow", "AO"), batches,
+                                                      device_outs, host_outs):
+        idx = np.unique(np.linspace(0, rays.shape[0] - 1, rays_per_batch).astype(np.int64))
+        any_hit = kind == "any"
+        if fv is not None:
+            ref = O.trace_fast(fv, cv, rays[idx], any_hit, counters=False)
+        else:
+            ref = O.trace_instrumented(cv, rays[idx], shadow=any_hit, counters=False)
+        want = ref["occluded"] if any_hit else ref["hits"].view(np.uint32)
+        got = [np.ascontiguousarray(o[idx]) for o in (dev_out, host_out)]
+        if not any_hit:
+            got = [g.view(np.uint32) for g in got]
+        res[name] = bool(all(np.array_equal(g, want) for g in got))
+    res["rays_checked_per_batch"] = int(min(rays_per_batch, min(r.shape[0] for r, _ in batches)))
+    res["oracle"] = ("fast profile restatement (FastNodeManager::intersect / "
+                     "intersectSecondary)" if fv is not None else
+                     "instrumented restatement (CompactNodeManager::intersectImmediately)")
+    return res
+
+
 def run_reference(a):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -531,9 +563,12 @@ def run_ours(a):
         compare["persistent_fp32"] = frame_ms([(plain, {"scheme": "persistent"})] * 3)
         compare["this_method"] = ms / a.steps
         compare["speedup_vs_plain_per_ray"] = compare["plain_per_ray_fp32"] / (ms / a.steps)
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, tris, bvh, primary, shadow, ao, a.cpu_sample)
+        parity = oracle_check(a, bvh, ((primary, "closest"), (shadow, "any"), (ao, "any")),
+                              [x.cpu().numpy() for x in (out_h, out_s, out_a)],
+                              [x.numpy() for x in h_out])
 
     if a.report and rank == 0:
         from bvhraytracer_gb300 import report
@@ -555,6 +590,7 @@ def run_ours(a):
                 "rays_per_step": n_rays, "primary": int(primary.shape[0]),
                 "shadow": int(shadow.shape[0]), "ao": int(ao.shape[0]),
                 "results_equal_plain_kernel": bool(ok),
+                "oracle_equal": parity,
                 "l2": "inputs larger than L2 (rays ~%d MB per step); BVH stays L2-resident"
                       % (n_rays * 32 // 2**20),
                 "bvh_bytes": {"nodes_fp32": plain.node_bytes, "leaves": plain.leaf_bytes},

@@ -170,6 +170,34 @@ class Bvh:
             pass
 
 
+
+def check_noalloc_batch(rays, kind: str, out, device) -> None:
+    """Rejects a batch for :meth:`Scene.trace_batches_noalloc` that the kernel
+    would read or write out of bounds: rays must be a contiguous float32
+    ``[n, 8]`` tensor and ``out`` a contiguous ``[n, 4]`` float32 (closest)
+    or ``[n]`` uint8 (any) tensor, both on ``device``. Raises ``ValueError``
+    instead of copying, since a copy would allocate."""
+    import torch
+    if kind not in _KIND:
+        raise ValueError(f"no-alloc trace: kind must be 'closest' or 'any', not {kind!r}")
+    dev = torch.device(device)
+    if not isinstance(rays, torch.Tensor) or not isinstance(out, torch.Tensor):
+        raise ValueError("no-alloc trace: rays and out must be tensors")
+    for name, t in (("rays", rays), ("out", out)):
+        if t.device != dev:
+            raise ValueError(f"no-alloc trace: {name} on {t.device}, scene on {dev}")
+        if not t.is_contiguous():
+            raise ValueError(f"no-alloc trace: {name} must be contiguous (a copy would allocate)")
+    if rays.dtype != torch.float32 or rays.dim() != 2 or rays.shape[1] != 8:
+        raise ValueError("no-alloc trace: rays must be float32 [n, 8]")
+    n = rays.shape[0]
+    if _KIND[kind] == N.CLOSEST:
+        if out.dtype != torch.float32 or tuple(out.shape) != (n, 4):
+            raise ValueError(f"no-alloc trace: closest-hit out must be float32 [{n}, 4]")
+    elif out.dtype != torch.uint8 or tuple(out.shape) != (n,):
+        raise ValueError(f"no-alloc trace: any-hit out must be uint8 [{n}]")
+
+
 class Scene:
     """A BVH resident in GPU memory (device layout of the C ABI)."""
 
@@ -313,7 +341,7 @@ class Scene:
         return outs
 
     def trace_batches_noalloc(self, batches, *, profile: str = "instrumented", policy: int = 0,
-                              refill: int = 0, stream=None) -> None:
+                              refill: int = 0, any_order: bool = False, stream=None) -> None:
         """Traces up to 64 batches with no GPU allocation in the call.
 
         ``batches``: list of ``(rays, kind, out)`` with device tensors: rays
@@ -325,11 +353,13 @@ class Scene:
         import torch
         arr = (N.Batch * max(1, len(batches)))()
         for i, (rays, kind, out) in enumerate(batches):
+            check_noalloc_batch(rays, kind, out, self.device)
             k = _KIND[kind]
             arr[i] = N.Batch(_ptr(rays), rays.shape[0], k, 0,
                              _ptr(out) if k == N.CLOSEST else None,
                              _ptr(out) if k == N.ANY else None)
-        o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)
+        o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill,
+                        0, 0, 0, int(any_order))
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
         N.check(N.lib().bvhgpu_trace_batches_noalloc(self._h, arr, len(batches), C.byref(o),
                                                      C.c_void_p(s.cuda_stream)))

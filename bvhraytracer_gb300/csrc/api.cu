@@ -1337,12 +1337,17 @@ int bvhgpu_scene_status(bvhgpu_scene_t s, void* stream) {
 // The array is a file-scope device variable: every GPU that loads the library
 // holds its kNoAllocQueueSlots * 8 bytes until the process exits. Host code
 // may not use the symbol as an address, so the device address is looked up
-// once per device with cudaGetSymbolAddress (with that device current) on the
-// first call for that device; make that first call before any stream capture.
+// with cudaGetSymbolAddress (with that device current) on the first call for
+// that device, and again on the first call after the device's context was
+// destroyed and re-created (cudaDeviceReset), since the array then lives at a
+// new address; make that first call before any stream capture. The first call
+// with a given ray kind, profile, policy and node width may also load that
+// kernel variant into the context (CUDA's lazy module loading), which can
+// take device memory for the code itself; a caller that must see no device
+// memory change at all warms up every combination it will use.
 // Every call shares the array and leaves its contents behind: each call clears
 // the heads it uses before its launches, and calls that overlap on the GPU
-// (different streams, or devices sharing nothing but the caller) race on the
-// heads, so serialise them.
+// (different streams of one device) race on the heads, so serialise them.
 namespace {
 
 constexpr int kNoAllocQueueSlots = 64;  // at most 64 batches per call (512 bytes)
@@ -1351,17 +1356,48 @@ static __device__ __align__(256) unsigned long long g_noalloc_queue[kNoAllocQueu
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};  // context id of each address
 
-// Device address of g_noalloc_queue on `device` (which must be current).
+// Unique id of the calling thread's current context (ids are never reused
+// within a process, unlike context handles), through the driver entry points
+// the runtime hands out, so the library does not link libcuda itself.
+// Returns 0 when the driver does not provide them.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of g_noalloc_queue on `device` (which must be current): looked
+// up once per device and context.
 int noalloc_scratch(int device, unsigned long long** out) {
   if (device < 0 || device >= kNoAllocMaxDevices)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "no-alloc trace: device ordinal above 63");
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[device]) {
+  if (!g_noalloc_addr[device] || ctx == 0 || g_noalloc_ctx[device] != ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_queue);
     if (e != cudaSuccess) return cuda_error(e, "no-alloc trace: cudaGetSymbolAddress");
     g_noalloc_addr[device] = static_cast<unsigned long long*>(p);
+    g_noalloc_ctx[device] = ctx;
   }
   *out = g_noalloc_addr[device];
   return BVHGPU_OK;
@@ -1384,19 +1420,22 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
   if (rc) return rc;
   if (cfg.reorder)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "no-alloc trace: reorder needs scratch memory");
+  if (cfg.save_distance || cfg.stack_local)
+    return set_error(BVHGPU_ERR_UNSUPPORTED,
+                     "no-alloc trace runs the persistent scheme: no save_distance or stack_local");
   cfg.scheme = BVHGPU_PERSISTENT;
   for (int i = 0; i < n_batches; ++i) {
     const bvhgpu_batch_t& b = batches[i];
     if (b.kind != BVHGPU_CLOSEST && b.kind != BVHGPU_ANY)
       return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: batch kind");
     if (b.n == 0) continue;
+    if (b.n > (1ull << 40)) return set_error(BVHGPU_ERR_BAD_ARG, "too many rays");
     if (!b.rays || ((uintptr_t)b.rays & 15))
       return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: rays null or not 16-byte aligned");
     if (b.kind == BVHGPU_CLOSEST ? (!b.hits || ((uintptr_t)b.hits & 15)) : !b.occluded)
       return set_error(BVHGPU_ERR_BAD_ARG, "no-alloc trace: result buffer null or misaligned");
   }
-  if ((size_t)s->max_stack * 128 * 4 > 227 * 1024)
-    return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
+  if ((rc = check_smem_fit(cfg, stack_cap(s)))) return rc;
   if (n_batches == 0) return BVHGPU_OK;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaSetDevice(s->device);
@@ -1426,6 +1465,9 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t s, const bvhgpu_batch_t* batches
     c.queue = heads + i;
     c.queue_cleared = true;
     c.fmt = s->layout.node_format;
+    // Top levels staged in shared memory, as the regular persistent launches do.
+    c.top_nodes = std::min(s->layout.top_nodes, kTopStageBytes / (uint32_t)s->layout.record_bytes);
+    c.stall_bytes = s->stall_bytes;
     switch (s->layout.node_stride) {
       case 4: e = dev::launch_trace_n4(sc, a, c, st); break;
       case 8: e = dev::launch_trace_n8(sc, a, c, st); break;

@@ -421,9 +421,16 @@ int bvhgpu_adjoint_hits(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bv
  * batches with the persistent kernel, whose scratch (one ray-queue head per
  * batch) lives in a fixed 512-byte device array inside the library instead of
  * being allocated. More than 64 batches -> BVHGPU_ERR_BAD_ARG. The first call
- * on a device looks up that array's address (make it before any stream
- * capture). All calls share the array: calls that overlap on the GPU race.
- * opts: profile, policy and refill are used; scheme is always persistent. */
+ * on a device, and the first after that device's context was destroyed and
+ * re-created (cudaDeviceReset), looks up that array's address: make it before
+ * any stream capture. The first call with a given kind, profile, policy and
+ * node width may also load that kernel variant (CUDA lazy loading), which can
+ * take device memory for its code: warm up each combination once where no
+ * change of free device memory may be seen. All calls share the array: calls
+ * that overlap on the GPU race. opts: profile, policy, refill and any_order
+ * are used; scheme is always persistent; reorder, save_distance and
+ * stack_local -> BVHGPU_ERR_UNSUPPORTED. The top levels are staged in shared
+ * memory as in the regular persistent launches. */
 typedef struct {
   const bvhgpu_ray_t* rays; /* device, 16-byte aligned */
   uint64_t n;

@@ -186,3 +186,72 @@ def test_new_entry_points_validate_arguments_without_a_gpu():
     assert lib.bvhgpu_adjoint_hits(None, None, None, 1, None, None, None, None, 0, 0, None,
                                    None, None, None) == N.ERR_BAD_ARG
     assert b"null" in lib.bvhgpu_last_error()
+
+
+def test_noalloc_entry_point_rejects_bad_arguments_without_a_gpu():
+    """bvhgpu_trace_batches_noalloc checks its batches and options before any
+    CUDA call. The scene handle is a zeroed host buffer: none of these checks
+    reads it."""
+    lib = N.lib()
+    fake_scene = C.create_string_buffer(4096)
+    rays = np.zeros((4, 8), np.float32)
+    hits = np.zeros((4, 4), np.float32)
+    occ = np.zeros(4, np.uint8)
+    o = N.TraceOpts(0, 2, 0, 16, 128, 0, 0, 0, 0, 0, 0)
+
+    def call(batches, n=None, opts=o):
+        arr = (N.Batch * max(1, len(batches)))(*batches)
+        return lib.bvhgpu_trace_batches_noalloc(fake_scene, arr,
+                                                len(batches) if n is None else n,
+                                                C.byref(opts) if opts is not None else None, None)
+
+    good = N.Batch(rays.ctypes.data, 4, N.CLOSEST, 0, hits.ctypes.data, None)
+    assert call([good] * 65) == N.ERR_BAD_ARG  # more heads than the fixed scratch holds
+    assert b"64" in lib.bvhgpu_last_error()
+    assert lib.bvhgpu_trace_batches_noalloc(fake_scene, None, 1, C.byref(o), None) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_trace_batches_noalloc(None, None, 0, C.byref(o), None) == N.ERR_BAD_ARG
+    assert call([good], opts=None) == N.ERR_BAD_ARG
+    assert call([N.Batch(rays.ctypes.data, 4, 7, 0, hits.ctypes.data, None)]) == N.ERR_BAD_ARG
+    assert b"kind" in lib.bvhgpu_last_error()
+    assert call([N.Batch(rays.ctypes.data + 4, 4, N.CLOSEST, 0, hits.ctypes.data, None)]) \
+        == N.ERR_BAD_ARG
+    assert call([N.Batch(None, 4, N.CLOSEST, 0, hits.ctypes.data, None)]) == N.ERR_BAD_ARG
+    assert call([N.Batch(rays.ctypes.data, 4, N.CLOSEST, 0, hits.ctypes.data + 8, None)]) \
+        == N.ERR_BAD_ARG
+    assert call([N.Batch(rays.ctypes.data, 4, N.ANY, 0, None, None)]) == N.ERR_BAD_ARG
+    assert call([N.Batch(rays.ctypes.data, 1 << 41, N.ANY, 0, None, occ.ctypes.data)]) \
+        == N.ERR_BAD_ARG
+    for bad in (N.TraceOpts(0, 2, 0, 16, 128, 0, 0, 0, 10, 0, 0),   # reorder
+                N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 1, 0, 0, 0),    # save_distance
+                N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0, 1, 0)):   # stack_local
+        assert call([good], opts=bad) == N.ERR_UNSUPPORTED
+    assert call([good], opts=N.TraceOpts(0, 2, 0, 16, 128, 3, 0, 0, 0, 0, 0)) == N.ERR_BAD_ARG
+
+
+def test_noalloc_python_binding_rejects_mismatched_buffers():
+    """The binding checks shapes, dtypes, contiguity and devices before the
+    call, since the kernel writes n records into ``out`` unchecked."""
+    torch = pytest.importorskip("torch")
+    check = pkg.check_noalloc_batch
+    rays = torch.zeros((6, 8), dtype=torch.float32)
+    check(rays, "closest", torch.zeros((6, 4), dtype=torch.float32), "cpu")
+    check(rays, "any", torch.zeros(6, dtype=torch.uint8), "cpu")
+    bad = [
+        (rays, "closest", torch.zeros((5, 4), dtype=torch.float32)),       # too few rows
+        (rays, "closest", torch.zeros((6, 4), dtype=torch.float64)),       # dtype
+        (rays, "any", torch.zeros(5, dtype=torch.uint8)),                  # too few bytes
+        (rays, "any", torch.zeros((6, 4), dtype=torch.float32)),           # any-hit as closest
+        (rays, "closest", torch.zeros((4, 6), dtype=torch.float32).t()),   # strided out
+        (torch.zeros((8, 6), dtype=torch.float32).t(), "closest",
+         torch.zeros((6, 4), dtype=torch.float32)),                        # strided rays
+        (torch.zeros((6, 8), dtype=torch.float64), "closest",
+         torch.zeros((6, 4), dtype=torch.float32)),                        # ray dtype
+        (torch.zeros((6, 7), dtype=torch.float32), "closest",
+         torch.zeros((6, 4), dtype=torch.float32)),                        # ray width
+        (rays, "nearest", torch.zeros((6, 4), dtype=torch.float32)),       # kind
+    ]
+    for r, k, o in bad:
+        with pytest.raises(ValueError):
+            check(r, k, o, "cpu")
+    with pytest.raises(ValueError):  # buffers on another device than the scene
+        check(rays, "closest", torch.zeros((6, 4), dtype=torch.float32), "cuda:0")

@@ -67,16 +67,29 @@ def test_noalloc_rejects_more_batches_than_the_scratch_holds():
     assert all(torch.equal(o.view(torch.int32), ref.view(torch.int32)) for o in outs)
 
 
-def test_noalloc_makes_no_allocation():
+@pytest.mark.parametrize("options", [dict(), dict(profile="fast", policy=2, refill=24,
+                                                    any_order=True)])
+def test_noalloc_makes_no_allocation(options):
     scene, prim, shadow, _ = _frame()
     out_h = torch.empty((prim.shape[0], 4), dtype=torch.float32, device="cuda")
     out_s = torch.empty(shadow.shape[0], dtype=torch.uint8, device="cuda")
-    # First call: the scratch address look-up and the kernels' first load.
-    scene.trace_batches_noalloc([(prim, "closest", out_h), (shadow, "any", out_s)])
+    batches = [(prim, "closest", out_h), (shadow, "any", out_s)]
+    # Warm-up with the same options: the scratch address look-up and the
+    # first load of each kernel variant these options select.
+    scene.trace_batches_noalloc(batches, **options)
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
     for _ in range(3):
-        scene.trace_batches_noalloc([(prim, "closest", out_h), (shadow, "any", out_s)])
+        scene.trace_batches_noalloc(batches, **options)
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
+    ref_h = scene.trace(prim, profile=options.get("profile", "instrumented"))["hits"]
+    assert torch.equal(out_h.view(torch.int32), ref_h.view(torch.int32))
+
+
+def test_noalloc_rejects_a_short_result_buffer():
+    scene, prim, _, _ = _frame()
+    short = torch.empty((prim.shape[0] - 1, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError):
+        scene.trace_batches_noalloc([(prim, "closest", short)])
