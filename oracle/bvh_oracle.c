@@ -25,10 +25,15 @@
  *     intersectSecondaryWideAlternative ... fastNodeManager.h:835-1230
  *   the ISPC kernels as single calls (oracle_*_calls) .. rayTracerTemplate.ispc:26-233
  *
- * Parity status: UNPINNED at the reference level. The reference ships no
- * golden vectors or known-answer tests for this path and cannot be built here
- * (it needs GLM, the ISPC compiler and MSVC-only code), so this restatement is
- * checked against analytic known answers and hand-counted traversals instead.
+ * Parity status of the instrumented profile: PINNED against the reference's
+ * own code. oracle/ref/build_ref.py compiles the reference's SAH builder and
+ * instrumented traversal (aabb.cpp, node.cpp, bvh.cpp, compactNode.cpp,
+ * triangle.cpp, ray.cpp) here with g++ and a GLM stand-in; the tests compare
+ * this restatement with it (trees node for node; hit triangle, t, hit point,
+ * counters, per-depth and fullness histograms ray for ray) and with the
+ * fixtures it generated (tests/golden/). The fast profile (the ISPC kernels
+ * and FastNodeManager) needs the ISPC compiler, which is absent: it stays
+ * checked against analytic known answers and hand-counted traversals.
  *
  * Deviations (both deliberate and documented):
  *   - the stream traversal of a tree whose root is a leaf tests that leaf
@@ -52,6 +57,9 @@
 #endif
 
 #define MAX_DEPTH 64
+/* childFullness / primitiveFullness bins (Ray::childFullness[childCount],
+ * ray.h:36-37): child or primitive counts 0..16. */
+#define MAX_FULL 17
 
 /* ---------------------------------------------------------------- views -- */
 typedef struct {
@@ -161,8 +169,8 @@ static float gamma_n(int n) {
 /* Triangle::intersect(Ray&) (triangle.cpp:52-249) without its counters and
  * material lookup (the alpha test passes for opaque untextured meshes).
  * Returns 1 on a hit with *t, *b1, *b2. */
-static int watertight(const float* tri, const oray_t* r, float tmax, float* t_out, float* b1_out,
-                      float* b2_out) {
+static int watertight_b0(const float* tri, const oray_t* r, float tmax, float* t_out,
+                         float* b0_out, float* b1_out, float* b2_out) {
   const float* p0 = tri;
   const float* p1 = tri + 3;
   const float* p2 = tri + 6;
@@ -227,6 +235,7 @@ static int watertight(const float* tri, const oray_t* r, float tmax, float* t_ou
   if (det < 0 && (t_scaled >= 0 || t_scaled < tmax * det)) return 0;
   else if (det > 0 && (t_scaled <= 0 || t_scaled > tmax * det)) return 0;
   float inv_det = 1 / det;
+  float b0 = e0 * inv_det;
   float b1 = e1 * inv_det;
   float b2 = e2 * inv_det;
   float t = t_scaled * inv_det;
@@ -242,9 +251,15 @@ static int watertight(const float* tri, const oray_t* r, float tmax, float* t_ou
       3 * (gamma_n(3) * max_e * max_zt + delta_e * max_zt + delta_z * max_e) * fabsf(inv_det);
   if (t <= delta_t) return 0;
   *t_out = t;
+  if (b0_out) *b0_out = b0;
   *b1_out = b1;
   *b2_out = b2;
   return 1;
+}
+
+static int watertight(const float* tri, const oray_t* r, float tmax, float* t_out, float* b1_out,
+                      float* b2_out) {
+  return watertight_b0(tri, r, tmax, t_out, NULL, b1_out, b2_out);
 }
 
 /* One lane of triIntersect{L} (rayTracerTemplate.ispc:35-76): p0/p1/p2 as
@@ -286,6 +301,7 @@ typedef struct {
   int hit;
   octr_t c;
   uint64_t* hist; /* [2][MAX_DEPTH], nullable */
+  uint64_t* full; /* [2][MAX_FULL]: childFullness, primitiveFullness; nullable */
 } ostate_t;
 
 /* One leaf visit; returns 1 if any triangle was hit. */
@@ -294,6 +310,8 @@ static int leaf_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s) {
   s->c.leaf_visits++;
   s->c.tri_tests += pc;
   if (s->hist) s->hist[MAX_DEPTH + (b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1)]++;
+  /* ray.primitiveFullness[primCount]++ (compactNode.cpp:655) */
+  if (s->full) s->full[MAX_FULL + (pc < MAX_FULL ? pc : MAX_FULL - 1)]++;
   int any = 0;
   for (uint32_t k = 0; k < pc; ++k) {
     float t, b1, b2;
@@ -317,6 +335,8 @@ static void node_visit(const oracle_compact_t* b, uint32_t id, ostate_t* s, int3
   uint32_t cb = b->child_begin[id], cc = b->child_count[id];
   s->c.node_visits++;
   if (s->hist) s->hist[b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1]++;
+  /* ray.childFullness[childCount]++ (compactNode.cpp:716) */
+  if (s->full) s->full[cc < MAX_FULL ? cc : MAX_FULL - 1]++;
   const int8_t* ord = b->order48 + (size_t)id * 48 + s->r.code * 16;
   for (uint32_t k = 0; k < cc; ++k) {
     int i = s->r.reverse ? (int)k : (int)(cc - 1 - k);
@@ -362,7 +382,7 @@ static int stack_need(const oracle_compact_t* b) {
  * (compactNode.cpp:637-645); the root enters with distance 0. */
 int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint64_t n, int shadow,
                               ohit_t* hits, uint8_t* occluded, octr_t* ctrs, uint64_t* hist,
-                              int use_distance) {
+                              int use_distance, uint64_t* fullness) {
   int cap = stack_need(b);
   int rc = 0;
 #pragma omp parallel
@@ -370,6 +390,7 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
     int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
     float* dstack = use_distance ? (float*)malloc(sizeof(float) * (size_t)cap) : NULL;
     uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
+    uint64_t* f = fullness ? (uint64_t*)calloc(2 * MAX_FULL, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 64)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
       ostate_t s;
@@ -377,6 +398,7 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
       s.shadow = shadow;
       s.best_prim = -1;
       s.hist = h;
+      s.full = f;
       make_ray(rays + i * 8, 1, &s.r);
       if (!isnan(rays[i * 8])) {
         int sp = 0;
@@ -402,6 +424,11 @@ int oracle_trace_instrumented(const oracle_compact_t* b, const float* rays, uint
 #pragma omp critical
       for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
       free(h);
+    }
+    if (fullness) {
+#pragma omp critical
+      for (int k = 0; k < 2 * MAX_FULL; ++k) fullness[k] += f[k];
+      free(f);
     }
     free(dstack);
     free(stack);
@@ -436,7 +463,7 @@ static uint32_t distinct(int32_t* ids, int k) {
 static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n, int shadow,
                        int packet, ohit_t* hits, uint8_t* occluded, octr_t* ctrs,
                        uint64_t* hist, int step_cap, uint32_t* steps, uint32_t* step_count,
-                       int wide_alt) {
+                       int wide_alt, uint64_t* fullness) {
   int cap = stack_need(b);
   if (packet <= 0 || packet > 65535) return 1;
   int64_t npk = (int64_t)((n + (uint64_t)packet - 1) / (uint64_t)packet);
@@ -451,6 +478,7 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
     int32_t* ids = (int32_t*)malloc(sizeof(int32_t) * (size_t)packet);
     uint16_t* ext = (uint16_t*)malloc(2 * (size_t)packet);
     uint64_t* h = hist ? (uint64_t*)calloc(2 * MAX_DEPTH, sizeof(uint64_t)) : NULL;
+    uint64_t* f = fullness ? (uint64_t*)calloc(2 * MAX_FULL, sizeof(uint64_t)) : NULL;
 #pragma omp for schedule(dynamic, 4)
     for (int64_t pk = 0; pk < npk; ++pk) {
       uint64_t first = (uint64_t)pk * (uint64_t)packet;
@@ -465,6 +493,7 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
         s->shadow = shadow;
         s->best_prim = -1;
         s->hist = h;
+        s->full = f;
         make_ray(rays + (first + (uint64_t)j) * 8, 1, &s->r);
         stacks[(size_t)j * cap] = root_leaf ? 0 : 0;
         sps[j] = 1;
@@ -551,6 +580,11 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
       for (int k = 0; k < 2 * MAX_DEPTH; ++k) hist[k] += h[k];
       free(h);
     }
+    if (fullness) {
+#pragma omp critical
+      for (int k = 0; k < 2 * MAX_FULL; ++k) fullness[k] += f[k];
+      free(f);
+    }
     free(stacks); free(sps); free(st); free(w1); free(w2); free(ids); free(ext);
   }
   return rc;
@@ -558,17 +592,18 @@ static int stream_impl(const oracle_compact_t* b, const float* rays, uint64_t n,
 
 int oracle_trace_instrumented_stream(const oracle_compact_t* b, const float* rays, uint64_t n,
                                      int shadow, int packet, ohit_t* hits, uint8_t* occluded,
-                                     octr_t* ctrs, uint64_t* hist) {
-  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, 0, NULL, NULL, 1);
+                                     octr_t* ctrs, uint64_t* hist, uint64_t* fullness) {
+  return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, 0, NULL, NULL, 1,
+                     fullness);
 }
 
 int oracle_trace_instrumented_stream_steps(const oracle_compact_t* b, const float* rays,
                                            uint64_t n, int shadow, int packet, ohit_t* hits,
                                            uint8_t* occluded, octr_t* ctrs, uint64_t* hist,
                                            int step_cap, uint32_t* steps, uint32_t* step_count,
-                                           int wide_alternative) {
+                                           int wide_alternative, uint64_t* fullness) {
   return stream_impl(b, rays, n, shadow, packet, hits, occluded, ctrs, hist, step_cap, steps,
-                     step_count, wide_alternative);
+                     step_count, wide_alternative, fullness);
 }
 
 /* ------------------------------------------------------------ fast path -- */
@@ -953,6 +988,31 @@ void oracle_fp64_pairs(const float* rays, const float* tri9, uint64_t n, int nor
     o3[0] = tt;
     o3[1] = b1;
     o3[2] = b2;
+  }
+}
+
+/* The instrumented profile's hit point of each (ray, triangle) pair:
+ * Triangle::intersect's pHit = b0 * p0 + b1 * p1 + b2 * p2 (triangle.cpp:201,
+ * glm vec3 operations, left to right), which the reference stores as
+ * Ray::surfacePosition. Recomputes the watertight test for the given triangle
+ * (its barycentrics do not depend on tMax); pairs it does not hit get NaN. */
+void oracle_hit_points(const float* rays, const float* tri9, uint64_t n, float* out_pos) {
+  for (uint64_t i = 0; i < n; ++i) {
+    oray_t r;
+    make_ray(rays + i * 8, 1, &r);
+    const float* p = tri9 + i * 9;
+    float t, b0, b1, b2;
+    float* o = out_pos + i * 3;
+    if (!watertight_b0(p, &r, INFINITY, &t, &b0, &b1, &b2)) {
+      o[0] = o[1] = o[2] = NAN;
+      continue;
+    }
+    for (int a = 0; a < 3; ++a) {
+      float x = b0 * p[a];
+      float y = b1 * p[3 + a];
+      float z = b2 * p[6 + a];
+      o[a] = (x + y) + z;
+    }
   }
 }
 

@@ -1,9 +1,10 @@
 """ctypes wrapper of the CPU oracle (oracle/bvh_oracle.c) — TEST INFRASTRUCTURE.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
-import this module. Parity status: unpinned at the reference level (the
-reference ships no golden vectors for the path and cannot be built here);
-see the header of bvh_oracle.c.
+import this module. Parity status: the instrumented profile is pinned
+against the reference's own code compiled here (oracle/ref/) and the fixtures
+it generated (tests/golden/); the fast (ISPC) profile is not, see the header
+of bvh_oracle.c.
 """
 from __future__ import annotations
 
@@ -40,18 +41,20 @@ def lib() -> C.CDLL:
             L = C.CDLL(str(build()))
             L.oracle_trace_instrumented.restype = C.c_int
             L.oracle_trace_instrumented.argtypes = [C.POINTER(_Compact), _P, C.c_uint64, C.c_int,
-                                                    _P, _P, _P, _P, C.c_int]
+                                                    _P, _P, _P, _P, C.c_int, _P]
             L.oracle_trace_instrumented_stream.restype = C.c_int
             L.oracle_trace_instrumented_stream.argtypes = [C.POINTER(_Compact), _P, C.c_uint64,
-                                                           C.c_int, C.c_int, _P, _P, _P, _P]
+                                                           C.c_int, C.c_int, _P, _P, _P, _P, _P]
             L.oracle_trace_instrumented_stream_steps.restype = C.c_int
             L.oracle_trace_instrumented_stream_steps.argtypes = [
                 C.POINTER(_Compact), _P, C.c_uint64, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int,
-                _P, _P, C.c_int]
+                _P, _P, C.c_int, _P]
             L.oracle_trace_fast.restype = C.c_int
             L.oracle_trace_fast.argtypes = [C.POINTER(_Fast), C.POINTER(_Compact), _P, C.c_uint64,
                                             C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
                                             C.c_int]
+            L.oracle_hit_points.restype = None
+            L.oracle_hit_points.argtypes = [_P, _P, C.c_uint64, _P]
             L.oracle_fp64_pairs.restype = None
             L.oracle_fp64_pairs.argtypes = [_P, _P, C.c_uint64, C.c_int, _P]
             L.oracle_aabb_intersect_calls.restype = None
@@ -91,24 +94,31 @@ class FastView:
 def trace_instrumented(view: CompactView, rays: np.ndarray, shadow: bool, packet: int = 0,
                        counters: bool = True, use_distance: bool = False) -> dict:
     """CompactNodeManager::intersectImmediately(ray, use_distance) (packet ==
-    0) or intersectWideAlternative over packets of ``packet`` rays."""
+    0) or intersectWideAlternative over packets of ``packet`` rays. With
+    ``counters``: per-ray counters, per-depth node / leaf visits
+    (``depth_hist``) and Ray::childFullness / primitiveFullness summed over
+    the rays (``fullness`` [2, 17]: visits of nodes with c children, of leaves
+    with c triangles)."""
     rays = np.ascontiguousarray(rays, np.float32)
     n = rays.shape[0]
     hits = None if shadow else np.zeros((n, 4), np.float32)
     occ = np.zeros(n, np.uint8) if shadow else None
     ctr = np.zeros((n, 8), np.uint32) if counters else None
     hist = np.zeros((2, 64), np.uint64) if counters else None
+    full = np.zeros((2, 17), np.uint64) if counters else None
     if packet and use_distance:
         raise ValueError("use_distance is a per-ray traversal")
     if packet:
         rc = lib().oracle_trace_instrumented_stream(C.byref(view.c), _p(rays), n, int(shadow),
-                                                     packet, _p(hits), _p(occ), _p(ctr), _p(hist))
+                                                     packet, _p(hits), _p(occ), _p(ctr), _p(hist),
+                                                     _p(full))
     else:
         rc = lib().oracle_trace_instrumented(C.byref(view.c), _p(rays), n, int(shadow), _p(hits),
-                                             _p(occ), _p(ctr), _p(hist), int(use_distance))
+                                             _p(occ), _p(ctr), _p(hist), int(use_distance),
+                                             _p(full))
     if rc:
         raise RuntimeError(f"oracle error {rc}")
-    return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist}
+    return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist, "fullness": full}
 
 
 def trace_fast(fview: FastView, cview: CompactView, rays: np.ndarray, any_hit: bool,
@@ -150,13 +160,24 @@ def trace_instrumented_steps(view: CompactView, rays: np.ndarray, shadow: bool, 
     hist = np.zeros((2, 64), np.uint64)
     steps = np.zeros((npk, step_cap, 5), np.uint32)
     count = np.zeros(npk, np.uint32)
+    full = np.zeros((2, 17), np.uint64)
     rc = lib().oracle_trace_instrumented_stream_steps(
         C.byref(view.c), _p(rays), n, int(shadow), packet, _p(hits), _p(occ), _p(ctr), _p(hist),
-        step_cap, _p(steps), _p(count), int(wide_alternative))
+        step_cap, _p(steps), _p(count), int(wide_alternative), _p(full))
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return {"hits": hits, "occluded": occ, "counters": ctr, "depth_hist": hist, "steps": steps,
-            "step_count": count}
+            "step_count": count, "fullness": full}
+
+
+def hit_points(rays: np.ndarray, tri9: np.ndarray) -> np.ndarray:
+    """Triangle::intersect's hit point b0 p0 + b1 p1 + b2 p2 of each (ray,
+    triangle) pair, instrumented profile (NaN where the pair does not hit)."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    tri9 = np.ascontiguousarray(tri9, np.float32)
+    out = np.zeros((rays.shape[0], 3), np.float32)
+    lib().oracle_hit_points(_p(rays), _p(tri9), rays.shape[0], _p(out))
+    return out
 
 
 def fp64_pairs(rays: np.ndarray, tri9: np.ndarray, normalise: bool) -> np.ndarray:

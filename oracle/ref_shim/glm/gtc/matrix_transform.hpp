@@ -1,0 +1,3 @@
+// Part of the GLM stand-in (see ../glm.hpp).
+#pragma once
+#include "../glm.hpp"
