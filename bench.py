@@ -88,13 +88,15 @@ def parse():
                         "_WorkGroupUniqueWork.txt) into this folder")
     p.add_argument("--workload", default="clutter",
                    choices=["clutter", "batch64", "adjoint", "scale8m", "terrain", "sweep",
-                            "gpuframe"],
+                            "gpuframe", "aolaunch"],
                    help="clutter: the 1M-triangle frame; batch64: 64 scenes in one launch; "
                         "adjoint: forward + backward of the hit distance; scale8m: 8M "
                         "triangles FP32 vs Q8 nodes; terrain: the 32k-triangle terrain, N4L4, "
                         "512x512 + shadow rays; sweep: the clutter frame for every N, L in "
                         "{4,8,12,16}^2, per-ray vs ray-stream; gpuframe: the clutter frame with "
-                        "every ray generated on the GPU, AO image read back")
+                        "every ray generated on the GPU, AO image read back; aolaunch: the "
+                        "clutter frame's AO launch alone on an evenly strided sample of "
+                        "--ao-sample rays (the case the ncu DRAM captures profile)")
     p.add_argument("--scenes", type=int, default=64)
     p.add_argument("--job-reorder", type=int, default=8,
                    help="batch64: direction bins per cube face side for the AO jobs (0 = off)")
@@ -102,6 +104,8 @@ def parse():
     p.add_argument("--job-any-order", type=int, default=1,
                    help="batch64: child-index push order for the AO jobs (1) or the "
                         "reference's order (0)")
+    p.add_argument("--ao-sample", type=int, default=2_000_000,
+                   help="aolaunch: AO rays traced per launch (strided sample of the frame's)")
     p.add_argument("--tune-nl", action="store_true",
                    help="batch64: let the autotuner pick N/L per scene")
     return p.parse_args()
@@ -423,7 +427,8 @@ def run_ours(a):
         cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
         if a.report:
             from bvhraytracer_gb300 import report
-            stats.append(report.RayStats.from_trace(c["counters"], c["depth_hist"]))
+            stats.append(report.RayStats.from_trace(c["counters"], c["depth_hist"],
+                                                    fullness=c["fullness"]))
         alg.append({"node_visits": int(cs[0]), "leaf_visits": int(cs[1]), "tri_tests": int(cs[4]),
                     "bytes": int(cs[0]) * sc.node_record_bytes + int(cs[4]) * 36})
     for sc, _ in chosen:
@@ -548,6 +553,10 @@ def run_ours(a):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg[dom]["bytes"] / (per_kernel_ms[dom] / 1e3) / 1e9
+    # The BVH (nodes + leaves) fits the 129 MB L2, so the bound that applies
+    # is L2's read rate: measured here with the library's streaming read
+    # kernel over a 60 MB buffer (median of 7, 20 passes each).
+    l2_peak = pkg.read_bandwidth(60 << 20, device=local)
     traffic = None
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
@@ -610,6 +619,9 @@ def run_ours(a):
                                    if traffic else None),
                 "algorithmic_bytes_per_launch": alg[dom]["bytes"],
                 "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
+                "l2_peak": l2_peak, "l2_frac": achieved / l2_peak,
+                "l2_peak_source": "measured: bvhgpu_read_bandwidth, 60 MB buffer read 20 times "
+                                  "per launch, L1 bypassed, median of 7",
             },
             "e2e": {"value": n_rays * world / e2e_s / 1e6, "unit": METRIC,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -1271,6 +1283,51 @@ def run_sweep(a):
     print(json.dumps(line))
 
 
+def run_aolaunch(a):
+    """The frame's AO batch alone, an evenly strided sample of --ao-sample
+    rays, traced with the bench's AO plan (persistent kernel, speculative
+    any-hit policy 2, refill 24, 6 x 10 x 10 direction bins, child-index push
+    order) --warmup + --steps times; node format --nodes. Prints the device
+    time and the algorithmic bytes per launch. It is the case the ncu DRAM
+    captures of the AO launch use (a launch of about 2M rays keeps a capture
+    short); the bytes per ray they measure scale with the ray count."""
+    import torch
+    import bvhraytracer_gb300 as pkg
+    dev = torch.device("cuda", 0)
+    tris, bvh, primary = make_frame(a)
+    plain = pkg.Scene(bvh)
+    scene = plain if a.nodes == "fp32" else pkg.Scene(bvh, node_format=a.nodes)
+    hits = plain.trace(torch.from_numpy(primary).to(dev))["hits"]
+    _, ao = secondaries(a, tris, primary, pkg.hit_prims(hits.cpu().numpy()))
+    idx = np.unique(np.linspace(0, ao.shape[0] - 1, min(a.ao_sample, ao.shape[0])).astype(np.int64))
+    rays = torch.from_numpy(ao[idx]).to(dev)
+    out = torch.empty(rays.shape[0], dtype=torch.uint8, device=dev)
+    plan = {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10, "any_order": True}
+    c = scene.trace(rays, kind="any", counters=True, **{k: v for k, v in plan.items()
+                                                         if k not in ("reorder", "any_order")})
+    cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
+    alg = int(cs[0]) * scene.node_record_bytes + int(cs[4]) * 36
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(a.warmup):
+        scene.trace(rays, kind="any", out=out, **plan)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        scene.trace(rays, kind="any", out=out, **plan)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    scene.status()
+    print(json.dumps({
+        "metric": METRIC, "value": rays.shape[0] / (ms / 1e3) / 1e6, "unit": METRIC,
+        "ms_per_launch": ms, "rays": int(rays.shape[0]), "workload": workload_name(a),
+        "nodes": a.nodes, "plan": plan, "triangles": int(bvh.info["n_tris"]),
+        "algorithmic_bytes_per_launch": alg, "node_record_bytes": scene.node_record_bytes,
+        "node_visits_per_ray": float(cs[0]) / rays.shape[0],
+        "tri_tests_per_ray": float(cs[4]) / rays.shape[0]}))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -1287,6 +1344,8 @@ def main():
         run_sweep(a)
     elif a.workload == "gpuframe":
         run_gpuframe(a)
+    elif a.workload == "aolaunch":
+        run_aolaunch(a)
     else:
         run_ours(a)
 

@@ -229,7 +229,10 @@ class Scene:
 
         Returns ``{"hits": [n,4] f32}`` (closest) or ``{"occluded": [n] u8}``
         (any), plus ``"counters"`` ``[n, 8]`` int32 and ``"depth_hist"``
-        ``[2, 64]`` int64 when requested. Asynchronous on ``stream``
+        ``[2, 64]`` int64 when requested (with ``depth_hist`` also
+        ``"fullness"`` ``[2, 17]`` int64: visits of nodes with c children and
+        of leaves with c triangles, the reference's Ray::childFullness and
+        primitiveFullness summed over the rays). Asynchronous on ``stream``
         (default: torch's current stream). ``save_distance`` (per-ray scheme):
         intersectSaveDistance / intersectImmediately(ray, useDistance=true).
         ``reorder`` = K > 0 traces the rays grouped into 6 K^2 direction bins
@@ -264,11 +267,13 @@ class Scene:
             res["counters"] = torch.zeros((n, N.COUNTERS_PER_RAY), dtype=torch.int32, device=dev)
             cp = _ptr(res["counters"])
         if depth_hist:
-            res["depth_hist"] = torch.zeros((2, 64), dtype=torch.int64, device=dev)
-            hh = _ptr(res["depth_hist"])
+            hbuf = torch.zeros(2 * 64 + 2 * 17, dtype=torch.int64, device=dev)
+            res["depth_hist"] = hbuf[:128].view(2, 64)
+            res["fullness"] = hbuf[128:].view(2, 17)
+            hh = _ptr(hbuf)
         o = N.TraceOpts(k, _SCHEME[scheme], _PROFILE[profile], workgroup, block, policy, refill,
                         int(save_distance), int(reorder), int(stack == "local"),
-                        int(any_order))
+                        int(any_order), int(bool(depth_hist)))
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         if steps:
             packets = -(-n // (workgroup * workgroup))
@@ -548,6 +553,15 @@ def tri_any_hit(l: int, tri, tri_ids, fastrays, stream=None):
     N.check(N.lib().bvhgpu_tri_any_hit(l, _ptr(tri), _ptr(tri_ids), _ptr(fastrays), _ptr(res),
                                        count, _stream_ptr(tri_ids, stream)))
     return res
+
+
+def read_bandwidth(bytes_: int, *, passes: int = 20, repeats: int = 7, device: int = 0) -> float:
+    """Median read bandwidth in GB/s of a ``bytes_`` buffer read ``passes``
+    times per timed launch (bvhgpu_read_bandwidth): the L2 ceiling for a
+    buffer that fits L2, the HBM read rate for one far larger."""
+    g = C.c_double()
+    N.check(N.lib().bvhgpu_read_bandwidth(device, int(bytes_), passes, repeats, C.byref(g)))
+    return g.value
 
 
 def hit_prims(hits) -> "np.ndarray":

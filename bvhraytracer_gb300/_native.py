@@ -53,7 +53,8 @@ class TraceOpts(C.Structure):
     _fields_ = [("kind", C.c_int32), ("scheme", C.c_int32), ("profile", C.c_int32),
                 ("workgroup", C.c_int32), ("block", C.c_int32), ("policy", C.c_int32),
                 ("refill", C.c_int32), ("save_distance", C.c_int32),
-                ("reorder", C.c_int32), ("stack_local", C.c_int32), ("any_order", C.c_int32)]
+                ("reorder", C.c_int32), ("stack_local", C.c_int32), ("any_order", C.c_int32),
+                ("fullness", C.c_int32)]
 
 
 class Batch(C.Structure):
@@ -118,6 +119,8 @@ _SIGS = {
     "bvhgpu_trace": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P, _P, _P]),
     "bvhgpu_trace_host": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(TraceOpts), _P, _P, _P]),
     "bvhgpu_fp64_check": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_int32, _P, _P]),
+    "bvhgpu_read_bandwidth": (C.c_int, [C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
+                                        C.POINTER(C.c_double)]),
     "bvhgpu_scene_set_stack_limit": (C.c_int, [_P, C.c_int32]),
     "bvhgpu_scene_inject_stall": (C.c_int, [_P, C.c_int32]),
     "bvhgpu_adjoint": (C.c_int, [_P, _P, C.c_uint64, _P, _P, _P, _P]),

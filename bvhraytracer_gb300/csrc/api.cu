@@ -589,6 +589,11 @@ static int trace_device(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
   a.occluded = occluded;
   a.counters = counters;
   a.depth_hist = reinterpret_cast<unsigned long long*>(depth_hist);
+  if (opts->fullness) {
+    if (!depth_hist)
+      return set_error(BVHGPU_ERR_BAD_ARG, "fullness: needs depth_hist (2 x 64 + 2 x 17 entries)");
+    a.fullness = a.depth_hist + 128;
+  }
   a.stack_cap = stack_cap(s);
   if (step_stats) {
     if (cfg.scheme != BVHGPU_STREAM || !cfg.count || !step_count || step_cap < 1 || cfg.reorder)

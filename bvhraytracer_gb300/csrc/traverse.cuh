@@ -53,6 +53,10 @@ struct TraceArgs {
   uint8_t* occluded;
   uint32_t* counters;
   unsigned long long* depth_hist;
+  // With counters: visits of nodes with c children (fullness[c]) and of
+  // leaves with c triangles (fullness[17 + c]), c <= 16: the reference's
+  // Ray::childFullness / primitiveFullness (ray.h:36-37) summed over the rays.
+  unsigned long long* fullness = nullptr;
   int stack_cap;              // stack entries per ray
   // Reordered traces: the i-th ray the kernel takes is input ray
   // out_index[i] (null: i), and its results go to that input slot.
@@ -179,7 +183,7 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   const uint32_t inner_base = meta.x, leaf_base = meta.y;
   const uint32_t leaf_mask = meta.z & 0xFFFFu;
   const int count = (int)((meta.z >> 16) & 0xFFu);
-  depth_out = (int)(meta.z >> 24);
+  depth_out = (int)(meta.z >> 24) | (count << 8);  // depth | child count << 8
 
   float ox = 0.f, oy = 0.f, oz = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
   if (FMT == kFmtQ8) {
@@ -482,6 +486,20 @@ BVHGPU_DEV bool leaf_step(const SceneDev& sc, uint32_t e, const Ray& r, float& t
 
 BVHGPU_DEV void record_error(int* status, int code) { atomicCAS(status, 0, code); }
 
+// Counting launches: one node visit (depth_count = depth | child count << 8,
+// as node_step returns it) into the per-depth histogram and childFullness
+// (compactNode.cpp:714-716), one leaf visit into the per-depth histogram and
+// primitiveFullness (compactNode.cpp:653-656).
+BVHGPU_DEV void count_node(const TraceArgs& a, int depth_count) {
+  if (a.depth_hist) atomicAdd(a.depth_hist + min(depth_count & 0xFF, 63), 1ull);
+  if (a.fullness) atomicAdd(a.fullness + min(depth_count >> 8, 16), 1ull);
+}
+BVHGPU_DEV void count_leaf(const SceneDev& sc, const TraceArgs& a, uint32_t e) {
+  if (a.depth_hist)
+    atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+  if (a.fullness) atomicAdd(a.fullness + 17 + (int)((e >> kLeafCountShift) & 15u) + 1, 1ull);
+}
+
 // Rays are 32-byte records read with two 128-bit loads (16-byte aligned buffer).
 BVHGPU_DEV bvhgpu_ray_t load_ray(const bvhgpu_ray_t* rays, uint64_t i) {
   const float4* p = reinterpret_cast<const float4*>(rays + i);
@@ -576,8 +594,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
     const uint32_t e = stack[sp * stride];
     if (DIST && dstack[sp * stride] > tmax) continue;
     if (e & kLeafBit) {
-      if (COUNT && a.depth_hist)
-        atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+      if (COUNT) count_leaf(sc, a, e);
       bool h = leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr);
       if (h) {
         hit = true;
@@ -592,7 +609,7 @@ __global__ void __launch_bounds__(128) trace_dfs_kernel(SceneDev sc, TraceArgs a
         best = Best();
         break;
       }
-      if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+      if (COUNT) count_node(a, depth);
       if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
     }
   }
@@ -790,8 +807,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
       if (log && set_insert(set, 2 * P, e))
         atomicAdd(is_node ? &ctl->unique_nodes : &ctl->unique_leaves, 1);
       auto leaf_visit = [&](uint32_t le) {
-        if (COUNT && a.depth_hist)
-          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[le & kLeafIndexMask], 63), 1ull);
+        if (COUNT) count_leaf(sc, a, le);
         Best best;
         best.leaf = best_leaf[ray];
         best.lane = (int)(int8_t)(misc & 0xFF);
@@ -820,7 +836,7 @@ __global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArg
           done = true;
           sp = 0;
         }
-        if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+        if (COUNT) count_node(a, depth);
         // intersectWide's schedule (compactNode.cpp:118-356, step log only):
         // a ray whose next entry is a leaf visits it in the same step.
         if (log && a.step_wide && !done && sp > 0 && (stacks[(sp - 1) * P + ray] & kLeafBit)) {
@@ -1070,15 +1086,14 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
             best = Best();
             sp = 0;
           }
-          if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+          if (COUNT) count_node(a, depth);
           if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
         }
       }
       if (active && sp > 0) {
         --sp;
         const uint32_t e = stack[sp * stride];
-        if (COUNT && a.depth_hist)
-          atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+        if (COUNT) count_leaf(sc, a, e);
         if (leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr)) {
           hit = true;
           if (KIND == BVHGPU_ANY) sp = 0;
@@ -1089,8 +1104,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
         --sp;
         const uint32_t e = stack[sp * stride];
         if (e & kLeafBit) {
-          if (COUNT && a.depth_hist)
-            atomicAdd(a.depth_hist + 64 + min((int)sc.leaf_depth[e & kLeafIndexMask], 63), 1ull);
+          if (COUNT) count_leaf(sc, a, e);
           if (leaf_step<PROFILE, KIND, COUNT>(sc, e, r, tmax, best, ctr)) {
             hit = true;
             if (KIND == BVHGPU_ANY) sp = 0;
@@ -1104,7 +1118,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
             best = Best();
             sp = 0;
           }
-          if (COUNT && a.depth_hist) atomicAdd(a.depth_hist + min(depth, 63), 1ull);
+          if (COUNT) count_node(a, depth);
           if (COUNT) ctr.max_stack = max(ctr.max_stack, (uint32_t)sp);
         }
       }

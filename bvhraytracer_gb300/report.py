@@ -5,12 +5,10 @@ value as the first number after a fixed key) can consume GPU results.
 * ``<name><problem>_Info.txt`` — CameraData::renderImage's traversal
   statistics (src/cameraData.h:241-325): per-ray node / leaf / box / triangle
   counts, success ratios, waste factors, traversal fullness and the per-depth
-  node and leaf visit histograms, for primary and secondary rays. The
-  averages of the fullness sections come from the counters (every node visit
-  tests all its children and every leaf visit all its triangles, so average
-  child fullness = box tests / node visits and average leaf fullness =
-  triangle tests / leaf visits); the per-count fullness lines of the
-  reference are not written because the kernels do not histogram them.
+  node and leaf visit histograms, for primary and secondary rays, and the
+  fullness sections (visits of nodes with x children and of leaves with x
+  triangles per primary ray, with their averages) from the kernels'
+  childFullness / primitiveFullness histograms.
 * ``WorkGroupSize_<wg>_Version_<v>/...`` — CameraData::workGroupAnalysisPerImage
   (cameraData.h:660-1105): the primary / secondary whisker plots of the
   termination steps per workgroup, ``_WorkGroupData.txt`` (per step: average
@@ -48,14 +46,20 @@ class RayStats:
     tri_hits: int
     node_depth: np.ndarray
     leaf_depth: np.ndarray
+    # visits of nodes with c children / leaves with c triangles ([17] each)
+    child_fullness: np.ndarray | None = None
+    prim_fullness: np.ndarray | None = None
 
     @classmethod
-    def from_trace(cls, counters, depth_hist, rays_counted: int | None = None) -> "RayStats":
+    def from_trace(cls, counters, depth_hist, rays_counted: int | None = None,
+                   fullness=None) -> "RayStats":
         c = np.asarray(_host(counters), np.int64).reshape(-1, 8)
         h = np.asarray(_host(depth_hist), np.int64).reshape(2, -1)
         s = c.sum(0)
+        f = None if fullness is None else np.asarray(_host(fullness), np.uint64).reshape(2, -1)
         return cls(int(rays_counted if rays_counted is not None else c.shape[0]), int(s[0]),
-                   int(s[1]), int(s[2]), int(s[3]), int(s[4]), int(s[5]), h[0], h[1])
+                   int(s[1]), int(s[2]), int(s[3]), int(s[4]), int(s[5]), h[0], h[1],
+                   None if f is None else f[0], None if f is None else f[1])
 
 
 def _host(x):
@@ -83,6 +87,22 @@ def _section(prefix: str, s: RayStats, branching: int) -> list[str]:
     ]
 
 
+def _fullness(title: str, avg: str, hist, bins: int, rays: int) -> list[str]:
+    """One fullness section as CameraData writes it (cameraData.h:267-294):
+    the float average sum(i * h[i]) / sum(h) (std::to_string) and per count
+    h[i] / rays in float (bins = N + 1 or L + 1 entries)."""
+    h = np.asarray(hist, np.uint64)[:bins]
+    acc = np.float32(0)
+    for i in range(bins):
+        acc = np.float32(acc + np.float32(int(h[i]) * i))
+    total = int(h.sum())
+    acc = np.float32(acc / np.float32(total)) if total else np.float32("nan")
+    factor = np.float32(1) / np.float32(max(rays, 1))
+    out = [title, f"{avg}{float(acc):.6f}"]
+    out += [f"{i} : {_fmt(float(np.float32(np.float32(int(h[i])) * factor)))}" for i in range(bins)]
+    return out
+
+
 def write_info(path: str, name: str, problem: str, branching: int, leaf_size: int,
                primary: RayStats, secondary: RayStats) -> str:
     """Writes ``<path>/<name><problem>_Info.txt``; returns the file name."""
@@ -92,12 +112,21 @@ def write_info(path: str, name: str, problem: str, branching: int, leaf_size: in
     lines += _section("secondary", secondary, branching) + [""]
     # Fullness is collected from primary rays only (collectPrimaryRayData,
     # cameraData.h:577-621).
-    lines += ["intersections with nodes with x children :",
-              "average child fullness: "
-              f"{primary.box_tests / max(primary.node_visits, 1):.6f}", "",
-              "intersections with leaf nodes with x primitives :",
-              "average leaf fullness: "
-              f"{primary.tri_tests / max(primary.leaf_visits, 1):.6f}"]
+    if primary.child_fullness is not None:
+        lines += _fullness("intersections with nodes with x children :",
+                           "average child fullness: ", primary.child_fullness, branching + 1,
+                           primary.rays)
+        lines += [""]
+        lines += _fullness("intersections with leaf nodes with x primitives :",
+                           "average leaf fullness: ", primary.prim_fullness, leaf_size + 1,
+                           primary.rays)
+    else:  # averages only, from the counters
+        lines += ["intersections with nodes with x children :",
+                  "average child fullness: "
+                  f"{primary.box_tests / max(primary.node_visits, 1):.6f}", "",
+                  "intersections with leaf nodes with x primitives :",
+                  "average leaf fullness: "
+                  f"{primary.tri_tests / max(primary.leaf_visits, 1):.6f}"]
     for title, hist, s in (("primary node intersections at depth x :", primary.node_depth, primary),
                            ("primary leaf intersections at depth x :", primary.leaf_depth, primary),
                            ("secondary node intersections at depth x :", secondary.node_depth,

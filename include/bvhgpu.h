@@ -229,12 +229,19 @@ typedef struct {
                         profiles. Same results (an any-hit ray's result does not depend
                         on the order in which its leaves are reached); short rays
                         (ambient occlusion) run faster, long rays toward a light slower. */
+  int32_t fullness;  /* nonzero (with depth_hist): depth_hist holds 2 x 64 + 2 x 17 uint64;
+                        after the per-depth rows come the reference's Ray::childFullness
+                        and primitiveFullness (ray.h:36-37, compactNode.cpp:655,716)
+                        summed over the rays: visits of nodes with c children
+                        (entry 128 + c) and of leaves with c triangles (entry 145 + c),
+                        c = 0..16. Instrumented and fast profile, every scheme. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):
  * node visits, leaf visits, box tests, box hits, triangle tests,
  * triangle hits, deepest stack, reserved. `depth_hist` (nullable):
- * 2 x 64 uint64, node visits then leaf visits per tree depth, accumulated. */
+ * 2 x 64 uint64, node visits then leaf visits per tree depth, accumulated;
+ * with opts.fullness, 2 x 17 more: the fullness histograms. */
 #define BVHGPU_COUNTERS_PER_RAY 8
 
 /* Device pointers. Closest: writes hits[n]. Any: writes occluded[n] (0/1).
@@ -453,6 +460,17 @@ int bvhgpu_trace_batches_noalloc(bvhgpu_scene_t scene, const bvhgpu_batch_t* bat
  * (rays, hits 16-byte aligned); stream-ordered. */
 int bvhgpu_fp64_check(bvhgpu_scene_t scene, const bvhgpu_ray_t* rays, const bvhgpu_hit_t* hits,
                       uint64_t n, int32_t profile, double* out, void* stream);
+
+/* ---- measurement ------------------------------------------------------- */
+/* No counterpart in the reference. Read bandwidth of `device` in GB/s: a
+ * buffer of `bytes` (allocated and freed inside the call) is read `passes`
+ * times by one L2-cached, L1-bypassing streaming kernel, timed with CUDA
+ * events `repeats` times; *gb_per_s is the median. A buffer that fits L2
+ * (129 MB on GB300) gives the L2 read ceiling of the traversal kernels when
+ * the BVH is L2-resident; a buffer far larger than L2 gives the HBM read
+ * rate. Synchronous (default stream). */
+int bvhgpu_read_bandwidth(int32_t device, uint64_t bytes, int32_t passes, int32_t repeats,
+                          double* gb_per_s);
 
 /* ---- ray generation on the GPU ----------------------------------------- */
 /* Pinhole camera of Camera::getRayTargetPosition (camera.h:82-98): pixel (w, h)

@@ -47,7 +47,7 @@ def test_status_codes_match_header():
 def test_struct_sizes_match_header_layout():
     assert C.sizeof(N.BuildParams) == 24
     assert C.sizeof(N.SceneParams) == 20
-    assert C.sizeof(N.TraceOpts) == 44
+    assert C.sizeof(N.TraceOpts) == 48
     assert C.sizeof(N.Job) == 56
 
 
@@ -255,3 +255,11 @@ def test_noalloc_python_binding_rejects_mismatched_buffers():
             check(r, k, o, "cpu")
     with pytest.raises(ValueError):  # buffers on another device than the scene
         check(rays, "closest", torch.zeros((6, 4), dtype=torch.float32), "cuda:0")
+
+
+def test_read_bandwidth_rejects_bad_arguments_without_a_gpu():
+    lib = N.lib()
+    g = C.c_double()
+    assert lib.bvhgpu_read_bandwidth(0, 1024, 1, 1, C.byref(g)) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_read_bandwidth(0, 1 << 20, 0, 1, C.byref(g)) == N.ERR_BAD_ARG
+    assert lib.bvhgpu_read_bandwidth(0, 1 << 20, 1, 1, None) == N.ERR_BAD_ARG

@@ -5,8 +5,8 @@ reference's SAH tree; tests/golden/make_golden.py).
 Every scheme traverses the reference's tree from the fixture (imported with
 bvhgpu_bvh_import_compact) in the instrumented profile, and must return the
 reference's hit triangle and t bit for bit, its occlusion results, and, with
-counters, its per-ray node / leaf / box / triangle counts and per-depth
-visits. 8-bit quantised nodes keep the same hits.
+counters, its per-ray node / leaf / box / triangle counts, per-depth visits
+and fullness histograms. 8-bit quantised nodes keep the same hits.
 """
 from pathlib import Path
 
@@ -63,6 +63,8 @@ def test_kernels_equal_reference_fixture(case, scheme, kw):
             assert np.array_equal(c, z[batch + "_counters"]), batch
             assert np.array_equal(r["depth_hist"].cpu().numpy().astype(np.uint64),
                                   z[batch + "_depth_hist"]), batch
+            assert np.array_equal(r["fullness"].cpu().numpy().astype(np.uint64),
+                                  z[batch + "_fullness"]), batch
     scene.status()
 
 

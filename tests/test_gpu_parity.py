@@ -35,6 +35,8 @@ def check_closest(got, ref, counters=True):
         gc = got["counters"].cpu().numpy().astype(np.uint32)[:, :7]
         assert np.array_equal(gc, ref["counters"][:, :7])
         assert np.array_equal(got["depth_hist"].cpu().numpy().astype(np.uint64), ref["depth_hist"])
+        if ref.get("fullness") is not None:
+            assert np.array_equal(got["fullness"].cpu().numpy().astype(np.uint64), ref["fullness"])
 
 
 def check_any(got, ref, counters=True):
@@ -43,6 +45,8 @@ def check_any(got, ref, counters=True):
         gc = got["counters"].cpu().numpy().astype(np.uint32)[:, :7]
         assert np.array_equal(gc, ref["counters"][:, :7])
         assert np.array_equal(got["depth_hist"].cpu().numpy().astype(np.uint64), ref["depth_hist"])
+        if ref.get("fullness") is not None:
+            assert np.array_equal(got["fullness"].cpu().numpy().astype(np.uint64), ref["fullness"])
 
 
 def _first_diff(g, r):

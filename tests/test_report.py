@@ -135,3 +135,24 @@ def test_whisker_from_step_log_matches_counters():
     want = np.concatenate([np.sort(steps[:4]), np.sort(steps[4:])])
     assert np.array_equal(from_log, want)
     assert R._whisker_rows(from_log, 4) == R._whisker_rows(steps, 4)
+
+
+def test_info_file_fullness_sections(tmp_path):
+    """The per-count fullness lines of CameraData (cameraData.h:267-294):
+    visits of nodes with x children and of leaves with x triangles per
+    primary ray, and their float averages, from the kernels' histograms."""
+    p, _, _ = _stats(0, 100)
+    s, _, _ = _stats(1, 300)
+    full = np.zeros((2, 17), np.uint64)
+    full[0, 2], full[0, 4] = 3, 5
+    full[1, 1], full[1, 3] = 7, 1
+    p = R.RayStats.from_trace(np.zeros((100, 8)), np.zeros((2, 64)), fullness=full)
+    fn = R.write_info(str(tmp_path), "clutter", "_b4_l3", 4, 3, p, s)
+    lines = open(fn).read().splitlines()
+    i = lines.index("intersections with nodes with x children :")
+    assert lines[i + 1] == "average child fullness: 3.250000"
+    assert lines[i + 2:i + 7] == ["0 : 0", "1 : 0", "2 : 0.03", "3 : 0", "4 : 0.05"]
+    j = lines.index("intersections with leaf nodes with x primitives :")
+    assert lines[j + 1] == "average leaf fullness: 1.250000"
+    assert lines[j + 2:j + 6] == ["0 : 0", "1 : 0.07", "2 : 0", "3 : 0.01"]
+    assert first_number("\n".join(lines), "average leaf fullness:") == 1.25
