@@ -36,18 +36,15 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mrays/s"
 
-# DRAM traffic per ray of the AO launch (persistent kernel, policy 2, FP32
-# nodes), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
-# of a 4,147,200-ray AO launch on the 251k-triangle clutter scene; the traffic
-# is the ray stream plus cold misses (the BVH stays in L2), so it grows with
-# the ray count and is scaled by it.
-# Source: profiles/trace_persistent_p2_ao_clutter250k_N8L8.md
-# With reordering the launch is the four reorder passes plus the trace (the
-# rays read once to bin them and once, gathered in bin order, by the trace;
-# the bins and the index permutation): the bench's plan, 6 x 10 x 10 bins and
-# child-index push order.
-# Source: profiles/traffic_ao_reorder_k10_anyorder_clutter250k_N8L8.md
-NCU_TRAFFIC_PER_AO_RAY = {0: 140371712 / 4147200, "reorder": 457373696 / 4147200}
+# DRAM bytes per AO ray (dram__bytes_read.sum + dram__bytes_write.sum) of
+# this workload's AO call (clutter 4,000 objects, N8L8, FP32 nodes;
+# persistent kernel, refill 24, 6 x 10 x 10 direction bins, child-index
+# order), from one ncu capture of `bench.py --workload aolaunch --steps 1
+# --warmup 1` (2,000,000 AO rays, an evenly strided sample of the frame's):
+# the trace kernel 91,570,688 B, the four reorder passes 70,398,208 B. The
+# traffic is the ray stream plus the BVH lines that miss L2, so it is scaled
+# to a launch by its ray count.
+NCU_DRAM_BYTES_PER_AO_RAY = {"trace": 91570688 / 2e6, "with_reorder": (91570688 + 70398208) / 2e6}
 
 
 def parse():
@@ -560,9 +557,9 @@ def run_ours(a):
     traffic = None
     dom_opts = chosen[dom][1]
     if (names[dom].startswith("AO") and dom_opts.get("scheme") == "persistent"
-            and dom_opts.get("policy") == 2 and chosen[dom][0].node_format == "fp32"):
-        key = "reorder" if dom_opts.get("reorder", 0) else 0
-        traffic = NCU_TRAFFIC_PER_AO_RAY[key] * int(batches[dom][0].shape[0])
+            and dom_opts.get("reorder") == 10 and chosen[dom][0].node_format == "fp32"
+            and a.objects == 4000 and a.branching == 8 and a.leaf == 8):
+        traffic = NCU_DRAM_BYTES_PER_AO_RAY["with_reorder"] * int(batches[dom][0].shape[0])
 
     compare = {}
     if not a.no_compare:
@@ -613,10 +610,9 @@ def run_ours(a):
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks
                 else "fallback",
                 "traffic": traffic,
-                "traffic_source": ("ncu DRAM bytes per AO ray of a 4.1M-ray capture on the "
-                                   "251k-triangle scene (with the reorder passes, K=10 and "
-                                   "child-index order, when the plan reorders), scaled by rays"
-                                   if traffic else None),
+                "traffic_source": ("ncu DRAM bytes per AO ray of the same scene's AO call "
+                                   "(trace kernel + reorder passes), captured on a 2M-ray "
+                                   "strided sample and scaled by rays" if traffic else None),
                 "algorithmic_bytes_per_launch": alg[dom]["bytes"],
                 "bytes_rule": "node visits x node record bytes + triangle tests x 36 B",
                 "l2_peak": l2_peak, "l2_frac": achieved / l2_peak,
@@ -937,6 +933,16 @@ def run_adjoint(a):
     print(json.dumps(line))
 
 
+# DRAM bytes per AO ray of the 8M-triangle scene's AO call (trace kernel +
+# the four reorder passes; policy 2, refill 24, 6 x 10 x 10 bins,
+# child-index order), from one ncu capture each of `bench.py --workload
+# aolaunch --objects 32000 --leaf 4 --ao 16 --steps 1 --warmup 1 [--nodes
+# q8]` (2,000,000 strided AO rays): FP32 165,708,544 + 70,393,600 B, Q8
+# 147,883,264 + 70,468,864 B.
+SCALE8M_DRAM_BYTES_PER_AO_RAY = {"fp32": (165708544 + 70393600) / 2e6,
+                                 "q8": (147883264 + 70468864) / 2e6}
+
+
 def run_scale(a):
     """Clutter scene scaled to ~8M triangles (32,000 objects), N8L4, one frame
     of 1920x1080 primary rays + 16 AO rays per hit: FP32 against Q8 nodes
@@ -946,6 +952,8 @@ def run_scale(a):
     import bvhraytracer_gb300 as pkg
     from bvhraytracer_gb300 import scenes as S
     dev = torch.device("cuda", 0)
+    pk = ROOT / "MEASURED_PEAKS.json"
+    hbm_peak = json.loads(pk.read_text()).get("hbm_gbs", 6800.0) if pk.exists() else 6800.0
     n_obj = 32000
     t0 = time.time()
     tris = S.clutter(n_obj, seed=1)
@@ -993,6 +1001,12 @@ def run_scale(a):
             "algorithmic_gb_per_s_ao": bytes_[1] / (ms[1] / 1e3) / 1e9,
             "_outs": outs,
         }
+        if o.get("reorder") == 10 and o.get("policy") in (2, 3):
+            # HBM side of the AO call from measured DRAM bytes per AO ray
+            dram = SCALE8M_DRAM_BYTES_PER_AO_RAY[name] * nrays[1]
+            res[name]["dram_bytes_per_ao_ray"] = SCALE8M_DRAM_BYTES_PER_AO_RAY[name]
+            res[name]["dram_gb_per_s_ao"] = dram / (ms[1] / 1e3) / 1e9
+            res[name]["hbm_frac_ao"] = res[name]["dram_gb_per_s_ao"] / hbm_peak
         sc.status()
     same_h = torch.equal(res["q8"]["_outs"][0].view(torch.int32), res["fp32"]["_outs"][0].view(torch.int32))
     same_a = torch.equal(res["q8"]["_outs"][1], res["fp32"]["_outs"][1])
@@ -1287,7 +1301,9 @@ def run_aolaunch(a):
     """The frame's AO batch alone, an evenly strided sample of --ao-sample
     rays, traced with the bench's AO plan (persistent kernel, speculative
     any-hit policy 2, refill 24, 6 x 10 x 10 direction bins, child-index push
-    order) --warmup + --steps times; node format --nodes. Prints the device
+    order; or the --plan specs "scheme,policy,refill,reorder,any_order"
+    joined by ';', each timed in turn and checked against the first)
+    --warmup + --steps times; node format --nodes. Prints per plan the device
     time and the algorithmic bytes per launch. It is the case the ncu DRAM
     captures of the AO launch use (a launch of about 2M rays keeps a capture
     short); the bytes per ray they measure scale with the ray count."""
@@ -1301,31 +1317,41 @@ def run_aolaunch(a):
     _, ao = secondaries(a, tris, primary, pkg.hit_prims(hits.cpu().numpy()))
     idx = np.unique(np.linspace(0, ao.shape[0] - 1, min(a.ao_sample, ao.shape[0])).astype(np.int64))
     rays = torch.from_numpy(ao[idx]).to(dev)
-    out = torch.empty(rays.shape[0], dtype=torch.uint8, device=dev)
-    plan = {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10, "any_order": True}
-    c = scene.trace(rays, kind="any", counters=True, **{k: v for k, v in plan.items()
-                                                         if k not in ("reorder", "any_order")})
+    plans = [{"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10, "any_order": True}]
+    if a.plan:
+        plans = []
+        for spec in a.plan.split(";"):
+            f = spec.split(",")
+            plans.append({"scheme": f[0], "policy": int(f[1]), "refill": int(f[2]),
+                          "reorder": int(f[3]), "any_order": bool(int(f[4]))})
+    c = scene.trace(rays, kind="any", counters=True, scheme="persistent", policy=0, refill=24)
     cs = c["counters"].to(torch.int64).sum(0).cpu().numpy()
     alg = int(cs[0]) * scene.node_record_bytes + int(cs[4]) * 36
     stream = torch.cuda.current_stream(dev)
-    for _ in range(a.warmup):
-        scene.trace(rays, kind="any", out=out, **plan)
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(a.steps):
-        scene.trace(rays, kind="any", out=out, **plan)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / max(a.steps, 1)
-    scene.status()
-    print(json.dumps({
-        "metric": METRIC, "value": rays.shape[0] / (ms / 1e3) / 1e6, "unit": METRIC,
-        "ms_per_launch": ms, "rays": int(rays.shape[0]), "workload": workload_name(a),
-        "nodes": a.nodes, "plan": plan, "triangles": int(bvh.info["n_tris"]),
-        "algorithmic_bytes_per_launch": alg, "node_record_bytes": scene.node_record_bytes,
-        "node_visits_per_ray": float(cs[0]) / rays.shape[0],
-        "tri_tests_per_ray": float(cs[4]) / rays.shape[0]}))
+    first = None
+    for plan in plans:
+        out = torch.empty(rays.shape[0], dtype=torch.uint8, device=dev)
+        for _ in range(a.warmup):
+            scene.trace(rays, kind="any", out=out, **plan)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            scene.trace(rays, kind="any", out=out, **plan)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / max(a.steps, 1)
+        scene.status()
+        if first is None:
+            first = out.clone()
+        print(json.dumps({
+            "metric": METRIC, "value": rays.shape[0] / (ms / 1e3) / 1e6, "unit": METRIC,
+            "ms_per_launch": ms, "rays": int(rays.shape[0]), "workload": workload_name(a),
+            "nodes": a.nodes, "plan": plan, "triangles": int(bvh.info["n_tris"]),
+            "same_as_first_plan": bool(torch.equal(out, first)),
+            "algorithmic_bytes_per_launch": alg, "node_record_bytes": scene.node_record_bytes,
+            "node_visits_per_ray": float(cs[0]) / rays.shape[0],
+            "tri_tests_per_ray": float(cs[4]) / rays.shape[0]}))
 
 
 def main():

@@ -135,7 +135,7 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (o->kind != BVHGPU_CLOSEST && o->kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "kind");
   if (o->scheme != BVHGPU_PER_RAY && o->scheme != BVHGPU_STREAM && o->scheme != BVHGPU_PERSISTENT)
     return set_error(BVHGPU_ERR_BAD_ARG, "scheme");
-  if (o->policy < 0 || o->policy > 2) return set_error(BVHGPU_ERR_BAD_ARG, "policy");
+  if (o->policy < 0 || o->policy > 3) return set_error(BVHGPU_ERR_BAD_ARG, "policy");
   if (o->refill < 0 || o->refill > 32) return set_error(BVHGPU_ERR_BAD_ARG, "refill");
   c.policy = o->policy;
   c.refill_min = o->refill ? o->refill : 8;
@@ -171,8 +171,11 @@ static int check_smem_fit(const dev::LaunchCfg& cfg, int cap) {
       dev::stream_smem_bytes(cfg.packet, cap, cfg.count) > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED,
                      "stream packet does not fit shared memory for this tree depth");
+  // persistent scheme: plus up to 8 KB of staged top levels and 6 KB of ray
+  // records (policy 3)
+  const size_t extra = cfg.scheme == BVHGPU_PERSISTENT ? 8192 + 128 * 48 : 0;
   if (cfg.scheme != BVHGPU_STREAM &&
-      (size_t)cap * 128 * 4 * (cfg.save_distance ? 2 : 1) > 227 * 1024)
+      (size_t)cap * 128 * 4 * (cfg.save_distance ? 2 : 1) + extra > 227 * 1024)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "stack does not fit shared memory for this tree depth");
   return BVHGPU_OK;
 }

@@ -953,6 +953,124 @@ struct QueueArgs {
 #ifndef BVHGPU_PERSIST_MIN_BLOCKS
 #define BVHGPU_PERSIST_MIN_BLOCKS 6
 #endif
+
+// POLICY 3: the ray constants a leaf test needs, one 48-byte record per
+// thread in shared memory (written when the lane takes the ray), so that any
+// lane of the warp can test a triangle for any other lane's ray.
+// Instrumented profile: origin, tMax | 1 / direction, shear x | shear y, z,
+// axes (kx | ky << 2 | kz << 4 | exact << 6). Fast profile: origin, tMax |
+// direction, 0 | 0, 0, exact << 6.
+constexpr int kRayRecWords = 12;
+// POLICY 3: leaves a lane may set aside before the warp tests them (1 or 2).
+#ifndef BVHGPU_SPEC_LEAVES
+#define BVHGPU_SPEC_LEAVES 2
+#endif
+
+template <int PROFILE>
+BVHGPU_DEV void store_ray_rec(float4* rec, const Ray& r) {
+  const int packed = r.kx | (r.ky << 2) | (r.code << 4) | ((r.exact ? 1 : 0) << 6);
+  if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) {
+    rec[0] = make_float4(r.o[0], r.o[1], r.o[2], r.tmax);
+    rec[1] = make_float4(r.inv[0], r.inv[1], r.inv[2], r.sx);
+    rec[2] = make_float4(r.sy, r.sz, __int_as_float(packed), 0.f);
+  } else {
+    rec[0] = make_float4(r.o[0], r.o[1], r.o[2], r.tmax);
+    rec[1] = make_float4(r.d[0], r.d[1], r.d[2], 0.f);
+    rec[2] = make_float4(0.f, 0.f, __int_as_float(packed), 0.f);
+  }
+}
+
+// The fields of a Ray that the leaf tests read, from its shared record.
+template <int PROFILE>
+BVHGPU_DEV Ray load_ray_rec(const float4* rec) {
+  Ray r;
+  const float4 a = rec[0], b = rec[1], c = rec[2];
+  const int packed = __float_as_int(c.z);
+  r.o[0] = a.x; r.o[1] = a.y; r.o[2] = a.z;
+  r.tmax = a.w;
+  if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) {
+    r.inv[0] = b.x; r.inv[1] = b.y; r.inv[2] = b.z;
+    r.sx = b.w; r.sy = c.x; r.sz = c.y;
+  } else {
+    r.d[0] = b.x; r.d[1] = b.y; r.d[2] = b.z;
+  }
+  r.kx = packed & 3;
+  r.ky = (packed >> 2) & 3;
+  r.code = (packed >> 4) & 3;
+  r.exact = (packed >> 6) & 1;
+  return r;
+}
+
+// POLICY 3 leaf phase: the leaves the warp's lanes set aside (e0 / e1, with
+// c0 / c1 triangles; 0 triangles where a slot is empty) form one pool of
+// (ray, triangle) pairs, and the 32 lanes test 32 pairs at a time: pair p
+// belongs to the lane j with off_j <= p < off_j + c0_j + c1_j (a warp prefix
+// sum), and a lane testing it reads ray j's record from shared memory. A
+// lane's result is the OR over its pairs, as testing its leaves one after
+// the other would give (any-hit, tMax fixed). Every lane of the warp calls it.
+template <int PROFILE>
+BVHGPU_DEV bool coop_leaf_phase(const SceneDev& sc, const float4* warp_recs, uint32_t e0,
+                                uint32_t e1, int c0, int c1, unsigned lane) {
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const int c = c0 + c1;
+  int incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(FULL, incl, d);
+    if ((int)lane >= d) incl += v;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
+  const int off = incl - c;
+  bool mine = false;
+  for (int base = 0; base < total; base += 32) {
+    const int p = base + (int)lane;
+    // Owner: the largest lane j with off_j <= p (lanes without pairs share
+    // the next lane's offset, so the largest such j has pairs when p < total).
+    int j = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int v = __shfl_sync(FULL, off, j + step);
+      if (v <= p) j += step;
+    }
+    const int off_j = __shfl_sync(FULL, off, j);
+    const uint32_t e0_j = __shfl_sync(FULL, e0, j), e1_j = __shfl_sync(FULL, e1, j);
+    const int c0_j = __shfl_sync(FULL, c0, j);
+    bool h = false;
+    if (p < total) {
+      const int q = p - off_j;
+      const uint32_t e = q < c0_j ? e0_j : e1_j;
+      const int i = q < c0_j ? q : q - c0_j;
+      const int cnt = (int)((e >> kLeafCountShift) & 15u) + 1;
+      const int stride = ((cnt - 1) / sc.gang + 1) * sc.gang;
+      const float* blk = sc.leaves + (size_t)(e & kLeafIndexMask) * 9 * sc.leaf_memory;
+      const Ray r = load_ray_rec<PROFILE>(warp_recs + (size_t)j * 3);
+      int ax0 = 0, ax1 = 1, ax2 = 2;
+      if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED) { ax0 = r.kx; ax1 = r.ky; ax2 = r.code; }
+      float pt[3][3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        pt[v][0] = __ldg(blk + (v * 3 + ax0) * stride + i);
+        pt[v][1] = __ldg(blk + (v * 3 + ax1) * stride + i);
+        pt[v][2] = __ldg(blk + (v * 3 + ax2) * stride + i);
+      }
+      float t, b1, b2;
+      if (PROFILE == BVHGPU_PROFILE_INSTRUMENTED)
+        h = r.exact ? watertight<false>(pt, r, r.tmax, t, b1, b2)
+                    : watertight<true>(pt, r, r.tmax, t, b1, b2);
+      else
+        h = moller_trumbore(pt, r, r.tmax, t, b1, b2);
+    }
+    const unsigned hits = __ballot_sync(FULL, h);
+    // This lane's pairs in the window [base, base + 32).
+    const int lo = min(max(off - base, 0), 32), hi = min(max(off + c - base, 0), 32);
+    if (hi > lo) {
+      const unsigned upto = hi == 32 ? FULL : ((1u << hi) - 1u);
+      const unsigned from = lo == 32 ? 0u : ~((1u << lo) - 1u);
+      if (hits & upto & from) mine = true;
+    }
+  }
+  return mine;
+}
 template <int N, int PROFILE, int KIND, bool COUNT, int POLICY, int FMT>
 __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
     trace_persistent_kernel(SceneDev sc, TraceArgs a, QueueArgs q) {
@@ -985,6 +1103,14 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
   const unsigned below = (1u << lane) - 1u;
   const int cap = a.stack_cap;
   constexpr unsigned FULL = 0xFFFFFFFFu;
+  // POLICY 3: per-thread ray records after the top levels (16-byte aligned).
+  float4* ray_recs = reinterpret_cast<float4*>(
+      top_smem + (((size_t)top * NodeFmt<N, FMT>::REC + 15) / 16) * 16);
+  float4* my_rec = ray_recs + (size_t)threadIdx.x * 3;
+  const float4* warp_recs = ray_recs + (size_t)(threadIdx.x & ~31u) * 3;
+  uint32_t post1 = 0xFFFFFFFFu;  // POLICY 3: second leaf set aside
+  (void)my_rec;
+  (void)warp_recs;
 
   Ray r;
   float tmax = 0.f;
@@ -1023,6 +1149,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
             stack[0] = sc.root_entry;
             sp = 1;
             active = true;
+            if (POLICY == 3) store_ray_rec<PROFILE>(my_rec, r);
           }
         }
       }
@@ -1032,7 +1159,58 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
       continue;
     }
 
-    if (POLICY == 2) {
+    if (POLICY == 3) {
+      // Any-hit rays without counters, speculative with two leaves per lane:
+      // a lane sets aside the leaves it reaches (up to two) and keeps
+      // visiting nodes while another lane still has no leaf; then the warp
+      // tests all set-aside leaves together, 32 (ray, triangle) pairs at a
+      // time (coop_leaf_phase). A ray whose leaves hit is done; the others
+      // go on. Whether an any-hit ray is occluded does not depend on the
+      // order in which its reachable leaves are tested (tMax does not
+      // change), so results equal the depth-first order's; a leaf that the
+      // depth-first order would have skipped after an earlier hit costs
+      // work but changes no result.
+      constexpr bool kTwo = BVHGPU_SPEC_LEAVES >= 2;
+      while (true) {
+        while (active && sp > 0 && (kTwo ? post1 : postponed) == 0xFFFFFFFFu &&
+               (stack[(sp - 1) * stride] & kLeafBit) != 0u) {
+          --sp;
+          const uint32_t le = stack[sp * stride];
+          if (postponed == 0xFFFFFFFFu) postponed = le;
+          else post1 = le;
+        }
+        const bool want = active && sp > 0 && (kTwo ? post1 : postponed) == 0xFFFFFFFFu &&
+                          (stack[(sp - 1) * stride] & kLeafBit) == 0u;
+        const unsigned holding =
+            __ballot_sync(FULL, !active || postponed != 0xFFFFFFFFu || sp == 0);
+        if (__ballot_sync(FULL, want) == 0 || holding == FULL) break;
+        if (want) {
+          --sp;
+          const uint32_t e = stack[sp * stride];
+          int depth;
+          if (!node_step<N, PROFILE, KIND, COUNT, FMT>(sc, e, top_smem, top, r, tmax, stack,
+                                                       stride, sp, cap, ctr, depth)) {
+            record_error(sc.status, kDevErrStackOverflow);
+            hit = false;
+            sp = 0;
+            postponed = post1 = 0xFFFFFFFFu;
+          }
+        }
+      }
+      const bool holds = active && postponed != 0xFFFFFFFFu;
+      if (__ballot_sync(FULL, holds) != 0) {
+        const uint32_t e0 = holds ? postponed : 0u;
+        const uint32_t e1 = (holds && post1 != 0xFFFFFFFFu) ? post1 : 0u;
+        const int c0 = holds ? (int)((e0 >> kLeafCountShift) & 15u) + 1 : 0;
+        const int c1 = (holds && post1 != 0xFFFFFFFFu) ? (int)((e1 >> kLeafCountShift) & 15u) + 1 : 0;
+        __syncwarp();  // the lanes' ray records are visible to the whole warp
+        if (coop_leaf_phase<PROFILE>(sc, warp_recs, e0, e1, c0, c1, lane) && holds) {
+          hit = true;
+          sp = 0;
+        }
+        postponed = post1 = 0xFFFFFFFFu;
+      }
+    } else if (POLICY == 2) {
       // Any-hit rays without counters: a lane that reaches a leaf sets it
       // aside and keeps visiting nodes until every lane holds a leaf (or has
       // no node left); then all lanes test their leaf together. Whether an

@@ -25,8 +25,11 @@ TREE = ("lo3", "hi3", "child_begin", "child_count", "prim_begin", "prim_count", 
 SCHEMES = [("per_ray", {}), ("per_ray", {"stack": "local"}), ("per_ray", {"save_distance": True}),
            ("stream", {}), ("persistent", {"policy": 0}), ("persistent", {"policy": 1, "refill": 1}),
            ("persistent", {"policy": 2, "refill": 24}),
-           ("persistent", {"policy": 2, "refill": 24, "reorder": 10})]
-IDS = ["per_ray", "per_ray_local", "per_ray_dist", "stream", "ww", "ifif", "spec", "spec_reorder"]
+           ("persistent", {"policy": 2, "refill": 24, "reorder": 10}),
+           ("persistent", {"policy": 3, "refill": 24}),
+           ("persistent", {"policy": 3, "refill": 24, "reorder": 10, "any_order": True})]
+IDS = ["per_ray", "per_ray_local", "per_ray_dist", "stream", "ww", "ifif", "spec", "spec_reorder",
+       "coop", "coop_reorder_anyorder"]
 
 
 @pytest.fixture(scope="module", params=GOLDEN, ids=[p.stem for p in GOLDEN])
@@ -38,6 +41,17 @@ def case(request):
     return z, bvh, pkg.Scene(bvh)
 
 
+def _check_results(z, batch, kind, r):
+    if kind == "any":
+        assert np.array_equal(r["occluded"].cpu().numpy(), z[batch + "_occluded"]), batch
+    else:
+        h = r["hits"].cpu().numpy()
+        prim = h.view(np.int32)[:, 0]
+        assert np.array_equal(prim, z[batch + "_prim"]), batch
+        hit = prim >= 0
+        assert np.array_equal(h[hit, 1].view(np.uint32), z[batch + "_t"][hit].view(np.uint32))
+
+
 @pytest.mark.parametrize("scheme,kw", SCHEMES, ids=IDS)
 def test_kernels_equal_reference_fixture(case, scheme, kw):
     z, bvh, scene = case
@@ -45,19 +59,18 @@ def test_kernels_equal_reference_fixture(case, scheme, kw):
         if kw.get("save_distance") and kind == "any":
             continue
         rays = torch.from_numpy(z[batch + "_rays"]).cuda()
-        # reordered launches take no counters; save-distance skips pops, so
-        # its counters are its own (its hits are the reference's)
-        counting = not kw.get("reorder") and not kw.get("save_distance")
-        r = scene.trace(rays, kind=kind, scheme=scheme, counters=counting, depth_hist=counting,
-                        **kw)
-        if kind == "any":
-            assert np.array_equal(r["occluded"].cpu().numpy(), z[batch + "_occluded"]), batch
-        else:
-            h = r["hits"].cpu().numpy()
-            prim = h.view(np.int32)[:, 0]
-            assert np.array_equal(prim, z[batch + "_prim"]), batch
-            hit = prim >= 0
-            assert np.array_equal(h[hit, 1].view(np.uint32), z[batch + "_t"][hit].view(np.uint32))
+        # Without counters every option runs its own kernel (with counters the
+        # speculative any-hit policies run the counting one). Save-distance
+        # skips pops, so its counters are its own (its hits are the
+        # reference's); reordered and any_order launches are compared on
+        # results.
+        r = scene.trace(rays, kind=kind, scheme=scheme, **kw)
+        _check_results(z, batch, kind, r)
+        counting = not (kw.get("reorder") or kw.get("save_distance") or kw.get("any_order"))
+        if not counting:
+            continue
+        r = scene.trace(rays, kind=kind, scheme=scheme, counters=True, depth_hist=True, **kw)
+        _check_results(z, batch, kind, r)
         if counting:
             c = r["counters"].cpu().numpy().astype(np.uint32)[:, :6]
             assert np.array_equal(c, z[batch + "_counters"]), batch

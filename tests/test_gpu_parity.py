@@ -16,8 +16,10 @@ pytestmark = pytest.mark.gpu
 LIGHT = [2.0, 3.0, 2.0]
 # (scheme, extra trace options): every traversal scheme and persistent policy
 SCHEMES = [("per_ray", {}), ("stream", {}), ("persistent", {"policy": 0}),
-           ("persistent", {"policy": 1, "refill": 1}), ("persistent", {"policy": 2, "refill": 16})]
-SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1", "persistent_spec"]
+           ("persistent", {"policy": 1, "refill": 1}), ("persistent", {"policy": 2, "refill": 16}),
+           ("persistent", {"policy": 3, "refill": 24})]
+SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1", "persistent_spec",
+              "persistent_coop"]
 
 
 def dev(a):
@@ -589,7 +591,9 @@ def test_any_order_keeps_any_hit_results(profile, fmt):
         d = dev(sec)
         for scheme, kw in (("per_ray", {}), ("per_ray", {"stack": "local"}),
                            ("stream", {}), ("persistent", {"policy": 0, "refill": 8}),
-                           ("persistent", {"policy": 2, "refill": 24, "reorder": 10})):
+                           ("persistent", {"policy": 2, "refill": 24, "reorder": 10}),
+                           ("persistent", {"policy": 3, "refill": 24, "reorder": 10}),
+                           ("persistent", {"policy": 3, "refill": 8})):
             if fmt == "q8" and scheme == "stream":
                 continue
             got = scene.trace(d, kind="any", scheme=scheme, profile=profile, any_order=True,
