@@ -218,9 +218,11 @@ def sample_packets(rays: np.ndarray, frac: float, packet: int = 256) -> np.ndarr
 
 
 def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=5):
-    """The oracle's restatement of the reference's ISPC fast path
+    """The restatement of the reference's ISPC fast path
     (intersectWideAlternative / intersectSecondaryWideAlternative, 16x16
-    workgroups, OpenMP dynamic scheduling) on a sample of the frame."""
+    workgroups, OpenMP dynamic scheduling) with the ISPC kernels' gang lanes
+    as 4-wide vectors (oracle/_build/libcpubaseline.so, -O3), on a sample of
+    the frame."""
     from oracle import oracle as O
     cv = O.CompactView(bvh.export_compact())
     fv = O.FastView(bvh.export_fast(gang=4))
@@ -233,7 +235,7 @@ def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=5):
         t0 = time.perf_counter()
         for r, any_hit in sample:
             O.trace_fast(fv, cv, r, any_hit, packet=256, threads=cores, counters=False,
-                         outputs=True)
+                         outputs=True, baseline=True)
         return time.perf_counter() - t0
 
     once()  # warm-up, like the reference's first render
@@ -241,8 +243,8 @@ def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=5):
     med = statistics.median(ts)
     return {"value": n / med / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": f"{n} rays (every {int(round(1 / frac))}th 256-ray packet of each batch "
-                      "of the frame), fast profile, "
-                      f"ray-stream 16x16 packets, median of {repeats} after 1 warm-up",
+                      "of the frame), fast profile (ISPC kernels with 4-wide vector gang lanes, "
+                      f"-O3), ray-stream 16x16 packets, median of {repeats} after 1 warm-up",
             "seconds": med}
 
 
@@ -279,18 +281,27 @@ def oracle_check(a, bvh, batches, device_outs, host_outs, rays_per_batch=24_000)
 
 
 def run_reference(a):
+    """The reference's CPU path (the restated ISPC fast path, vectorised,
+    OpenMP on every host core) on a bounded sample of the frame. Nothing of
+    the product library runs here: the tree comes from the oracle's C
+    restatement of the reference's SAH builder (oracle/sah_builder.c) and the
+    FastNodeManager arrays from the oracle's restatement of its constructor;
+    the scene and rays come from the numpy generators of
+    bvhraytracer_gb300.scenes."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    import bvhraytracer_gb300 as pkg  # noqa: F401  (host builder only)
+    from bvhraytracer_gb300 import scenes as S  # numpy scene generators only
     from oracle import oracle as O
-    tris, bvh, primary = make_frame(a)
-    cv = O.CompactView(bvh.export_compact())
-    fv = O.FastView(bvh.export_fast(gang=4))
+    tris = S.clutter(a.objects, seed=1)
+    primary = S.clutter_camera(a.objects, a.width, a.height)
+    tree = O.build_tree(tris, a.branching, a.leaf)
+    cv = O.CompactView(tree)
+    fv = O.FastView(O.fast_arrays(tree, gang=4))
     # Secondary rays from the oracle's own primary hits on the sample.
     frac = a.ref_sample
     ps = sample_packets(primary, frac)
-    hits = O.trace_fast(fv, cv, ps, False, packet=256, counters=False)["hits"]
+    hits = O.trace_fast(fv, cv, ps, False, packet=256, counters=False, baseline=True)["hits"]
     prims = hits.view(np.int32)[:, 0]
     shadow, ao = secondaries(a, tris, ps, prims)
     sample = [(ps, False), (shadow, True), (ao, True)]
@@ -300,7 +311,8 @@ def run_reference(a):
     def step():
         t0 = time.perf_counter()
         for r, any_hit in sample:
-            O.trace_fast(fv, cv, r, any_hit, packet=256, threads=cores, counters=False)
+            O.trace_fast(fv, cv, r, any_hit, packet=256, threads=cores, counters=False,
+                         baseline=True)
         return time.perf_counter() - t0
 
     for _ in range(a.warmup):
@@ -316,7 +328,10 @@ def run_reference(a):
         "config": {"workload": workload_name(a), "sample": f"{n} rays per step (every "
                    f"{int(round(1 / frac))}th 256-ray packet of the frame's primary rays and "
                    "their secondaries)", "profile": "fast",
-                   "scheme": "ray-stream 16x16 packets"},
+                   "scheme": "ray-stream 16x16 packets",
+                   "kernels": "ISPC kernels restated with 4-wide vector gang lanes, -O3 "
+                              "(oracle/_build/libcpubaseline.so)",
+                   "tree": "oracle/sah_builder.c (the reference's SAH builder restated in C)"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
                          "sample": f"{n} rays per step"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -135,7 +135,7 @@ static int check_opts(const bvhgpu_trace_opts_t* o, dev::LaunchCfg& c) {
   if (o->kind != BVHGPU_CLOSEST && o->kind != BVHGPU_ANY) return set_error(BVHGPU_ERR_BAD_ARG, "kind");
   if (o->scheme != BVHGPU_PER_RAY && o->scheme != BVHGPU_STREAM && o->scheme != BVHGPU_PERSISTENT)
     return set_error(BVHGPU_ERR_BAD_ARG, "scheme");
-  if (o->policy < 0 || o->policy > 3) return set_error(BVHGPU_ERR_BAD_ARG, "policy");
+  if (o->policy < 0 || o->policy > 4) return set_error(BVHGPU_ERR_BAD_ARG, "policy");
   if (o->refill < 0 || o->refill > 32) return set_error(BVHGPU_ERR_BAD_ARG, "refill");
   c.policy = o->policy;
   c.refill_min = o->refill ? o->refill : 8;

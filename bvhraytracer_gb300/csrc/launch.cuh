@@ -15,7 +15,8 @@ struct LaunchCfg {
   int block = 128;      // per-ray scheme threads per block
   int packet = 256;     // stream scheme rays per block
   int policy = 0;       // persistent scheme: 0 while-while, 1 if-if, 2 speculative any-hit,
-                        // 3 speculative any-hit with two leaves per lane, tested warp-wide
+                        // 3 the same with two leaves per lane, 4 as 3 with the leaves
+                        // tested warp-wide
   int refill_min = 8;   // persistent scheme: idle lanes that trigger a refill
   unsigned long long* queue = nullptr;  // persistent scheme: queue head
   bool queue_cleared = false;  // true: the caller zeroed the head already
@@ -58,17 +59,19 @@ inline cudaError_t launch_one(const SceneDev& sc, const TraceArgs& a, const Laun
     k<<<(unsigned)grid, bs, smem, s>>>(sc, a);
   } else if (cfg.scheme == BVHGPU_PERSISTENT) {
     const int bs = 128;
-    // Policies 2 and 3 change the order of leaf tests, which only any-hit
+    // Policies 2 to 4 change the order of leaf tests, which only any-hit
     // rays without counters may do; the others fall back to policy 0.
     constexpr bool kSpec = KIND == BVHGPU_ANY && !COUNT;
-    const bool coop = cfg.policy == 3 && kSpec;
+    const bool coop = cfg.policy == 4 && kSpec;
     const size_t smem = (size_t)a.stack_cap * bs * 4 +
                         ((size_t)cfg.top_nodes * NodeFmt<NM, FMT>::REC + 15) / 16 * 16 +
                         (coop ? (size_t)bs * kRayRecWords * 4 : 0);
     auto k = cfg.policy == 1 ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 1, FMT>
              : (cfg.policy == 2 && kSpec)
                  ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, (kSpec ? 2 : 0), FMT>
-             : coop ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, (kSpec ? 3 : 0), FMT>
+             : (cfg.policy == 3 && kSpec)
+                 ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, (kSpec ? 3 : 0), FMT>
+             : coop ? trace_persistent_kernel<NM, PROFILE, KIND, COUNT, (kSpec ? 4 : 0), FMT>
                     : trace_persistent_kernel<NM, PROFILE, KIND, COUNT, 0, FMT>;
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;

@@ -954,14 +954,14 @@ struct QueueArgs {
 #define BVHGPU_PERSIST_MIN_BLOCKS 6
 #endif
 
-// POLICY 3: the ray constants a leaf test needs, one 48-byte record per
+// POLICY 4: the ray constants a leaf test needs, one 48-byte record per
 // thread in shared memory (written when the lane takes the ray), so that any
 // lane of the warp can test a triangle for any other lane's ray.
 // Instrumented profile: origin, tMax | 1 / direction, shear x | shear y, z,
 // axes (kx | ky << 2 | kz << 4 | exact << 6). Fast profile: origin, tMax |
 // direction, 0 | 0, 0, exact << 6.
 constexpr int kRayRecWords = 12;
-// POLICY 3: leaves a lane may set aside before the warp tests them (1 or 2).
+// POLICIES 3 and 4: leaves a lane may set aside per round (1 or 2).
 #ifndef BVHGPU_SPEC_LEAVES
 #define BVHGPU_SPEC_LEAVES 2
 #endif
@@ -1001,7 +1001,7 @@ BVHGPU_DEV Ray load_ray_rec(const float4* rec) {
   return r;
 }
 
-// POLICY 3 leaf phase: the leaves the warp's lanes set aside (e0 / e1, with
+// POLICY 4 leaf phase: the leaves the warp's lanes set aside (e0 / e1, with
 // c0 / c1 triangles; 0 triangles where a slot is empty) form one pool of
 // (ray, triangle) pairs, and the 32 lanes test 32 pairs at a time: pair p
 // belongs to the lane j with off_j <= p < off_j + c0_j + c1_j (a warp prefix
@@ -1103,12 +1103,12 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
   const unsigned below = (1u << lane) - 1u;
   const int cap = a.stack_cap;
   constexpr unsigned FULL = 0xFFFFFFFFu;
-  // POLICY 3: per-thread ray records after the top levels (16-byte aligned).
+  // POLICY 4: per-thread ray records after the top levels (16-byte aligned).
   float4* ray_recs = reinterpret_cast<float4*>(
       top_smem + (((size_t)top * NodeFmt<N, FMT>::REC + 15) / 16) * 16);
   float4* my_rec = ray_recs + (size_t)threadIdx.x * 3;
   const float4* warp_recs = ray_recs + (size_t)(threadIdx.x & ~31u) * 3;
-  uint32_t post1 = 0xFFFFFFFFu;  // POLICY 3: second leaf set aside
+  uint32_t post1 = 0xFFFFFFFFu;  // POLICIES 3, 4: second leaf set aside
   (void)my_rec;
   (void)warp_recs;
 
@@ -1149,7 +1149,7 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
             stack[0] = sc.root_entry;
             sp = 1;
             active = true;
-            if (POLICY == 3) store_ray_rec<PROFILE>(my_rec, r);
+            if (POLICY == 4) store_ray_rec<PROFILE>(my_rec, r);
           }
         }
       }
@@ -1159,17 +1159,18 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
       continue;
     }
 
-    if (POLICY == 3) {
+    if (POLICY == 3 || POLICY == 4) {
       // Any-hit rays without counters, speculative with two leaves per lane:
       // a lane sets aside the leaves it reaches (up to two) and keeps
-      // visiting nodes while another lane still has no leaf; then the warp
-      // tests all set-aside leaves together, 32 (ray, triangle) pairs at a
-      // time (coop_leaf_phase). A ray whose leaves hit is done; the others
-      // go on. Whether an any-hit ray is occluded does not depend on the
-      // order in which its reachable leaves are tested (tMax does not
-      // change), so results equal the depth-first order's; a leaf that the
-      // depth-first order would have skipped after an earlier hit costs
-      // work but changes no result.
+      // visiting nodes while another lane still has no leaf. Then each lane
+      // tests its set-aside leaves in turn (POLICY 3; the second only if the
+      // first has no hit), or the warp tests all of them together, 32 (ray,
+      // triangle) pairs at a time (POLICY 4, coop_leaf_phase). A ray whose
+      // leaves hit is done; the others go on. Whether an any-hit ray is
+      // occluded does not depend on the order in which its reachable leaves
+      // are tested (tMax does not change), so results equal the depth-first
+      // order's; a leaf that the depth-first order would have skipped after
+      // an earlier hit costs work but changes no result.
       constexpr bool kTwo = BVHGPU_SPEC_LEAVES >= 2;
       while (true) {
         while (active && sp > 0 && (kTwo ? post1 : postponed) == 0xFFFFFFFFu &&
@@ -1198,7 +1199,18 @@ __global__ void __launch_bounds__(128, BVHGPU_PERSIST_MIN_BLOCKS)
         }
       }
       const bool holds = active && postponed != 0xFFFFFFFFu;
-      if (__ballot_sync(FULL, holds) != 0) {
+      if (POLICY == 3) {
+        if (holds) {
+          bool h = leaf_step<PROFILE, KIND, COUNT>(sc, postponed, r, tmax, best, ctr);
+          if (!h && post1 != 0xFFFFFFFFu)
+            h = leaf_step<PROFILE, KIND, COUNT>(sc, post1, r, tmax, best, ctr);
+          if (h) {
+            hit = true;
+            sp = 0;
+          }
+        }
+        postponed = post1 = 0xFFFFFFFFu;
+      } else if (__ballot_sync(FULL, holds) != 0) {
         const uint32_t e0 = holds ? postponed : 0u;
         const uint32_t e1 = (holds && post1 != 0xFFFFFFFFu) ? post1 : 0u;
         const int c0 = holds ? (int)((e0 >> kLeafCountShift) & 15u) + 1 : 0;

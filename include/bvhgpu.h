@@ -202,10 +202,10 @@ typedef struct {
   int32_t workgroup; /* stream scheme: packet = workgroup^2 rays (8, 16); 0 = 16 */
   int32_t block;     /* per-ray scheme: threads per block (32, 64, 128; 0 = 128) */
   int32_t policy;    /* persistent scheme: 0 while-while, 1 if-if, 2 while-while with
-                        one leaf per lane set aside, 3 while-while with up to two leaves
-                        per lane set aside and the warp's set-aside leaves tested as one
-                        pool of (ray, triangle) pairs, 32 at a time (2 and 3: any-hit
-                        rays without counters; else 0) */
+                        one leaf per lane set aside, 3 the same with up to two leaves per
+                        lane, 4 as 3 with the warp's set-aside leaves tested as one pool
+                        of (ray, triangle) pairs, 32 at a time (2 to 4: any-hit rays
+                        without counters; else 0) */
   int32_t refill;    /* persistent scheme: idle lanes of a warp that trigger a refill
                         (1..32; 0 = 8) */
   int32_t save_distance; /* per-ray scheme, nonzero: the save-distance traversal of

@@ -676,6 +676,156 @@ static int tri_any_hit(const oracle_fast_t* f, uint32_t begin, int stride, int r
   return result;
 }
 
+
+#ifdef ORACLE_SIMD
+/* ------------------------------------------- vectorised gang kernels -- */
+/* The CPU baseline build (-DORACLE_SIMD -O3, oracle/build_oracle.py): the
+ * ISPC kernels with their gang lanes as 4-wide GCC vectors (SSE on x86-64,
+ * NEON on aarch64; the reference's SSE4 target has gang 4), each lane doing
+ * exactly the scalar lane's float operations in the same order, so results
+ * equal the scalar restatement's bit for bit. Used where the loop count is a
+ * multiple of 4; the traversal loops around them are shared. */
+typedef float v4f __attribute__((vector_size(16)));
+typedef int32_t v4i __attribute__((vector_size(16)));
+
+static inline v4f vld(const float* p) { v4f v; memcpy(&v, p, 16); return v; }
+static inline v4f vsplat(float x) { v4f v = {x, x, x, x}; return v; }
+static inline v4f vsel(v4i m, v4f a, v4f b) { /* m ? a : b */
+  return (v4f)(((v4i)a & m) | ((v4i)b & ~m));
+}
+static inline v4i vseli(v4i m, v4i a, v4i b) { return (a & m) | (b & ~m); }
+static inline int vany(v4i m) { return (m[0] | m[1] | m[2] | m[3]) != 0; }
+static inline uint32_t vbits(v4i m) {
+  return (uint32_t)((m[0] & 1) | (m[1] & 2) | (m[2] & 4) | (m[3] & 8));
+}
+
+/* Moller-Trumbore on 4 triangles (rows of a leaf block at column i). */
+static inline v4i mt4(const float* blk, int i, int stride, const oray_t* r, float tmax,
+                      v4f* t_out, v4f* b1_out, v4f* b2_out) {
+  const v4f p0x = vld(blk + i), p0y = vld(blk + i + stride), p0z = vld(blk + i + stride * 2);
+  const v4f p1x = vld(blk + i + stride * 3), p1y = vld(blk + i + stride * 4);
+  const v4f p1z = vld(blk + i + stride * 5);
+  const v4f p2x = vld(blk + i + stride * 6), p2y = vld(blk + i + stride * 7);
+  const v4f p2z = vld(blk + i + stride * 8);
+  const v4f d0 = vsplat(r->d[0]), d1 = vsplat(r->d[1]), d2 = vsplat(r->d[2]);
+  const v4f e1x = p1x - p0x, e1y = p1y - p0y, e1z = p1z - p0z;
+  const v4f e2x = p2x - p0x, e2y = p2y - p0y, e2z = p2z - p0z;
+  const v4f s1x = d1 * e2z - d2 * e2y, s1y = d2 * e2x - d0 * e2z, s1z = d0 * e2y - d1 * e2x;
+  const v4f divisor = s1x * e1x + s1y * e1y + s1z * e1z;
+  v4i hit = ~(divisor == vsplat(0.f));
+  const v4f inv_div = vsplat(1.f) / divisor;
+  const v4f dx = vsplat(r->o[0]) - p0x, dy = vsplat(r->o[1]) - p0y, dz = vsplat(r->o[2]) - p0z;
+  const v4f b1 = (dx * s1x + dy * s1y + dz * s1z) * inv_div;
+  hit &= ~((b1 < vsplat(0.f)) | (b1 > vsplat(1.f)));
+  const v4f s2x = dy * e1z - dz * e1y, s2y = dz * e1x - dx * e1z, s2z = dx * e1y - dy * e1x;
+  const v4f b2 = (d0 * s2x + d1 * s2y + d2 * s2z) * inv_div;
+  hit &= ~((b2 < vsplat(0.f)) | (b1 + b2 > vsplat(1.f)));
+  const v4f t = (e2x * s2x + e2y * s2y + e2z * s2z) * inv_div;
+  hit &= ~((t < vsplat(0.f)) | (t > vsplat(tmax)));
+  *t_out = t;
+  *b1_out = b1;
+  *b2_out = b2;
+  return hit;
+}
+
+static int tri_any_hit_v(const oracle_fast_t* f, uint32_t begin, int stride, int real,
+                         const oray_t* r, octr_t* c) {
+  const float* blk = f->tri_points + begin;
+  v4i any = {0, 0, 0, 0};
+  for (int i = 0; i < stride; i += 4) {
+    v4f t, b1, b2;
+    const v4i hit = mt4(blk, i, stride, r, r->tmax, &t, &b1, &b2);
+    if (c) {
+      const uint32_t bits = vbits(hit);
+      for (int k = 0; k < 4; ++k)
+        if ((bits >> k & 1u) && i + k < real) c->tri_hits++;
+    }
+    any |= hit;
+  }
+  return vany(any);
+}
+
+/* triIntersect{L}: lane i % gang keeps its first minimum below its running
+ * value (rayTracerTemplate.ispc:28-101); gang 4 or 8 (one or two vectors of
+ * lane state). */
+static int tri_intersect_v(const oracle_fast_t* f, uint32_t begin, int stride, int real,
+                           oray_t* r, float* u, float* v, octr_t* c) {
+  const int gang = f->gang;
+  v4f ts[2] = {vsplat(1000000.f), vsplat(1000000.f)};
+  v4i orig[2] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
+  v4f us[2] = {vsplat(0.f), vsplat(0.f)}, vs[2] = {vsplat(0.f), vsplat(0.f)};
+  v4i result = {0, 0, 0, 0};
+  const float* blk = f->tri_points + begin;
+  const float tmax = r->tmax;
+  for (int i = 0; i < stride; i += 4) {
+    const int g = (i % gang) / 4;
+    v4f t, b1, b2;
+    const v4i hit = mt4(blk, i, stride, r, tmax, &t, &b1, &b2);
+    if (c) {
+      const uint32_t bits = vbits(hit);
+      for (int k = 0; k < 4; ++k)
+        if ((bits >> k & 1u) && i + k < real) c->tri_hits++;
+    }
+    const v4i m = hit & (ts[g] > t);
+    const v4i idx = {i, i + 1, i + 2, i + 3};
+    ts[g] = vsel(m, t, ts[g]);
+    orig[g] = vseli(m, idx, orig[g]);
+    us[g] = vsel(m, b1, us[g]);
+    vs[g] = vsel(m, b2, vs[g]);
+    result |= m;
+  }
+  if (!vany(result)) return -1;
+  float tl[8], ul[8], vl[8];
+  int ol[8];
+  for (int l = 0; l < gang; ++l) {
+    tl[l] = ts[l / 4][l % 4];
+    ol[l] = orig[l / 4][l % 4];
+    ul[l] = us[l / 4][l % 4];
+    vl[l] = vs[l / 4][l % 4];
+  }
+  float best = tl[0];
+  for (int l = 1; l < gang; ++l) best = rmin(best, tl[l]);
+  int idx = -1, wl = -1;
+  for (int l = 0; l < gang; ++l)
+    if (tl[l] == best && ol[l] > idx) { idx = ol[l]; wl = l; }
+  r->tmax = best;
+  *u = ul[wl];
+  *v = vl[wl];
+  return idx;
+}
+
+/* aabbIntersect over 4 children at a time; bits of the real children. */
+static uint32_t aabb_intersect_v(const float* bd, int real, uint32_t cc, const oray_t* r,
+                                 float* dist) {
+  uint32_t mask = 0;
+  const v4f ox = vsplat(r->o[0]), oy = vsplat(r->o[1]), oz = vsplat(r->o[2]);
+  const v4f ix = vsplat(r->inv[0]), iy = vsplat(r->inv[1]), iz = vsplat(r->inv[2]);
+  for (uint32_t j = 0; j < cc; j += 4) {
+    v4f t0 = vsplat(0.f), t1 = vsplat(r->tmax);
+    const v4f lo[3] = {vld(bd + j), vld(bd + j + real), vld(bd + j + real * 2)};
+    const v4f hi[3] = {vld(bd + j + real * 3), vld(bd + j + real * 4),
+                       vld(bd + j + real * 5)};
+    const v4f o[3] = {ox, oy, oz}, inv[3] = {ix, iy, iz};
+    for (int a = 0; a < 3; ++a) {
+      v4f tn = (lo[a] - o[a]) * inv[a];
+      v4f tf = (hi[a] - o[a]) * inv[a];
+      const v4i sw = tn > tf;
+      const v4f n2 = vsel(sw, tf, tn), f2 = vsel(sw, tn, tf);
+      t0 = vsel(n2 < t0, t0, n2);   /* rmax(tn, t0) = (tn < t0) ? t0 : tn */
+      t1 = vsel(t1 < f2, t1, f2);   /* rmin(tf, t1) = (t1 < tf) ? t1 : tf */
+    }
+    const uint32_t bits = vbits(t0 <= t1);
+    for (uint32_t k = 0; k < 4 && j + k < cc; ++k) {
+      if (bits >> k & 1u) {
+        mask |= 1u << (j + k);
+        if (dist) dist[j + k] = t0[k];
+      }
+    }
+  }
+  return mask;
+}
+#endif
+
 /* aabbIntersect over the node's real children; bit j set if child j is hit. */
 static uint32_t aabb_intersect(const oracle_fast_t* f, const oracle_compact_t* b, uint32_t id,
                                const oray_t* r, float* dist) {
@@ -684,6 +834,9 @@ static uint32_t aabb_intersect(const oracle_fast_t* f, const oracle_compact_t* b
   if (f->node_memory != f->gang && isnan(bd[f->node_memory * 6 - 1]))
     real = (int)bd[f->node_memory * 6 - 2];
   uint32_t cc = b->child_count[id];
+#ifdef ORACLE_SIMD
+  if (real % 4 == 0) return aabb_intersect_v(bd, real, cc, r, dist);
+#endif
   uint32_t mask = 0;
   for (uint32_t j = 0; j < cc; ++j) {
     float lo[3] = {bd[j], bd[j + real], bd[j + real * 2]};
@@ -716,10 +869,22 @@ static void fast_leaf(const oracle_fast_t* f, const oracle_compact_t* b, uint32_
   s->c.tri_tests += (uint32_t)real;
   if (hist) hist[MAX_DEPTH + (b->depth[id] < MAX_DEPTH ? b->depth[id] : MAX_DEPTH - 1)]++;
   if (s->any) {
+#ifdef ORACLE_SIMD
+    if (stride % 4 == 0) {
+      if (tri_any_hit_v(f, begin, stride, real, &s->r, &s->c)) s->hit = 1;
+      return;
+    }
+#endif
     if (tri_any_hit(f, begin, stride, real, &s->r, &s->c)) s->hit = 1;
   } else {
     float u, v;
+#ifdef ORACLE_SIMD
+    int idx = (stride % 4 == 0 && f->gang <= 8)
+                  ? tri_intersect_v(f, begin, stride, real, &s->r, &u, &v, &s->c)
+                  : tri_intersect(f, begin, stride, real, &s->r, &u, &v, &s->c);
+#else
     int idx = tri_intersect(f, begin, stride, real, &s->r, &u, &v, &s->c);
+#endif
     if (idx != -1) {
       s->hit = 1;
       s->leaf_begin = (int32_t)begin;

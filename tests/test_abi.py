@@ -225,7 +225,7 @@ def test_noalloc_entry_point_rejects_bad_arguments_without_a_gpu():
                 N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 1, 0, 0, 0),    # save_distance
                 N.TraceOpts(0, 0, 0, 16, 128, 0, 0, 0, 0, 1, 0)):   # stack_local
         assert call([good], opts=bad) == N.ERR_UNSUPPORTED
-    assert call([good], opts=N.TraceOpts(0, 2, 0, 16, 128, 4, 0, 0, 0, 0, 0)) == N.ERR_BAD_ARG
+    assert call([good], opts=N.TraceOpts(0, 2, 0, 16, 128, 5, 0, 0, 0, 0, 0)) == N.ERR_BAD_ARG
 
 
 def test_noalloc_python_binding_rejects_mismatched_buffers():

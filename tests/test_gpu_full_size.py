@@ -56,10 +56,12 @@ def test_bench_frame_with_the_bench_plan_equals_the_oracle(bench_frame):
     d_s, d_a = torch.from_numpy(shadow).cuda(), torch.from_numpy(ao).cuda()
     occ_s = scene.trace(d_s, kind="any", **BENCH_PLAN[1])["occluded"].cpu().numpy()
     occ_a = scene.trace(d_a, kind="any", **BENCH_PLAN[2])["occluded"].cpu().numpy()
-    # the warp-wide leaf phase (policy 3) gives the same occlusion
-    occ_c = scene.trace(d_a, kind="any", scheme="persistent", policy=3, refill=24, reorder=10,
-                        any_order=True)["occluded"].cpu().numpy()
-    assert np.array_equal(occ_c, occ_a)
+    # two leaves per lane set aside (policy 3), tested per lane or warp-wide
+    # (policy 4): the same occlusion
+    for policy in (3, 4):
+        occ_c = scene.trace(d_a, kind="any", scheme="persistent", policy=policy, refill=24,
+                            reorder=10, any_order=True)["occluded"].cpu().numpy()
+        assert np.array_equal(occ_c, occ_a), policy
     scene.status()
     cv = O.CompactView(bvh.export_compact())
     for rays, gpu, shadow_kind in ((primary, hits.cpu().numpy(), False), (shadow, occ_s, True),

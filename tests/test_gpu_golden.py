@@ -26,10 +26,11 @@ SCHEMES = [("per_ray", {}), ("per_ray", {"stack": "local"}), ("per_ray", {"save_
            ("stream", {}), ("persistent", {"policy": 0}), ("persistent", {"policy": 1, "refill": 1}),
            ("persistent", {"policy": 2, "refill": 24}),
            ("persistent", {"policy": 2, "refill": 24, "reorder": 10}),
-           ("persistent", {"policy": 3, "refill": 24}),
-           ("persistent", {"policy": 3, "refill": 24, "reorder": 10, "any_order": True})]
+           ("persistent", {"policy": 3, "refill": 24, "reorder": 10, "any_order": True}),
+           ("persistent", {"policy": 4, "refill": 24}),
+           ("persistent", {"policy": 4, "refill": 24, "reorder": 10, "any_order": True})]
 IDS = ["per_ray", "per_ray_local", "per_ray_dist", "stream", "ww", "ifif", "spec", "spec_reorder",
-       "coop", "coop_reorder_anyorder"]
+       "spec2_reorder_anyorder", "coop", "coop_reorder_anyorder"]
 
 
 @pytest.fixture(scope="module", params=GOLDEN, ids=[p.stem for p in GOLDEN])

@@ -17,9 +17,9 @@ LIGHT = [2.0, 3.0, 2.0]
 # (scheme, extra trace options): every traversal scheme and persistent policy
 SCHEMES = [("per_ray", {}), ("stream", {}), ("persistent", {"policy": 0}),
            ("persistent", {"policy": 1, "refill": 1}), ("persistent", {"policy": 2, "refill": 16}),
-           ("persistent", {"policy": 3, "refill": 24})]
+           ("persistent", {"policy": 3, "refill": 24}), ("persistent", {"policy": 4, "refill": 24})]
 SCHEME_IDS = ["per_ray", "stream", "persistent_ww", "persistent_ifif_r1", "persistent_spec",
-              "persistent_coop"]
+              "persistent_spec2", "persistent_coop"]
 
 
 def dev(a):
@@ -593,7 +593,8 @@ def test_any_order_keeps_any_hit_results(profile, fmt):
                            ("stream", {}), ("persistent", {"policy": 0, "refill": 8}),
                            ("persistent", {"policy": 2, "refill": 24, "reorder": 10}),
                            ("persistent", {"policy": 3, "refill": 24, "reorder": 10}),
-                           ("persistent", {"policy": 3, "refill": 8})):
+                           ("persistent", {"policy": 4, "refill": 24, "reorder": 10}),
+                           ("persistent", {"policy": 4, "refill": 8})):
             if fmt == "q8" and scheme == "stream":
                 continue
             got = scene.trace(d, kind="any", scheme=scheme, profile=profile, any_order=True,

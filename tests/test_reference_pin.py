@@ -7,7 +7,8 @@ need the reference's sources and are skipped where they are absent; the
 committed fixtures of tests/golden/ carry the same checks to every machine
 (tests/test_golden.py, tests/test_gpu_golden.py).
 
-* The builder (csrc/bvh_builder.cpp): node for node the reference's tree
+* The builders (csrc/bvh_builder.cpp, and oracle/sah_builder.c that the CPU
+  baseline uses): node for node the reference's tree
   (bounds, children, primitive ranges, per-axis push sequences, depths,
   primitive order) on scenes whose triangle centres are distinct per axis.
   Where centres tie, the reference's unstable std::sort and this builder's
@@ -65,6 +66,8 @@ def test_builder_equals_the_reference_builder(R, n, l):
     ours = pkg.Bvh(tris, n, l)
     assert ours.info["n_nodes"] == ref.n_nodes
     _same_tree(ref.export_compact(), ours.export_compact())
+    # the oracle's C builder (the CPU baseline's tree) as well
+    _same_tree(ref.export_compact(), O.build_tree(tris, n, l))
 
 
 @pytest.mark.parametrize("split", [0, 1, 2])
