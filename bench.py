@@ -104,7 +104,8 @@ def parse():
     p.add_argument("--ao-sample", type=int, default=2_000_000,
                    help="aolaunch: AO rays traced per launch (strided sample of the frame's)")
     p.add_argument("--tune-nl", action="store_true",
-                   help="batch64: let the autotuner pick N/L per scene")
+                   help="batch64: let the autotuner pick N/L per scene, timing each scene's "
+                        "jobs in the multi-scene launch itself")
     return p.parse_args()
 
 
@@ -699,23 +700,39 @@ def run_batch(a):
         tris, primary, light = make_batch_scene(kind, tt, rr, i)
         d_p = torch.from_numpy(primary).to(dev)
         if a.tune_nl:
-            def batches_fn(scene, d_p=d_p, tris=tris, primary=primary, light=light):
+            def batches_fn(scene, d_p=d_p, tris=tris, primary=primary, light=light, i=i):
                 h = scene.trace(d_p)["hits"]
                 m, p, n = S.surface(tris, primary, pkg.hit_prims(h.cpu().numpy()))
-                ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris))).to(dev)
-                return [(d_p, "closest"), (ao, "any")]
+                sh = torch.from_numpy(S.shadow_rays(p, n, light)).to(dev)
+                ao = torch.from_numpy(S.ao_rays(p, n, 4, 0.1 * S.scene_diagonal(tris),
+                                                seed=i)).to(dev)
+                return [(d_p, "closest"), (sh, "any"), (ao, "any")]
+
+            def time_fn(scene, batches):
+                # the scene's three jobs in the multi-scene launch itself
+                jobs = []
+                for (rays, k), (ro, ao_job) in zip(batches, ((0, 0), (0, 0),
+                                                             (a.job_reorder, a.job_any_order))):
+                    out = (torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+                           if k == "closest" else
+                           torch.empty(rays.shape[0], dtype=torch.uint8, device=dev))
+                    jobs.append((scene, rays, k, out, ro, ao_job))
+                stream = torch.cuda.current_stream(dev)
+                pkg.trace_jobs(jobs, policy=2, refill=a.job_refill)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(3):
+                    pkg.trace_jobs(jobs, policy=2, refill=a.job_refill)
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                return e0.elapsed_time(e1) / 3
+
             best, _ = autotune.tune_branching(
                 tris, batches_fn, pairs=tuple((n, l) for n in (4, 8, 16) for l in (4, 8, 16)),
-                layouts=(("fp32", 0),), options=({"scheme": "per_ray", "block": 32},
-                                                 {"scheme": "per_ray", "block": 64},
-                                                 {"scheme": "per_ray", "block": 128},
-                                                 {"scheme": "per_ray", "block": 128,
-                                                  "stack": "local"}),
-                reps=1)
+                layouts=(("fp32", 0),), time_fn=time_fn, reps=1)
             _, (bn, bl), bvh, plan, tuned = best
             scene = tuned[("fp32", 0)]
-            block = plan.choices[0][1]["block"]
-            stack = plan.choices[0][1].get("stack", "shared")
+            block, stack = 128, "shared"
         else:
             bn, bl, block, stack = a.branching, a.leaf, 128, "shared"
             bvh = pkg.Bvh(tris, bn, bl)
@@ -747,8 +764,8 @@ def run_batch(a):
     # The AO jobs' rays are grouped by direction inside the batched call.
     jobs_batched = [j + x for j, x in zip(jobs_plain, job_reorder)]
 
-    def batched():
-        pkg.trace_jobs(jobs_batched, policy=2, refill=a.job_refill)
+    def batched(one_launch=False):
+        pkg.trace_jobs(jobs_batched, policy=2, refill=a.job_refill, one_launch=one_launch)
 
     def timed(fn, steps):
         for _ in range(a.warmup):
@@ -769,10 +786,19 @@ def run_batch(a):
     torch.cuda.synchronize(dev)
     same = all(torch.equal(o.view(torch.uint8), r.view(torch.uint8))
                for (_, _, _, o), r in zip(jobs_plain, refs))
-    # The batched launch recorded in a CUDA graph.
+    batched(one_launch=True)
+    torch.cuda.synchronize(dev)
+    same_one = all(torch.equal(o.view(torch.uint8), r.view(torch.uint8))
+                   for (_, _, _, o), r in zip(jobs_plain, refs))
+    # The batched launches recorded in CUDA graphs: one launch per ray kind
+    # (and node width and format), and one launch for everything.
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
         batched()
+    g1 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g1):
+        batched(one_launch=True)
+    ms_one = timed(g1.replay, a.steps)
     with ClockSampler(0) as clk:
         ms_graph = timed(g.replay, a.steps)
     clocks = clk.summary()
@@ -798,6 +824,7 @@ def run_batch(a):
                       "bvhgpu_trace_jobs (one persistent launch per ray kind over all scenes; "
                       "speculative any-hit policy) in a CUDA graph",
             "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,
+            "ms_one_launch_graph": ms_one, "one_launch_results_identical": bool(same_one),
             "ms_sequential_plain_launches": ms_seq,
             "speedup_vs_sequential": ms_seq / ms_graph, "results_identical": bool(same),
             "autotuned_nl": bool(a.tune_nl), "scenes": scenes, "setup_s": round(setup_s, 1),

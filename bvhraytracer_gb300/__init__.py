@@ -476,8 +476,10 @@ def ao_factor(occluded, samples: int, stream=None):
 
 
 def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: int = 16,
-               stream=None) -> None:
-    """Traces many (scene, rays) jobs in one persistent launch per ray kind.
+               one_launch: bool = False, stream=None) -> None:
+    """Traces many (scene, rays) jobs in one persistent launch per ray kind
+    (and node width and format), or with ``one_launch`` in a single launch
+    whose warps trace one ray kind at a time.
 
     ``jobs``: list of ``(scene, rays, kind, out)``, ``(scene, rays, kind,
     out, reorder)`` or ``(scene, rays, kind, out, reorder, any_order)`` with
@@ -502,6 +504,7 @@ def trace_jobs(jobs, *, profile: str = "instrumented", policy: int = 2, refill: 
                        any_order, 0)
         dev = rays.device
     o = N.TraceOpts(N.CLOSEST, N.PERSISTENT, _PROFILE[profile], 16, 128, policy, refill)
+    o.one_launch = int(bool(one_launch))
     s = stream if stream is not None else torch.cuda.current_stream(dev)
     N.check(N.lib().bvhgpu_trace_jobs(arr, len(jobs), C.byref(o), C.c_void_p(s.cuda_stream)))
 

@@ -54,7 +54,7 @@ class TraceOpts(C.Structure):
                 ("workgroup", C.c_int32), ("block", C.c_int32), ("policy", C.c_int32),
                 ("refill", C.c_int32), ("save_distance", C.c_int32),
                 ("reorder", C.c_int32), ("stack_local", C.c_int32), ("any_order", C.c_int32),
-                ("fullness", C.c_int32)]
+                ("fullness", C.c_int32), ("one_launch", C.c_int32)]
 
 
 class Batch(C.Structure):

@@ -37,6 +37,9 @@ DEFAULT_OPTIONS = (
     # any-hit batches only: child-index push order
     {"scheme": "persistent", "policy": 2, "refill": 24, "reorder": 10, "any_order": True},
     {"scheme": "persistent", "policy": 2, "refill": 16, "any_order": True},
+    # any-hit batches only: two leaves set aside per lane, tested per lane / warp-wide
+    {"scheme": "persistent", "policy": 3, "refill": 16, "reorder": 10, "any_order": True},
+    {"scheme": "persistent", "policy": 4, "refill": 24, "reorder": 10, "any_order": True},
 )
 DEFAULT_LAYOUTS = (("fp32", 0), ("fp32", 2), ("q8", 2))
 
@@ -79,7 +82,7 @@ def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFA
         for (lay, sc), opts in itertools.product(scenes.items(), options):
             if lay[0] != "fp32" and opts["scheme"] == "stream":
                 continue
-            if opts.get("any_order") and kind != "any":
+            if (opts.get("any_order") or opts.get("policy", 0) >= 3) and kind != "any":
                 continue
             ms = _time(sc, rays, kind, opts, profile, reps)
             plan.table[(bi, lay, tuple(sorted(opts.items())))] = ms
@@ -91,18 +94,27 @@ def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFA
 
 def tune_branching(tris, batches_fn, *, pairs=((4, 4), (4, 8), (8, 4), (8, 8), (16, 4), (16, 8),
                                               (16, 16)),
-                   profile: str = "instrumented", reps: int = 2, device: int = 0, **kw):
+                   profile: str = "instrumented", reps: int = 2, device: int = 0,
+                   time_fn=None, **kw):
     """Also picks N and L: builds a BVH per pair, tunes each, returns the pair
     with the lowest total time. ``batches_fn(scene)`` returns the batches to
-    time for a scene (secondary rays may depend on the primary hits)."""
+    time for a scene (secondary rays may depend on the primary hits).
+    ``time_fn(scene, batches)``, when given, times the call the batches will
+    actually run in (for instance the multi-scene launch of bvhgpu_trace_jobs)
+    and returns its milliseconds; the plan then records that call."""
     best = None
     results = {}
     for n, l in pairs:
         bvh = Bvh(tris, n, l)
         scene = Scene(bvh, device=device)
         batches = batches_fn(scene)
-        plan, scenes = tune_scene(bvh, batches, profile=profile, reps=reps, device=device,
-                                  scenes={("fp32", 0): scene}, **kw)
+        if time_fn is not None:
+            ms = float(time_fn(scene, batches))
+            plan = Plan(choices=[(("fp32", 0), {"scheme": "time_fn"}, ms)])
+            scenes = {("fp32", 0): scene}
+        else:
+            plan, scenes = tune_scene(bvh, batches, profile=profile, reps=reps, device=device,
+                                      scenes={("fp32", 0): scene}, **kw)
         total = sum(ms for _, _, ms in plan.choices)
         results[(n, l)] = total
         if best is None or total < best[0]:

@@ -986,7 +986,30 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
   }
   std::sort(groups.begin(), groups.end());
-  if (!BVHGPU_JOBS_SPLIT) {
+  if (opts->one_launch) {
+    // One launch: closest-hit jobs first in queue order, then any-hit jobs.
+    std::unique_ptr<dev::JobTable> one(new (std::nothrow) dev::JobTable());
+    if (!one) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+      *one = *t;
+      int m = 0;
+      uint64_t begin = 0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int i = 0; i < nj; ++i) {
+          if ((t->jobs[i].kind == BVHGPU_ANY) != (pass == 1)) continue;
+          one->jobs[m] = t->jobs[i];
+          one->jobs[m].ray_begin = begin;
+          begin += t->jobs[i].n;
+          ++m;
+        }
+        // (pass 0 ends at the split between the kinds)
+      one->split = 0;
+      for (int i = 0; i < nj; ++i)
+        if (t->jobs[i].kind != BVHGPU_ANY) one->split += t->jobs[i].n;
+      one->head_any = first->d_queue + (first->queue_next.fetch_add(1) % bvhgpu_scene::kQueueSlots);
+      e = dev::launch_batched(*one, cfg.profile, 3, sms, st);
+    }
+  } else if (!BVHGPU_JOBS_SPLIT) {
     int kinds = 0;
     for (int i = 0; i < nj; ++i) kinds |= t->jobs[i].kind == BVHGPU_ANY ? 2 : 1;
     e = dev::launch_batched(*t, cfg.profile, kinds == 3 ? 0 : kinds, sms, st);

@@ -14,10 +14,14 @@ cudaError_t launch_batched(const JobTable& t, int profile, int kmode, int sm_cou
   const size_t smem = (size_t)t.stack_cap * bs * 4;
   constexpr int F = BVHGPU_PROFILE_FAST, I = BVHGPU_PROFILE_INSTRUMENTED;
   void (*k)(const JobTable) =
-      profile == F ? (kmode == 1 ? trace_batched_kernel<F, 1>
-                                 : kmode == 2 ? trace_batched_kernel<F, 2> : trace_batched_kernel<F, 0>)
-                   : (kmode == 1 ? trace_batched_kernel<I, 1>
-                                 : kmode == 2 ? trace_batched_kernel<I, 2> : trace_batched_kernel<I, 0>);
+      profile == F ? (kmode == 1   ? trace_batched_kernel<F, 1>
+                      : kmode == 2 ? trace_batched_kernel<F, 2>
+                      : kmode == 3 ? trace_batched_kernel<F, 3>
+                                   : trace_batched_kernel<F, 0>)
+                   : (kmode == 1   ? trace_batched_kernel<I, 1>
+                      : kmode == 2 ? trace_batched_kernel<I, 2>
+                      : kmode == 3 ? trace_batched_kernel<I, 3>
+                                   : trace_batched_kernel<I, 0>);
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024)
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -32,6 +36,10 @@ cudaError_t launch_batched(const JobTable& t, int profile, int kmode, int sm_cou
   if (grid == 0) return cudaSuccess;
   e = cudaMemsetAsync(t.head, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  if (kmode == 3) {
+    e = cudaMemsetAsync(t.head_any, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+  }
   k<<<(unsigned)grid, bs, smem, s>>>(t);
   return cudaGetLastError();
 }

@@ -44,6 +44,11 @@ struct JobTable {
   int refill_min;
   int stack_cap;
   int policy;  // 0 while-while, 2 speculative any-hit
+  // KMODE 3: rays [0, split) belong to closest-hit jobs, [split, total) to
+  // any-hit jobs (the jobs are ordered so); the any-hit rays have their own
+  // queue head.
+  uint64_t split;
+  unsigned long long* head_any;
 };
 
 // Node visit dispatched on the lane's node width and format.
@@ -76,7 +81,9 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
 #define BVHGPU_BATCHED_MIN_BLOCKS 5
 #endif
 // KMODE 0: every lane takes its job's ray kind; 1: closest-hit jobs only;
-// 2: any-hit jobs only (the other kind's code is compiled out).
+// 2: any-hit jobs only (the other kind's code is compiled out); 3: both
+// kinds in one launch with kind-uniform warps: a warp takes closest-hit rays
+// until their queue is empty and its lanes are done, then any-hit rays.
 template <int PROFILE, int KMODE>
 __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
     trace_batched_kernel(const __grid_constant__ JobTable t) {
@@ -101,20 +108,30 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
   sc.top_nodes = 0;
   int nm = 8, fmt = 0;
   int kind = KMODE == 2 ? BVHGPU_ANY : BVHGPU_CLOSEST;
+  // KMODE 3: the warp's ray kind (the same in every lane).
+  int wkind = KMODE == 3 && t.split == 0 ? BVHGPU_ANY : BVHGPU_CLOSEST;
   bool drained = false;
   uint32_t postponed = NONE;
 
   while (true) {
     const unsigned idle = __ballot_sync(FULL, !active);
+    if (KMODE == 3 && wkind == BVHGPU_CLOSEST && drained && idle == FULL) {
+      wkind = BVHGPU_ANY;  // closest-hit rays all taken and traced: any-hit rays next
+      drained = false;
+    }
+    const bool seg_any = KMODE == 3 && wkind == BVHGPU_ANY;
+    const uint64_t seg_begin = seg_any ? t.split : 0;
+    const uint64_t seg_end = KMODE == 3 && !seg_any ? t.split : t.total;
     if (!drained && idle != 0 && ((int)__popc(idle) >= t.refill_min || idle == FULL)) {
       const int leader = __ffs(idle) - 1;
       unsigned long long base = 0;
-      if ((int)lane == leader) base = atomicAdd(t.head, (unsigned long long)__popc(idle));
+      if ((int)lane == leader)
+        base = atomicAdd(seg_any ? t.head_any : t.head, (unsigned long long)__popc(idle));
       base = __shfl_sync(FULL, base, leader);
-      if (base + __popc(idle) >= t.total) drained = true;
+      if (seg_begin + base + __popc(idle) >= seg_end) drained = true;
       if (!active) {
-        const uint64_t g = base + __popc(idle & below);
-        if (g < t.total) {
+        const uint64_t g = seg_begin + base + __popc(idle & below);
+        if (g < seg_end) {
           // Job of global ray g: last job whose ray_begin <= g.
           int lo = 0, hi = t.n_jobs - 1;
           while (lo < hi) {
@@ -138,6 +155,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
           nm = J.nm;
           fmt = J.fmt;
           if (KMODE == 0) kind = J.kind;
+          if (KMODE == 3) kind = wkind;
           const bvhgpu_ray_t in = load_ray(J.rays, local);
           best = Best();
           hit = false;
@@ -157,7 +175,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
       }
     }
     if (__ballot_sync(FULL, active) == 0) {
-      if (drained) break;
+      if (drained && !(KMODE == 3 && wkind == BVHGPU_CLOSEST)) break;
       continue;
     }
 

@@ -238,6 +238,12 @@ typedef struct {
                         summed over the rays: visits of nodes with c children
                         (entry 128 + c) and of leaves with c triangles (entry 145 + c),
                         c = 0..16. Instrumented and fast profile, every scheme. */
+  int32_t one_launch; /* bvhgpu_trace_jobs: 0 one persistent launch per group of jobs with
+                        one ray kind, node width and node format; nonzero: one launch for
+                        all jobs, the closest-hit jobs' rays queued before the any-hit
+                        jobs', each warp tracing one kind at a time (it takes any-hit
+                        rays once the closest-hit queue is empty and its lanes are done).
+                        Same results. */
 } bvhgpu_trace_opts_t;
 
 /* Counters per ray when `counters` is non-null (8 uint32 per ray):

@@ -47,7 +47,7 @@ def test_status_codes_match_header():
 def test_struct_sizes_match_header_layout():
     assert C.sizeof(N.BuildParams) == 24
     assert C.sizeof(N.SceneParams) == 20
-    assert C.sizeof(N.TraceOpts) == 48
+    assert C.sizeof(N.TraceOpts) == 52
     assert C.sizeof(N.Job) == 56
 
 

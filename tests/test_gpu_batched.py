@@ -50,13 +50,14 @@ def _jobs(items, profile):
 
 @pytest.mark.parametrize("profile", ["instrumented", "fast"])
 @pytest.mark.parametrize("policy", [0, 2])
-def test_jobs_match_per_scene_kernels(profile, policy):
+@pytest.mark.parametrize("one_launch", [False, True], ids=["per_group", "one_launch"])
+def test_jobs_match_per_scene_kernels(profile, policy, one_launch):
     items = _scenes()
     jobs, refs = _jobs(items, profile)
     for _ in range(2):
         for j in jobs:
             j[3].fill_(7)
-        pkg.trace_jobs(jobs, profile=profile, policy=policy)
+        pkg.trace_jobs(jobs, profile=profile, policy=policy, one_launch=one_launch)
         torch.cuda.synchronize()
         for (scene, rays, kind, out), ref in zip(jobs, refs):
             if kind == "closest":
@@ -76,18 +77,19 @@ def test_jobs_against_oracle():
     assert np.array_equal(jobs[0][3].cpu().numpy().view(np.uint32), ref["hits"].view(np.uint32))
 
 
-def test_jobs_in_a_cuda_graph():
+@pytest.mark.parametrize("one_launch", [False, True], ids=["per_group", "one_launch"])
+def test_jobs_in_a_cuda_graph(one_launch):
     items = _scenes()
     jobs, refs = _jobs(items, "instrumented")
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
-        pkg.trace_jobs(jobs, stream=s)  # first call outside the capture
+        pkg.trace_jobs(jobs, stream=s, one_launch=one_launch)  # first call outside the capture
     torch.cuda.current_stream().wait_stream(s)
     torch.cuda.synchronize()
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
-        pkg.trace_jobs(jobs)
+        pkg.trace_jobs(jobs, one_launch=one_launch)
     for _ in range(3):
         for j in jobs:
             j[3].fill_(5)
@@ -125,11 +127,12 @@ def test_reordered_jobs(graph):
                 assert torch.equal(out, ref)
 
     if not graph:
-        for j in jobs:
-            j[3].fill_(7)
-        pkg.trace_jobs(jobs, policy=2, refill=24)
-        torch.cuda.synchronize()
-        check()
+        for one_launch in (False, True):
+            for j in jobs:
+                j[3].fill_(7)
+            pkg.trace_jobs(jobs, policy=2, refill=24, one_launch=one_launch)
+            torch.cuda.synchronize()
+            check()
         with pytest.raises(pkg.BvhgpuError):
             pkg.trace_jobs([jobs[1], jobs[3][:4] + (10,)])  # reordered jobs must share K
         return
@@ -177,9 +180,10 @@ def test_jobs_of_one_kind(kind):
     jobs, refs = _jobs(items, "instrumented")
     sel = [(j, r) for j, r in zip(jobs, refs) if j[2] == kind]
     for subset in (sel, [x for x in sel if x[0][0].node_format == "fp32"][:2]):
-        for j, _ in subset:
-            j[3].fill_(9)
-        pkg.trace_jobs([j for j, _ in subset], policy=2, refill=16)
-        torch.cuda.synchronize()
-        for (scene, rays, k, out), ref in subset:
-            assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
+        for one_launch in (False, True):
+            for j, _ in subset:
+                j[3].fill_(9)
+            pkg.trace_jobs([j for j, _ in subset], policy=2, refill=16, one_launch=one_launch)
+            torch.cuda.synchronize()
+            for (scene, rays, k, out), ref in subset:
+                assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
