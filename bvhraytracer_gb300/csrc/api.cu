@@ -54,6 +54,7 @@ struct bvhgpu_scene {
   uint32_t stall_bytes = 0;  // failure-detection tests: staging wait never completes
   std::vector<uint32_t> prim_slot;  // input triangle id -> leaf * leaf_memory + lane
   uint8_t* d_nodes = nullptr;
+  uint8_t* d_q8_perm = nullptr;  // Q8 scenes: push sequences, q8_perm_bytes per inner node
   float* d_leaves = nullptr;
   uint32_t* d_leaf_prim = nullptr;
   uint8_t* d_leaf_depth = nullptr;
@@ -86,10 +87,12 @@ struct bvhgpu_scene {
     s.gang = layout.gang;
     s.status = d_status;
     s.boxes_ordered = layout.boxes_ordered ? 1 : 0;
+    s.q8_perm = d_q8_perm;
     return s;
   }
   void release() {
     cudaFree(d_nodes);
+    cudaFree(d_q8_perm);
     cudaFree(d_leaves);
     cudaFree(d_leaf_prim);
     cudaFree(d_leaf_depth);
@@ -102,6 +105,7 @@ struct bvhgpu_scene {
     for (auto& ev : host_event)
       if (ev) cudaEventDestroy(ev);
     d_nodes = nullptr;
+    d_q8_perm = nullptr;
     d_leaves = nullptr;
     d_leaf_prim = nullptr;
     d_leaf_depth = nullptr;
@@ -484,10 +488,13 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   if (e == cudaSuccess && q8) {
     uint8_t* q8_nodes = nullptr;
     const size_t bytes = std::max<size_t>((size_t)s->layout.n_inner * s->layout.record_bytes, 16);
+    const size_t pbytes =
+        std::max<size_t>((size_t)s->layout.n_inner * q8_perm_bytes(s->layout.node_stride), 16);
     e = cudaMalloc((void**)&q8_nodes, bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_q8_perm, pbytes);
     if (e == cudaSuccess)
-      e = dev::launch_q8_encode(s->layout.node_stride, s->d_nodes, q8_nodes, s->layout.n_inner,
-                                s->d_status, nullptr);
+      e = dev::launch_q8_encode(s->layout.node_stride, s->d_nodes, q8_nodes, s->d_q8_perm,
+                                s->layout.n_inner, s->d_status, nullptr);
     int st = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(s->d_nodes);
@@ -527,11 +534,16 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
 int bvhgpu_scene_node_records(bvhgpu_scene_t s, void* out, uint64_t capacity, uint64_t* bytes) {
   if (!s || !bytes) return set_error(BVHGPU_ERR_BAD_ARG, "null argument");
   const uint64_t n = (uint64_t)s->layout.n_inner * (uint64_t)s->layout.record_bytes;
-  *bytes = n;
+  const uint64_t np = s->d_q8_perm
+                          ? (uint64_t)s->layout.n_inner * q8_perm_bytes(s->layout.node_stride)
+                          : 0;
+  *bytes = n + np;
   if (!out) return BVHGPU_OK;
-  if (capacity < n) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
+  if (capacity < n + np) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
   cudaError_t e = cudaSetDevice(s->device);
   if (e == cudaSuccess) e = cudaMemcpy(out, s->d_nodes, n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && np)
+    e = cudaMemcpy(static_cast<uint8_t*>(out) + n, s->d_q8_perm, np, cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? BVHGPU_OK : cuda_error(e, "node records");
 }
 
@@ -541,10 +553,13 @@ int bvhgpu_bvh_node_records(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* p, void
   DeviceLayout lay;
   int rc = build_device_layout(h->bvh, p->gang, p->leaf_memory, p->node_format, p->top_levels, lay);
   if (rc) return set_error(rc, "device layout failed");
-  *bytes = lay.nodes.size();
+  *bytes = lay.nodes.size() + lay.q8_perm.size();
   if (!out) return BVHGPU_OK;
-  if (capacity < lay.nodes.size()) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
+  if (capacity < *bytes) return set_error(BVHGPU_ERR_BAD_ARG, "node records: buffer too small");
   std::memcpy(out, lay.nodes.data(), lay.nodes.size());
+  if (!lay.q8_perm.empty())
+    std::memcpy(static_cast<uint8_t*>(out) + lay.nodes.size(), lay.q8_perm.data(),
+                lay.q8_perm.size());
   return BVHGPU_OK;
 }
 
@@ -927,6 +942,7 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.boxes_ordered = j.scene->layout.boxes_ordered ? 1 : 0;
     d.any_index_order = j.any_order ? 1 : 0;
     d.perm = nullptr;
+    d.q8_perm = j.scene->d_q8_perm;
     if (j.reorder && j.n > 1) {
       seg_k = j.reorder;
       seg_off.push_back(seg_bytes);

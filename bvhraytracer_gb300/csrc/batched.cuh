@@ -10,7 +10,7 @@
 namespace bvhgpu {
 namespace dev {
 
-constexpr int kMaxJobs = 192;  // 192 jobs x 88 bytes in the parameter block
+constexpr int kMaxJobs = 192;  // 192 jobs x 96 bytes in the parameter block
 
 struct JobDev {
   const uint8_t* nodes;
@@ -33,8 +33,9 @@ struct JobDev {
   // Reordered job: the job's i-th ray in queue order is ray perm[i], and its
   // result goes to slot perm[i] (null: i).
   const uint32_t* perm;
+  const uint8_t* q8_perm;  // SceneDev::q8_perm of the job's scene
 };
-static_assert(sizeof(JobDev) == 88, "job record size");
+static_assert(sizeof(JobDev) == 96, "job record size");
 
 struct JobTable {
   JobDev jobs[kMaxJobs];
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
           sc.status = J.status;
           sc.boxes_ordered = J.boxes_ordered;
           sc.any_index_order = J.any_index_order;
+          sc.q8_perm = J.q8_perm;
           nm = J.nm;
           fmt = J.fmt;
           if (KMODE == 0) kind = J.kind;

@@ -176,6 +176,8 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
 
   // Inner records.
   out.nodes.assign((size_t)out.n_inner * out.record_bytes, 0);
+  const int pbytes = q8_perm_bytes(nm);
+  if (node_format != 0) out.q8_perm.assign((size_t)out.n_inner * pbytes, 0);
   for (uint32_t g = 0; g < out.n_inner; ++g) {
     const uint32_t id = inner_order[g];
     const CompactNode& c = bvh.nodes[id];
@@ -274,7 +276,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
     // (the position of each child in it). The other direction pushes the
     // same children in the opposite order.
     const int wb = perm_word_bytes(nm);
-    uint8_t* perm = meta + 12;
+    uint8_t* perm = node_format == 0 ? meta + 12 : &out.q8_perm[(size_t)g * pbytes];
     for (int a = 0; a < 3; ++a) {
       const size_t c_n = bn->order[a].size();
       uint64_t up = 0, inv = 0;
@@ -285,10 +287,19 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
       std::memcpy(perm + (a * 2 + 0) * wb, &up, wb);
       std::memcpy(perm + (a * 2 + 1) * wb, &inv, wb);
     }
-    uint8_t* lcnt = meta + 12 + 6 * wb;
-    for (uint32_t j = 0; j < c.child_count; ++j) {
-      const CompactNode& ch = bvh.nodes[c.child_begin + j];
-      lcnt[j] = ch.child_count == 0 ? (uint8_t)ch.prim_count : 0;
+    if (node_format == 0) {
+      uint8_t* lcnt = meta + 12 + 6 * wb;
+      for (uint32_t j = 0; j < c.child_count; ++j) {
+        const CompactNode& ch = bvh.nodes[c.child_begin + j];
+        lcnt[j] = ch.child_count == 0 ? (uint8_t)ch.prim_count : 0;
+      }
+    } else {
+      uint8_t* nib = meta + 12;  // (count - 1) per leaf child, 4 bits
+      for (uint32_t j = 0; j < c.child_count; ++j) {
+        const CompactNode& ch = bvh.nodes[c.child_begin + j];
+        if (ch.child_count == 0)
+          nib[j / 2] |= (uint8_t)(((ch.prim_count - 1) & 15u) << (4 * (j & 1)));
+      }
     }
   }
 

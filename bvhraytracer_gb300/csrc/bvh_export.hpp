@@ -41,21 +41,29 @@ int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, Fast
 // = count rounded up to the gang, sentinel (stride, NaN) in the last two
 // floats when the stride is below leaf_memory).
 //
-// Q8 record (branching N, Nm as above), 16-byte aligned:
+// Q8 record (branching N, Nm as above), 16-byte aligned: N4 64 B, N8 80 B,
+// N12 112 B, N16 144 B (FP32: 128 / 240 / 352 / 464 B):
 //   float    origin[3]      parent box lower corner (the quantisation frame)
 //   int8     exp[3], pad    per-axis power-of-two step: step = 2^exp
 //   uint32   inner_base, leaf_base; uint16 leaf_mask; uint8 count; uint8 depth
-//   perm[3][2]; uint8 leaf_cnt[Nm]  (as above)
+//   nibble   leaf_cnt1[Nm]  triangles - 1 of leaf child j, 4 bits each (child j
+//                           in bits 4j..4j+3 of the little-endian words; 0 for
+//                           inner children), Nm / 2 bytes at 28
 //   uint8    q[6][Nm]       child boxes at q8_box_offset: lo = origin + q_lo*step
 //                           (rounded down), hi = origin + q_hi*step (rounded up)
+// The push sequences perm[3][2] of a Q8 node live in a side array, not in its
+// record: q8_perm_bytes(Nm) bytes per inner node in record order, read only by
+// traversals that push hit children in the reference's order.
 inline int perm_word_bytes(int nm) { return nm <= 4 ? 2 : (nm <= 8 ? 4 : 8); }
 inline int fp32_meta_offset(int nm) { return 24 * nm; }
-inline int q8_box_offset(int nm) { return (28 + 6 * perm_word_bytes(nm) + nm + 3) / 4 * 4; }
+inline int q8_box_offset(int nm) { return (28 + nm / 2 + 3) / 4 * 4; }
+inline int q8_perm_bytes(int nm) { return 6 * perm_word_bytes(nm); }
 struct DeviceLayout {
   int branching = 4, node_stride = 4, leaf_memory = 4, gang = 4;
   int node_format = 0;
   int record_bytes = 0;
   std::vector<uint8_t> nodes;         // n_inner * record_bytes
+  std::vector<uint8_t> q8_perm;       // Q8: n_inner * q8_perm_bytes push sequences
   std::vector<float> leaves;          // n_leaves * 9 * leaf_memory
   std::vector<uint32_t> leaf_prim;    // n_leaves * leaf_memory (input ids)
   std::vector<uint8_t> leaf_depth;    // n_leaves

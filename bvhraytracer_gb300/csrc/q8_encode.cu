@@ -6,7 +6,8 @@
 // largest q_lo with origin + q_lo * step <= lo rounded down and the smallest
 // q_hi with origin + q_hi * step >= hi rounded up. q * step is exact, and the
 // directed roundings are __fadd_rd / __fadd_ru, so the records equal the
-// host's byte for byte.
+// host's byte for byte. The meta block is copied, the leaf counts are packed
+// as (count - 1) nibbles, and the push sequences go to the Q8 side array.
 #include <cuda_runtime.h>
 
 #include "q8_encode.cuh"
@@ -23,7 +24,7 @@ __device__ __forceinline__ float step_of(int e) {
 
 template <int NM>
 __global__ void q8_encode_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
-                                 uint32_t n_nodes, int* status) {
+                                 uint8_t* __restrict__ perm_out, uint32_t n_nodes, int* status) {
   using F32 = NodeFmt<NM, kFmtFP32>;
   using Q8 = NodeFmt<NM, kFmtQ8>;
   const uint32_t node = blockIdx.x * blockDim.x + threadIdx.x;
@@ -33,8 +34,15 @@ __global__ void q8_encode_kernel(const uint8_t* __restrict__ in, uint8_t* __rest
   for (int b = 0; b < Q8::REC; b += 4) *reinterpret_cast<uint32_t*>(dst + b) = 0u;
   const float* box = reinterpret_cast<const float*>(src);
   const int count = (int)src[F32::META + 10];
-  // Meta (12 B), push sequences (6 words) and leaf counts (NM B) copied.
-  for (int b = 0; b < 12 + 6 * F32::PW + NM; ++b) dst[Q8::META + b] = src[F32::META + b];
+  // Meta (12 B) copied; leaf counts (NM bytes) packed as (count - 1)
+  // nibbles; push sequences (6 words) to the side array.
+  for (int b = 0; b < 12; ++b) dst[Q8::META + b] = src[F32::META + b];
+  for (int j = 0; j < NM; ++j) {
+    const int c = src[F32::LCNT + j];
+    if (c > 0) dst[Q8::LCNT + j / 2] |= (uint8_t)(((c - 1) & 15) << (4 * (j & 1)));
+  }
+  uint8_t* perm = perm_out + (size_t)node * Q8::PSB;
+  for (int b = 0; b < Q8::PSB; ++b) perm[b] = src[F32::PERM + b];
   float origin[3];
   int ex[3];
   for (int k = 0; k < 3; ++k) {
@@ -86,14 +94,14 @@ __global__ void q8_encode_kernel(const uint8_t* __restrict__ in, uint8_t* __rest
 }  // namespace
 
 cudaError_t launch_q8_encode(int nm, const uint8_t* fp32_nodes, uint8_t* q8_nodes,
-                             uint32_t n_nodes, int* status, cudaStream_t s) {
+                             uint8_t* q8_perm, uint32_t n_nodes, int* status, cudaStream_t s) {
   if (n_nodes == 0) return cudaSuccess;
   const unsigned grid = (n_nodes + 127) / 128;
   switch (nm) {
-    case 4: q8_encode_kernel<4><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, n_nodes, status); break;
-    case 8: q8_encode_kernel<8><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, n_nodes, status); break;
-    case 12: q8_encode_kernel<12><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, n_nodes, status); break;
-    case 16: q8_encode_kernel<16><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, n_nodes, status); break;
+    case 4: q8_encode_kernel<4><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, q8_perm, n_nodes, status); break;
+    case 8: q8_encode_kernel<8><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, q8_perm, n_nodes, status); break;
+    case 12: q8_encode_kernel<12><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, q8_perm, n_nodes, status); break;
+    case 16: q8_encode_kernel<16><<<grid, 128, 0, s>>>(fp32_nodes, q8_nodes, q8_perm, n_nodes, status); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

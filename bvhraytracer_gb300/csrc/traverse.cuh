@@ -36,6 +36,8 @@ struct SceneDev {
   // Any-hit rays without counters push hit children in child-index order
   // (bvhgpu_trace_opts_t.any_order), else in the profile's order.
   int any_index_order = 0;
+  // Q8 records: the push sequences, NodeFmt<N, Q8>::PSB bytes per inner node.
+  const uint8_t* q8_perm = nullptr;
 };
 
 #ifndef BVHGPU_NEARFAR
@@ -94,11 +96,13 @@ struct NodeFmt {
   // Push-sequence word: one nibble per child.
   static constexpr int PW = NM <= 4 ? 2 : (NM <= 8 ? 4 : 8);
   // FP32: float box[6][NM] | meta (12 B) | perm[3][2] | leaf_cnt[NM]
-  // Q8:   origin (3 f32) + exp (3 i8) | meta | perm | leaf_cnt | q[6][NM]
+  // Q8:   origin (3 f32) + exp (3 i8) | meta | (leaf_cnt - 1) nibbles | q[6][NM];
+  //       perm[3][2] in the side array (PSB bytes per node)
   static constexpr int META = FMT == kFmtFP32 ? 24 * NM : 16;
-  static constexpr int PERM = META + 12;
-  static constexpr int LCNT = PERM + 6 * PW;
-  static constexpr int QBOX = (28 + 6 * PW + NM + 3) / 4 * 4;
+  static constexpr int PERM = META + 12;  // FP32 only
+  static constexpr int LCNT = FMT == kFmtFP32 ? PERM + 6 * PW : META + 12;
+  static constexpr int PSB = 6 * PW;
+  static constexpr int QBOX = (28 + NM / 2 + 3) / 4 * 4;
   static constexpr int REC = FMT == kFmtFP32 ? ((24 * NM + 12 + 6 * PW + NM) + 15) / 16 * 16
                                              : ((QBOX + 6 * NM) + 15) / 16 * 16;
 };
@@ -176,7 +180,8 @@ template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, b
           bool NF = false>
 BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
                            int stride, int& sp, int cap, Counters& ctr, int& depth_out,
-                           float* dstack = nullptr, bool index_order = false) {
+                           float* dstack = nullptr, bool index_order = false,
+                           const uint8_t* q8_side = nullptr) {
   using F = NodeFmt<N, FMT>;
   constexpr int NM = F::NM;
   const uint4 meta = rec_u4<SH>(rec + F::META);
@@ -265,13 +270,22 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   }
   if (hit == 0) return true;
 
-  uint64_t clo, chi;
-  load_bytes<NM, SH>(rec + F::LCNT, clo, chi);
+  // Leaf child counts: bytes (FP32 records) or (count - 1) nibbles (Q8).
+  uint64_t clo = 0, chi = 0;
+  uint32_t n0 = 0, n1 = 0;
+  if (FMT == kFmtFP32) {
+    load_bytes<NM, SH>(rec + F::LCNT, clo, chi);
+  } else {
+    n0 = rec_u32<SH>(rec + F::LCNT);
+    if (NM > 8) n1 = rec_u32<SH>(rec + F::LCNT + 4);
+  }
   auto entry = [&](int c) -> uint32_t {
     const uint32_t below = (1u << c) - 1u;
     if ((leaf_mask >> c) & 1u) {
-      uint32_t cnt = (uint32_t)byte_at(clo, chi, c);
-      return kLeafBit | ((cnt - 1u) << kLeafCountShift) |
+      uint32_t cnt1;
+      if (FMT == kFmtFP32) cnt1 = (uint32_t)byte_at(clo, chi, c) - 1u;
+      else cnt1 = ((c < 8 ? n0 >> (4 * c) : n1 >> (4 * (c - 8)))) & 15u;
+      return kLeafBit | (cnt1 << kLeafCountShift) |
              (leaf_base + (uint32_t)__popc(leaf_mask & below));
     }
     return inner_base + (uint32_t)__popc(~leaf_mask & below);
@@ -292,18 +306,21 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
     perm = 0xFEDCBA9876543210ull;
     pm = hit;
   } else {
-    const uint8_t* pp = rec + F::PERM + r.code * 2 * F::PW;
+    // FP32: in the record (shared-memory copy or global); Q8: the side array
+    // (global).
+    constexpr bool PSH = SH && FMT == kFmtFP32;
+    const uint8_t* pp = (FMT == kFmtFP32 ? rec + F::PERM : q8_side) + r.code * 2 * F::PW;
     uint64_t inv;
     if (F::PW == 2) {
-      const uint32_t w = rec_u32<SH>(pp);  // sequence | inverse << 16, 4-byte aligned
+      const uint32_t w = rec_u32<PSH>(pp);  // sequence | inverse << 16, 4-byte aligned
       perm = w & 0xFFFFu;
       inv = w >> 16;
     } else if (F::PW == 4) {
-      perm = rec_u32<SH>(pp);
-      inv = rec_u32<SH>(pp + 4);
+      perm = rec_u32<PSH>(pp);
+      inv = rec_u32<PSH>(pp + 4);
     } else {
-      perm = (uint64_t)rec_u32<SH>(pp) | ((uint64_t)rec_u32<SH>(pp + 4) << 32);
-      inv = (uint64_t)rec_u32<SH>(pp + 8) | ((uint64_t)rec_u32<SH>(pp + 12) << 32);
+      perm = (uint64_t)rec_u32<PSH>(pp) | ((uint64_t)rec_u32<PSH>(pp + 4) << 32);
+      inv = (uint64_t)rec_u32<PSH>(pp + 8) | ((uint64_t)rec_u32<PSH>(pp + 12) << 32);
     }
     pm = 0;
     uint32_t h = hit;
@@ -457,24 +474,26 @@ BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_sme
                           const Ray& r, float tmax, uint32_t* stack, int stride, int& sp, int cap,
                           Counters& ctr, int& depth, float* dstack = nullptr) {
   constexpr int REC = NodeFmt<N, FMT>::REC;
+  const uint8_t* side =
+      FMT == kFmtFP32 ? nullptr : sc.q8_perm + (size_t)e * NodeFmt<N, FMT>::PSB;
   if (e < top) {
     const uint8_t* rec = top_smem + (size_t)e * REC;
     if (r.exact)
       return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true, DIST>(
-          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
+          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
   }
   const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
     return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
   constexpr bool kNF = BVHGPU_NEARFAR && FMT == kFmtFP32 && !DIST;
   if (kNF && sc.boxes_ordered)
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST, kNF>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
   return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST>(
-      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0);
+      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
 }
 
 template <int PROFILE, int KIND, bool COUNT>

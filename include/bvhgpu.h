@@ -534,8 +534,9 @@ int bvhgpu_ao_factor(const uint8_t* occluded, uint64_t n, int32_t samples, float
 
 /* ---- node records (no reference counterpart) --------------------------- */
 /* Copies the scene's device node records (n_inner * record bytes; Q8 scenes
- * encode them on the device) to `out`; *bytes gets the size (out may be null
- * to query it). */
+ * encode them on the device, and their push-sequence side array, n_inner *
+ * 6 * (2, 4 or 8 for 4, 8 or 12-16 child slots) bytes, follows the records)
+ * to `out`; *bytes gets the size (out may be null to query it). */
 int bvhgpu_scene_node_records(bvhgpu_scene_t scene, void* out, uint64_t capacity,
                               uint64_t* bytes);
 /* The same records as encoded on the host by the layout builder, for the
