@@ -1354,7 +1354,8 @@ def run_aolaunch(a):
     dev = torch.device("cuda", 0)
     tris, bvh, primary = make_frame(a)
     plain = pkg.Scene(bvh)
-    scene = plain if a.nodes == "fp32" else pkg.Scene(bvh, node_format=a.nodes)
+    scene = (plain if a.nodes == "fp32" and a.top_levels == 0 else
+             pkg.Scene(bvh, node_format=a.nodes, top_levels=a.top_levels))
     hits = plain.trace(torch.from_numpy(primary).to(dev))["hits"]
     _, ao = secondaries(a, tris, primary, pkg.hit_prims(hits.cpu().numpy()))
     idx = np.unique(np.linspace(0, ao.shape[0] - 1, min(a.ao_sample, ao.shape[0])).astype(np.int64))
@@ -1389,7 +1390,8 @@ def run_aolaunch(a):
         print(json.dumps({
             "metric": METRIC, "value": rays.shape[0] / (ms / 1e3) / 1e6, "unit": METRIC,
             "ms_per_launch": ms, "rays": int(rays.shape[0]), "workload": workload_name(a),
-            "nodes": a.nodes, "plan": plan, "triangles": int(bvh.info["n_tris"]),
+            "nodes": a.nodes, "top_levels": a.top_levels, "plan": plan,
+            "triangles": int(bvh.info["n_tris"]),
             "same_as_first_plan": bool(torch.equal(out, first)),
             "algorithmic_bytes_per_launch": alg, "node_record_bytes": scene.node_record_bytes,
             "node_visits_per_ray": float(cs[0]) / rays.shape[0],
