@@ -42,7 +42,7 @@ int export_fast(const Bvh& bvh, int gang, int node_memory, int leaf_memory, Fast
 // floats when the stride is below leaf_memory).
 //
 // Q8 record (branching N, Nm as above), 16-byte aligned: N4 64 B, N8 80 B,
-// N12 112 B, N16 144 B (FP32: 128 / 240 / 352 / 464 B):
+// N12 112 B, N16 144 B (FP32: 128 / 240 / 368 / 464 B):
 //   float    origin[3]      parent box lower corner (the quantisation frame)
 //   int8     exp[3], pad    per-axis power-of-two step: step = 2^exp
 //   uint32   inner_base, leaf_base; uint16 leaf_mask; uint8 count; uint8 depth

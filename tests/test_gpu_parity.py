@@ -619,7 +619,7 @@ def test_device_q8_encoding_matches_host(n, l):
         sc = pkg.Scene(b, node_format=fmt, top_levels=top)
         assert np.array_equal(sc.node_records(), b.node_records(node_format=fmt, top_levels=top))
         nm = -(-n // 4) * 4
-        want = {"q8": {4: 64, 8: 80, 12: 112, 16: 144}, "fp32": {4: 128, 8: 240, 12: 352,
+        want = {"q8": {4: 64, 8: 80, 12: 112, 16: 144}, "fp32": {4: 128, 8: 240, 12: 368,
                                                                  16: 464}}[fmt][nm]
         assert sc.node_record_bytes == want
 
