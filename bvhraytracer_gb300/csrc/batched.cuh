@@ -81,13 +81,19 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
 #ifndef BVHGPU_BATCHED_MIN_BLOCKS
 #define BVHGPU_BATCHED_MIN_BLOCKS 5
 #endif
-// KMODE 0: every lane takes its job's ray kind; 1: closest-hit jobs only;
-// 2: any-hit jobs only (the other kind's code is compiled out); 3: both
-// kinds in one launch with kind-uniform warps: a warp takes closest-hit rays
-// until their queue is empty and its lanes are done, then any-hit rays.
-template <int PROFILE, int KMODE>
-__global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
-    trace_batched_kernel(const __grid_constant__ JobTable t) {
+// KMODE 3 as one loop whose warps switch kind (0) or as the closest-hit loop
+// followed by the any-hit loop (1).
+#ifndef BVHGPU_BATCHED_TWO_LOOPS
+#define BVHGPU_BATCHED_TWO_LOOPS 0
+#endif
+// The persistent loop over the job list. KMODE 0: every lane takes its job's
+// ray kind; 1: closest-hit jobs only; 2: any-hit jobs only (the other kind's
+// code is compiled out); 3: both kinds with kind-uniform warps: a warp takes
+// closest-hit rays until their queue is empty and its lanes are done, then
+// any-hit rays from their own queue (the jobs are ordered closest-hit first;
+// t.split divides them). KSEG 1 / 2: the closest-hit / any-hit queue alone.
+template <int PROFILE, int KMODE, int KSEG = 0>
+__device__ __forceinline__ void batched_loop(const JobTable& t) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int stride = blockDim.x;
   uint32_t* stack = smem + threadIdx.x;
@@ -108,15 +114,15 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
   sc.leaf_depth = nullptr;
   sc.top_nodes = 0;
   int nm = 8, fmt = 0;
-  int kind = KMODE == 2 ? BVHGPU_ANY : BVHGPU_CLOSEST;
+  int kind = (KMODE == 2 || KSEG == 2) ? BVHGPU_ANY : BVHGPU_CLOSEST;
   // KMODE 3: the warp's ray kind (the same in every lane).
-  int wkind = KMODE == 3 && t.split == 0 ? BVHGPU_ANY : BVHGPU_CLOSEST;
-  bool drained = false;
+  int wkind = KMODE == 3 && (t.split == 0 || KSEG == 2) ? BVHGPU_ANY : BVHGPU_CLOSEST;
+  bool drained = KSEG == 1 && t.split == 0;
   uint32_t postponed = NONE;
 
   while (true) {
     const unsigned idle = __ballot_sync(FULL, !active);
-    if (KMODE == 3 && wkind == BVHGPU_CLOSEST && drained && idle == FULL) {
+    if (KMODE == 3 && KSEG == 0 && wkind == BVHGPU_CLOSEST && drained && idle == FULL) {
       wkind = BVHGPU_ANY;  // closest-hit rays all taken and traced: any-hit rays next
       drained = false;
     }
@@ -157,7 +163,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
           nm = J.nm;
           fmt = J.fmt;
           if (KMODE == 0) kind = J.kind;
-          if (KMODE == 3) kind = wkind;
+          if (KMODE == 3 && KSEG == 0) kind = wkind;
           const bvhgpu_ray_t in = load_ray(J.rays, local);
           best = Best();
           hit = false;
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
       }
     }
     if (__ballot_sync(FULL, active) == 0) {
-      if (drained && !(KMODE == 3 && wkind == BVHGPU_CLOSEST)) break;
+      if (drained && !(KMODE == 3 && KSEG == 0 && wkind == BVHGPU_CLOSEST)) break;
       continue;
     }
 
@@ -246,6 +252,17 @@ __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
       }
       active = false;
     }
+  }
+}
+
+template <int PROFILE, int KMODE>
+__global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
+    trace_batched_kernel(const __grid_constant__ JobTable t) {
+  if (KMODE == 3 && BVHGPU_BATCHED_TWO_LOOPS) {
+    batched_loop<PROFILE, 3, 1>(t);
+    batched_loop<PROFILE, 3, 2>(t);
+  } else {
+    batched_loop<PROFILE, KMODE>(t);
   }
 }
 
