@@ -81,17 +81,11 @@ BVHGPU_DEV bool batched_node_step(const SceneDev& sc, int nm, int fmt, uint32_t 
 #ifndef BVHGPU_BATCHED_MIN_BLOCKS
 #define BVHGPU_BATCHED_MIN_BLOCKS 5
 #endif
-// KMODE 3 as one loop whose warps switch kind (0) or as the closest-hit loop
-// followed by the any-hit loop (1).
-#ifndef BVHGPU_BATCHED_TWO_LOOPS
-#define BVHGPU_BATCHED_TWO_LOOPS 0
-#endif
 // The persistent loop over the job list. KMODE 0: every lane takes its job's
 // ray kind; 1: closest-hit jobs only; 2: any-hit jobs only (the other kind's
-// code is compiled out); 3: both kinds with kind-uniform warps: a warp takes
-// closest-hit rays until their queue is empty and its lanes are done, then
-// any-hit rays from their own queue (the jobs are ordered closest-hit first;
-// t.split divides them). KSEG 1 / 2: the closest-hit / any-hit queue alone.
+// code is compiled out). KSEG 0: every job's rays from t.head; 1: the
+// closest-hit segment [0, t.split) from t.head; 2: the any-hit segment
+// [t.split, t.total) from t.head_any (the jobs are ordered closest-hit first).
 template <int PROFILE, int KMODE, int KSEG = 0>
 __device__ __forceinline__ void batched_loop(const JobTable& t) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -114,26 +108,20 @@ __device__ __forceinline__ void batched_loop(const JobTable& t) {
   sc.leaf_depth = nullptr;
   sc.top_nodes = 0;
   int nm = 8, fmt = 0;
-  int kind = (KMODE == 2 || KSEG == 2) ? BVHGPU_ANY : BVHGPU_CLOSEST;
-  // KMODE 3: the warp's ray kind (the same in every lane).
-  int wkind = KMODE == 3 && (t.split == 0 || KSEG == 2) ? BVHGPU_ANY : BVHGPU_CLOSEST;
-  bool drained = KSEG == 1 && t.split == 0;
+  int kind = KMODE == 2 ? BVHGPU_ANY : BVHGPU_CLOSEST;
+  bool drained = KSEG != 0 && (KSEG == 1 ? t.split == 0 : t.split >= t.total);
   uint32_t postponed = NONE;
 
   while (true) {
     const unsigned idle = __ballot_sync(FULL, !active);
-    if (KMODE == 3 && KSEG == 0 && wkind == BVHGPU_CLOSEST && drained && idle == FULL) {
-      wkind = BVHGPU_ANY;  // closest-hit rays all taken and traced: any-hit rays next
-      drained = false;
-    }
-    const bool seg_any = KMODE == 3 && wkind == BVHGPU_ANY;
-    const uint64_t seg_begin = seg_any ? t.split : 0;
-    const uint64_t seg_end = KMODE == 3 && !seg_any ? t.split : t.total;
+    // The segment's bounds and queue head, read from the parameter bank
+    // where used rather than held in registers.
+    const uint64_t seg_begin = KSEG == 2 ? t.split : 0;
+    const uint64_t seg_end = KSEG == 1 ? t.split : t.total;
     if (!drained && idle != 0 && ((int)__popc(idle) >= t.refill_min || idle == FULL)) {
       const int leader = __ffs(idle) - 1;
       unsigned long long base = 0;
-      if ((int)lane == leader)
-        base = atomicAdd(seg_any ? t.head_any : t.head, (unsigned long long)__popc(idle));
+      if ((int)lane == leader) base = atomicAdd(KSEG == 2 ? t.head_any : t.head, (unsigned long long)__popc(idle));
       base = __shfl_sync(FULL, base, leader);
       if (seg_begin + base + __popc(idle) >= seg_end) drained = true;
       if (!active) {
@@ -163,7 +151,6 @@ __device__ __forceinline__ void batched_loop(const JobTable& t) {
           nm = J.nm;
           fmt = J.fmt;
           if (KMODE == 0) kind = J.kind;
-          if (KMODE == 3 && KSEG == 0) kind = wkind;
           const bvhgpu_ray_t in = load_ray(J.rays, local);
           best = Best();
           hit = false;
@@ -183,7 +170,7 @@ __device__ __forceinline__ void batched_loop(const JobTable& t) {
       }
     }
     if (__ballot_sync(FULL, active) == 0) {
-      if (drained && !(KMODE == 3 && KSEG == 0 && wkind == BVHGPU_CLOSEST)) break;
+      if (drained) break;
       continue;
     }
 
@@ -255,12 +242,16 @@ __device__ __forceinline__ void batched_loop(const JobTable& t) {
   }
 }
 
+// KMODE 0 to 2: one batched_loop over every job's rays. KMODE 3: both kinds
+// in one launch with kind-uniform warps: each warp runs the closest-hit loop
+// until the closest-hit queue is empty and its lanes are done, then the
+// any-hit loop over the any-hit queue (each loop compiled for its kind).
 template <int PROFILE, int KMODE>
 __global__ void __launch_bounds__(128, BVHGPU_BATCHED_MIN_BLOCKS)
     trace_batched_kernel(const __grid_constant__ JobTable t) {
-  if (KMODE == 3 && BVHGPU_BATCHED_TWO_LOOPS) {
-    batched_loop<PROFILE, 3, 1>(t);
-    batched_loop<PROFILE, 3, 2>(t);
+  if (KMODE == 3) {
+    batched_loop<PROFILE, 1, 1>(t);
+    batched_loop<PROFILE, 2, 2>(t);
   } else {
     batched_loop<PROFILE, KMODE>(t);
   }

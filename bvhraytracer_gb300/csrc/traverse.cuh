@@ -709,7 +709,11 @@ BVHGPU_DEV bool set_insert(uint32_t* tbl, int size, uint32_t key) {
 }
 
 template <int N, int PROFILE, int KIND, bool COUNT>
-__global__ void __launch_bounds__(256) trace_stream_kernel(SceneDev sc, TraceArgs a) {
+#ifndef BVHGPU_STREAM_MIN_BLOCKS
+#define BVHGPU_STREAM_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(256, BVHGPU_STREAM_MIN_BLOCKS)
+    trace_stream_kernel(SceneDev sc, TraceArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const int P = blockDim.x;
   const int tid = threadIdx.x;
