@@ -349,5 +349,47 @@ BVHGPU_DEV float f4get(const float4& v, int k) {
   return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
+// Packed pairs of floats in one 64-bit register, and the sm_100-family
+// instructions that apply one IEEE single-precision operation to both halves
+// (sub / mul .rn.f32x2: round to nearest per half, subnormals kept, no
+// contraction), so each half equals the scalar `a - b` / `a * b` of this
+// build (-fmad=false -ftz=false) bit for bit.
+BVHGPU_DEV uint64_t f2pack(float lo, float hi) {
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+BVHGPU_DEV float2 f2unpack(uint64_t v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+BVHGPU_DEV uint64_t f2sub(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+BVHGPU_DEV uint64_t f2mul(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// a + b rounded up / down per half (the pairs of __fadd_ru / __fadd_rd).
+BVHGPU_DEV uint64_t f2add_ru(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rp.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+BVHGPU_DEV uint64_t f2add_rd(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+BVHGPU_DEV uint64_t f2splat(float v) { return f2pack(v, v); }
+// (a - o) * s on a pair: two children's plane distances along one axis.
+BVHGPU_DEV float2 f2plane(float a0, float a1, uint64_t o2, uint64_t s2) {
+  return f2unpack(f2mul(f2sub(f2pack(a0, a1), o2), s2));
+}
+
 }  // namespace dev
 }  // namespace bvhgpu

@@ -43,6 +43,16 @@ struct SceneDev {
 #ifndef BVHGPU_NEARFAR
 #define BVHGPU_NEARFAR 1
 #endif
+// 1: the near / far slab test computes two children's plane distances per
+// packed f32x2 subtract and multiply; 0: one child per instruction.
+#ifndef BVHGPU_PAIRED_SLABS
+#define BVHGPU_PAIRED_SLABS 1
+#endif
+// 1: Q8 records take the paired slab test too, decoded two children per
+// packed instruction (more registers: the N8 any-hit kernel spills).
+#ifndef BVHGPU_PAIRED_Q8
+#define BVHGPU_PAIRED_Q8 0
+#endif
 // 1: leaf triangles loaded four at a time with 128-bit loads; 0: one at a time.
 #ifndef BVHGPU_LEAF_VEC
 #define BVHGPU_LEAF_VEC 1
@@ -165,6 +175,20 @@ BVHGPU_DEV float4 q8_row(uint32_t w, float origin, float step, bool up) {
   return v;
 }
 
+// q8_row as two packed pairs (children 0-1 and 2-3): the same bytes, the
+// same exact products and the same directed rounding per half.
+BVHGPU_DEV void q8_row2(uint32_t w, uint64_t origin2, uint64_t step2, bool up, uint64_t& p01,
+                        uint64_t& p23) {
+  const uint64_t bias = f2splat(8388608.0f);
+  const uint64_t b01 = f2pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u)),
+                              __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u)));
+  const uint64_t b23 = f2pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7542u)),
+                              __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7543u)));
+  const uint64_t q01 = f2mul(f2sub(b01, bias), step2), q23 = f2mul(f2sub(b23, bias), step2);
+  p01 = up ? f2add_ru(origin2, q01) : f2add_rd(origin2, q01);
+  p23 = up ? f2add_ru(origin2, q23) : f2add_rd(origin2, q23);
+}
+
 // One inner-node visit: slab-test the children and push the hits.
 // Returns false on stack overflow.
 // DIST: the save-distance traversal; each push also stores the child's entry
@@ -207,6 +231,14 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
     const int nx = r.inv[0] >= 0.0f ? 0 : 3, ny = r.inv[1] >= 0.0f ? 1 : 4;
     const int nz = r.inv[2] >= 0.0f ? 2 : 5;
     const int fx = nx == 0 ? 3 : 0, fy = ny == 1 ? 4 : 1, fz = nz == 2 ? 5 : 2;
+#if BVHGPU_PAIRED_SLABS
+    // Two children per subtract and multiply (f2plane); the minima, maxima
+    // and the comparison stay per child.
+    const uint64_t o2x = f2pack(r.o[0], r.o[0]), o2y = f2pack(r.o[1], r.o[1]);
+    const uint64_t o2z = f2pack(r.o[2], r.o[2]);
+    const uint64_t s2x = f2pack(r.inv[0], r.inv[0]), s2y = f2pack(r.inv[1], r.inv[1]);
+    const uint64_t s2z = f2pack(r.inv[2], r.inv[2]);
+#endif
 #pragma unroll
     for (int q = 0; q < NM / 4; ++q) {
       const float4 ax = rec_f4<SH>(rec + (nx * NM + 4 * q) * 4);
@@ -215,6 +247,28 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
       const float4 by = rec_f4<SH>(rec + (fy * NM + 4 * q) * 4);
       const float4 az = rec_f4<SH>(rec + (nz * NM + 4 * q) * 4);
       const float4 bz = rec_f4<SH>(rec + (fz * NM + 4 * q) * 4);
+#if BVHGPU_PAIRED_SLABS
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        if (4 * q + 2 * p < N) {
+          const int k = 2 * p;
+          const float2 nxp = f2plane(f4get(ax, k), f4get(ax, k + 1), o2x, s2x);
+          const float2 fxp = f2plane(f4get(bx, k), f4get(bx, k + 1), o2x, s2x);
+          const float2 nyp = f2plane(f4get(ay, k), f4get(ay, k + 1), o2y, s2y);
+          const float2 fyp = f2plane(f4get(by, k), f4get(by, k + 1), o2y, s2y);
+          const float2 nzp = f2plane(f4get(az, k), f4get(az, k + 1), o2z, s2z);
+          const float2 fzp = f2plane(f4get(bz, k), f4get(bz, k + 1), o2z, s2z);
+          float t0 = fmaxf(fmaxf(fmaxf(nxp.x, 0.0f), nyp.x), nzp.x);
+          float t1 = fminf(fminf(fminf(fxp.x, tmax), fyp.x), fzp.x);
+          hit |= (uint32_t)(t0 <= t1) << (4 * q + k);
+          if (4 * q + k + 1 < N) {
+            t0 = fmaxf(fmaxf(fmaxf(nxp.y, 0.0f), nyp.y), nzp.y);
+            t1 = fminf(fminf(fminf(fxp.y, tmax), fyp.y), fzp.y);
+            hit |= (uint32_t)(t0 <= t1) << (4 * q + k + 1);
+          }
+        }
+      }
+#else
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (4 * q + k < N) {
@@ -227,6 +281,52 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
           hit |= (uint32_t)(t0 <= t1) << (4 * q + k);
         }
       }
+#endif
+    }
+  } else if (BVHGPU_PAIRED_SLABS && MM && !DIST && (FMT == kFmtFP32 || BVHGPU_PAIRED_Q8)) {
+    // slab_mm with two children per subtract and multiply (and per Q8
+    // decode step), one axis at a time: t0 / t1 take the axes in slab_mm's
+    // order.
+#pragma unroll
+    for (int q = 0; q < NM / 4; ++q) {
+      float t0[4], t1[4];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        uint64_t lo[2], hi[2];
+        if (FMT == kFmtFP32) {
+          const float4 l = rec_f4<SH>(rec + (a * NM + 4 * q) * 4);
+          const float4 h = rec_f4<SH>(rec + ((3 + a) * NM + 4 * q) * 4);
+          lo[0] = f2pack(l.x, l.y);
+          lo[1] = f2pack(l.z, l.w);
+          hi[0] = f2pack(h.x, h.y);
+          hi[1] = f2pack(h.z, h.w);
+        } else {
+          const float qo = a == 0 ? ox : (a == 1 ? oy : oz);
+          const float qs = a == 0 ? sx : (a == 1 ? sy : sz);
+          const uint8_t* qb = rec + F::QBOX + 4 * q;
+          q8_row2(rec_u32<SH>(qb + a * NM), f2splat(qo), f2splat(qs), false, lo[0], lo[1]);
+          q8_row2(rec_u32<SH>(qb + (3 + a) * NM), f2splat(qo), f2splat(qs), true, hi[0], hi[1]);
+        }
+        const uint64_t o2 = f2splat(r.o[a]), s2 = f2splat(r.inv[a]);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          if (4 * q + 2 * p < N) {
+            const float2 tn = f2unpack(f2mul(f2sub(lo[p], o2), s2));
+            const float2 tf = f2unpack(f2mul(f2sub(hi[p], o2), s2));
+            const float mn[2] = {fminf(tn.x, tf.x), fminf(tn.y, tf.y)};
+            const float mx[2] = {fmaxf(tn.x, tf.x), fmaxf(tn.y, tf.y)};
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int k = 2 * p + j;
+              t0[k] = fmaxf(mn[j], a == 0 ? 0.0f : t0[k]);
+              t1[k] = fminf(mx[j], a == 0 ? tmax : t1[k]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (4 * q + k < N) hit |= (uint32_t)(t0[k] <= t1[k]) << (4 * q + k);
     }
   } else
 #pragma unroll
