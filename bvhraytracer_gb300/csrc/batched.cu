@@ -1,6 +1,16 @@
 // Instantiation and launch of the batched (multi-scene) persistent kernel.
 #include <cuda_runtime.h>
 
+// Slab tests of the multi-scene kernel: packed pairs (1) or one child per
+// instruction (0), independent of the single-scene kernels' choice. Device
+// code is compiled per translation unit (no device linking), so the two
+// choices do not meet.
+#ifndef BVHGPU_BATCHED_PAIRED
+#define BVHGPU_BATCHED_PAIRED 0
+#endif
+#undef BVHGPU_PAIRED_SLABS
+#define BVHGPU_PAIRED_SLABS BVHGPU_BATCHED_PAIRED
+
 #include "batched.cuh"
 
 namespace bvhgpu {

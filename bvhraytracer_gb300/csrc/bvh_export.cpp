@@ -178,6 +178,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
   out.nodes.assign((size_t)out.n_inner * out.record_bytes, 0);
   const int pbytes = q8_perm_bytes(nm);
   if (node_format != 0) out.q8_perm.assign((size_t)out.n_inner * pbytes, 0);
+  out.child_entry.assign((size_t)out.n_inner * nm, 0u);
   for (uint32_t g = 0; g < out.n_inner; ++g) {
     const uint32_t id = inner_order[g];
     const CompactNode& c = bvh.nodes[id];
@@ -196,6 +197,8 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
         have_inner = true;
       }
     }
+    for (uint32_t j = 0; j < c.child_count; ++j)
+      out.child_entry[(size_t)g * nm + j] = entry_of(c.child_begin + j);
     // Sibling contiguity in both numberings.
     {
       uint32_t li = leaf_base, ii = inner_base;

@@ -64,6 +64,10 @@ struct DeviceLayout {
   int record_bytes = 0;
   std::vector<uint8_t> nodes;         // n_inner * record_bytes
   std::vector<uint8_t> q8_perm;       // Q8: n_inner * q8_perm_bytes push sequences
+  // n_inner * node_stride: the stack entry of each child slot (the record's
+  // leaf / inner numbering resolved per child; 0 for empty slots), read by
+  // pushes in child-index order.
+  std::vector<uint32_t> child_entry;
   std::vector<float> leaves;          // n_leaves * 9 * leaf_memory
   std::vector<uint32_t> leaf_prim;    // n_leaves * leaf_memory (input ids)
   std::vector<uint8_t> leaf_depth;    // n_leaves

@@ -38,6 +38,9 @@ struct SceneDev {
   int any_index_order = 0;
   // Q8 records: the push sequences, NodeFmt<N, Q8>::PSB bytes per inner node.
   const uint8_t* q8_perm = nullptr;
+  // NodeFmt<N>::NM stack entries per inner node, one per child slot (null:
+  // computed from the record).
+  const uint32_t* child_entry = nullptr;
 };
 
 #ifndef BVHGPU_NEARFAR
@@ -48,10 +51,16 @@ struct SceneDev {
 #ifndef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS 1
 #endif
+// Pushes of hit children in child-index order from SceneDev::child_entry:
+// 0 off (entries computed from the record), 1 unrolled predicated stores,
+// 2 a loop over the hit children.
+#ifndef BVHGPU_ENTRY_PUSH
+#define BVHGPU_ENTRY_PUSH 2
+#endif
 // 1: Q8 records take the paired slab test too, decoded two children per
-// packed instruction (more registers: the N8 any-hit kernel spills).
+// packed instruction.
 #ifndef BVHGPU_PAIRED_Q8
-#define BVHGPU_PAIRED_Q8 0
+#define BVHGPU_PAIRED_Q8 1
 #endif
 // 1: leaf triangles loaded four at a time with 128-bit loads; 0: one at a time.
 #ifndef BVHGPU_LEAF_VEC
@@ -205,7 +214,7 @@ template <int N, int PROFILE, int KIND, bool COUNT, bool MM, int FMT, bool SH, b
 BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_t* stack,
                            int stride, int& sp, int cap, Counters& ctr, int& depth_out,
                            float* dstack = nullptr, bool index_order = false,
-                           const uint8_t* q8_side = nullptr) {
+                           const uint8_t* q8_side = nullptr, const uint32_t* ent = nullptr) {
   using F = NodeFmt<N, FMT>;
   constexpr int NM = F::NM;
   const uint4 meta = rec_u4<SH>(rec + F::META);
@@ -403,6 +412,35 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   uint32_t pm;
   bool descending = false;
   if (KIND == BVHGPU_ANY && (PROFILE == BVHGPU_PROFILE_FAST || (!COUNT && index_order))) {
+    if (BVHGPU_ENTRY_PUSH != 0 && ent != nullptr) {
+      // The children's stack entries precomputed per slot: the same pushes
+      // as the loop below (ascending child index). 1: N predicated stores
+      // that every lane runs in step; 2: a loop over the hit children with
+      // one load per push.
+      if (sp + __popc(hit) > cap) return false;
+      if (BVHGPU_ENTRY_PUSH == 1) {
+#pragma unroll
+        for (int q = 0; q < NM / 4; ++q) {
+          const uint4 w = ldgu4(ent + 4 * q);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (4 * q + k < N && ((hit >> (4 * q + k)) & 1u)) {
+              stack[sp * stride] = k == 0 ? w.x : (k == 1 ? w.y : (k == 2 ? w.z : w.w));
+              ++sp;
+            }
+          }
+        }
+      } else {
+        uint32_t h = hit;
+        while (h) {
+          const int c = __ffs(h) - 1;
+          h &= h - 1u;
+          stack[sp * stride] = __ldg(ent + c);
+          ++sp;
+        }
+      }
+      return true;
+    }
     perm = 0xFEDCBA9876543210ull;
     pm = hit;
   } else {
@@ -576,24 +614,26 @@ BVHGPU_DEV bool node_step(const SceneDev& sc, uint32_t e, const uint8_t* top_sme
   constexpr int REC = NodeFmt<N, FMT>::REC;
   const uint8_t* side =
       FMT == kFmtFP32 ? nullptr : sc.q8_perm + (size_t)e * NodeFmt<N, FMT>::PSB;
+  const uint32_t* ent =
+      sc.child_entry != nullptr ? sc.child_entry + (size_t)e * NodeFmt<N, FMT>::NM : nullptr;
   if (e < top) {
     const uint8_t* rec = top_smem + (size_t)e * REC;
     if (r.exact)
       return visit_node<N, PROFILE, KIND, COUNT, false, FMT, true, DIST>(
-          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
+          rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side, ent);
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, true, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side, ent);
   }
   const uint8_t* rec = sc.nodes + (size_t)e * REC;
   if (r.exact)
     return visit_node<N, PROFILE, KIND, COUNT, false, FMT, false, DIST>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side, ent);
   constexpr bool kNF = BVHGPU_NEARFAR && FMT == kFmtFP32 && !DIST;
   if (kNF && sc.boxes_ordered)
     return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST, kNF>(
-        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
+        rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side, ent);
   return visit_node<N, PROFILE, KIND, COUNT, true, FMT, false, DIST>(
-      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side);
+      rec, r, tmax, stack, stride, sp, cap, ctr, depth, dstack, sc.any_index_order != 0, side, ent);
 }
 
 template <int PROFILE, int KIND, bool COUNT>
