@@ -51,11 +51,10 @@ struct SceneDev {
 #ifndef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS 1
 #endif
-// Pushes of hit children in child-index order from SceneDev::child_entry:
-// 0 off (entries computed from the record), 1 unrolled predicated stores,
-// 2 a loop over the hit children.
+// 1: pushes of hit children in child-index order read their stack entries
+// from SceneDev::child_entry; 0: computed from the record.
 #ifndef BVHGPU_ENTRY_PUSH
-#define BVHGPU_ENTRY_PUSH 2
+#define BVHGPU_ENTRY_PUSH 1
 #endif
 // 1: Q8 records take the paired slab test too, decoded two children per
 // packed instruction.
@@ -412,32 +411,17 @@ BVHGPU_DEV bool visit_node(const uint8_t* rec, const Ray& r, float tmax, uint32_
   uint32_t pm;
   bool descending = false;
   if (KIND == BVHGPU_ANY && (PROFILE == BVHGPU_PROFILE_FAST || (!COUNT && index_order))) {
-    if (BVHGPU_ENTRY_PUSH != 0 && ent != nullptr) {
+    if (BVHGPU_ENTRY_PUSH && ent != nullptr) {
       // The children's stack entries precomputed per slot: the same pushes
-      // as the loop below (ascending child index). 1: N predicated stores
-      // that every lane runs in step; 2: a loop over the hit children with
-      // one load per push.
+      // as the loop below (ascending child index), one load per push instead
+      // of the record decode and the sequence lookup.
       if (sp + __popc(hit) > cap) return false;
-      if (BVHGPU_ENTRY_PUSH == 1) {
-#pragma unroll
-        for (int q = 0; q < NM / 4; ++q) {
-          const uint4 w = ldgu4(ent + 4 * q);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            if (4 * q + k < N && ((hit >> (4 * q + k)) & 1u)) {
-              stack[sp * stride] = k == 0 ? w.x : (k == 1 ? w.y : (k == 2 ? w.z : w.w));
-              ++sp;
-            }
-          }
-        }
-      } else {
-        uint32_t h = hit;
-        while (h) {
-          const int c = __ffs(h) - 1;
-          h &= h - 1u;
-          stack[sp * stride] = __ldg(ent + c);
-          ++sp;
-        }
+      uint32_t h = hit;
+      while (h) {
+        const int c = __ffs(h) - 1;
+        h &= h - 1u;
+        stack[sp * stride] = __ldg(ent + c);
+        ++sp;
       }
       return true;
     }
