@@ -252,20 +252,27 @@ static int scratch_alloc(int device, void** p, size_t bytes, cudaStream_t st) {
   return e == cudaSuccess ? BVHGPU_OK : set_error(BVHGPU_ERR_OOM, "scratch allocation failed");
 }
 
+// Scratch bytes of a reordered launch of n rays into k x k cells per face.
+static size_t reorder_bytes(uint64_t n, int k) {
+  return align256(n * 4) + dev::reorder_scratch_bytes(n, k);
+}
+
 // launch() after grouping the rays by direction when cfg.reorder > 0: a
 // counting sort writes the input indices in bin order, the kernels take the
 // rays in that order and write every result to its input slot. The scratch
-// (about 6 bytes per ray) is allocated and freed on the stream.
+// (about 6 bytes per ray, reorder_bytes) is the caller's `scratch` or is
+// allocated and freed on the stream.
 static int launch_reordered(bvhgpu_scene_t s, dev::TraceArgs a, const dev::LaunchCfg& cfg,
-                            cudaStream_t st) {
+                            cudaStream_t st, void* scratch = nullptr) {
   if (cfg.reorder <= 0 || a.n < 2) return launch(s, a, cfg, st);
   if (a.n > 0xFFFFFFFFull)
     return set_error(BVHGPU_ERR_UNSUPPORTED, "reorder: at most 2^32 - 1 rays per call");
   const size_t perm_bytes = align256(a.n * 4);
-  const size_t bytes = perm_bytes + dev::reorder_scratch_bytes(a.n, cfg.reorder);
-  void* p = nullptr;
-  int arc = scratch_alloc(s->device, &p, bytes, st);
-  if (arc) return arc;
+  void* p = scratch;
+  if (!p) {
+    int arc = scratch_alloc(s->device, &p, reorder_bytes(a.n, cfg.reorder), st);
+    if (arc) return arc;
+  }
   cudaError_t e;
   auto* perm = reinterpret_cast<uint32_t*>(p);
   e = dev::reorder_rays(a.rays, a.n, cfg.reorder, perm, static_cast<uint8_t*>(p) + perm_bytes,
@@ -277,8 +284,10 @@ static int launch_reordered(bvhgpu_scene_t s, dev::TraceArgs a, const dev::Launc
     a.out_index = perm;
     rc = launch(s, a, cfg, st);
   }
-  e = cudaFreeAsync(p, st);
-  if (rc == BVHGPU_OK && e != cudaSuccess) rc = cuda_error(e, "reorder scratch free");
+  if (!scratch) {
+    e = cudaFreeAsync(p, st);
+    if (rc == BVHGPU_OK && e != cudaSuccess) rc = cuda_error(e, "reorder scratch free");
+  }
   return rc;
 }
 
@@ -655,15 +664,27 @@ int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 
 }  // extern "C"
 
-// Host-buffer pipeline: chunks per batch and the largest chunk (Mi rays).
-// Measured on the 1M-triangle frame (20.7M rays in three batches): 4 / 4 Mi
-// 9.24 ms, 8 / 2 Mi 9.54, 8 / 4 Mi 9.55, 3 / 8 Mi 9.37, 2 / 8 Mi 9.75,
-// 16 / 1 Mi 9.68.
+// Host-buffer pipeline: chunks per batch and the largest chunk (Mi rays)
+// when the chunks do not grow. Measured on the 1M-triangle frame (20.7M rays
+// in three batches): 4 / 4 Mi 9.24 ms, 8 / 2 Mi 9.54, 8 / 4 Mi 9.55,
+// 3 / 8 Mi 9.37, 2 / 8 Mi 9.75, 16 / 1 Mi 9.68.
 #ifndef BVHGPU_HOST_CHUNKS
 #define BVHGPU_HOST_CHUNKS 4
 #endif
 #ifndef BVHGPU_HOST_CHUNK_MAX
 #define BVHGPU_HOST_CHUNK_MAX 4
+#endif
+// 1: chunks that double from 256 Ki rays up to BVHGPU_HOST_GROW_MAX Mi over
+// the whole call (across batch boundaries), instead of quarters of each
+// batch. Same frame, with the reorder scratch held per stream: median step
+// 8.74-8.75 ms growing to 8 Mi, 8.84-9.15 ms in quarters; growing to 4 Mi
+// (10.42 ms) or 16 Mi (10.27 ms, when the scratch came from the pool) was
+// slower.
+#ifndef BVHGPU_HOST_GROW
+#define BVHGPU_HOST_GROW 1
+#endif
+#ifndef BVHGPU_HOST_GROW_MAX
+#define BVHGPU_HOST_GROW_MAX 8
 #endif
 
 namespace {
@@ -699,23 +720,54 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
       if (e != cudaSuccess) return cuda_error(e, "create pipeline event");
     }
   }
-  // Chunks of a quarter of each batch, between 256 Ki and 4 Mi rays: small
-  // enough that the first copy in and the last copy out (the parts that do
-  // not overlap a trace) are short, large enough to fill the GPU and keep
-  // the per-chunk launch tails and reorder passes few.
-  std::vector<uint64_t> chunk(nb);
+  // The chunks (batch, first ray, rays). Growing: the first chunk is small,
+  // so the copy in that no trace overlaps is short, and each next one twice
+  // as large (copies run faster than traces, so a chunk's copy ends while
+  // the previous chunk traces), up to a cap; a batch's remainder below half
+  // the current size joins its last chunk. Otherwise: a quarter of each
+  // batch, between 256 Ki and 4 Mi rays.
+  struct Chunk {
+    int batch;
+    uint64_t first, n;
+  };
+  std::vector<Chunk> chunks;
   uint64_t max_chunk = 0;
-  for (int k = 0; k < nb; ++k) {
-    uint64_t c = (b[k].n + BVHGPU_HOST_CHUNKS - 1) / BVHGPU_HOST_CHUNKS;
-    c = std::max<uint64_t>(c, 256ull << 10);
-    c = std::min<uint64_t>(c, (uint64_t)BVHGPU_HOST_CHUNK_MAX << 20);
-    c = std::min<uint64_t>(c, b[k].n);
-    chunk[k] = c;
-    max_chunk = std::max(max_chunk, c);
+  if (BVHGPU_HOST_GROW) {
+    uint64_t size = 256ull << 10;
+    const uint64_t cap = (uint64_t)BVHGPU_HOST_GROW_MAX << 20;
+    for (int k = 0; k < nb; ++k) {
+      for (uint64_t first = 0; first < b[k].n;) {
+        uint64_t m = std::min<uint64_t>(size, b[k].n - first);
+        if (b[k].n - first - m < size / 2) m = b[k].n - first;
+        chunks.push_back({k, first, m});
+        max_chunk = std::max(max_chunk, m);
+        first += m;
+        size = std::min<uint64_t>(size * 2, cap);
+      }
+    }
+  } else {
+    for (int k = 0; k < nb; ++k) {
+      uint64_t c = (b[k].n + BVHGPU_HOST_CHUNKS - 1) / BVHGPU_HOST_CHUNKS;
+      c = std::max<uint64_t>(c, 256ull << 10);
+      c = std::min<uint64_t>(c, (uint64_t)BVHGPU_HOST_CHUNK_MAX << 20);
+      c = std::min<uint64_t>(c, b[k].n);
+      for (uint64_t first = 0; first < b[k].n; first += c) {
+        chunks.push_back({k, first, std::min<uint64_t>(c, b[k].n - first)});
+        max_chunk = std::max(max_chunk, c);
+      }
+    }
   }
   if (max_chunk == 0) return BVHGPU_OK;
+  // Per stream: the chunk's rays, its results and the reorder scratch of the
+  // largest reordered chunk (held for the call, so that no allocation on one
+  // stream waits for memory the other stream frees).
+  size_t sort_bytes = 0;
+  for (const Chunk& c : chunks)
+    if (b[c.batch].cfg.reorder > 0 && c.n >= 2)
+      sort_bytes = std::max(sort_bytes, reorder_bytes(c.n, b[c.batch].cfg.reorder));
   const size_t ray_bytes = align256(max_chunk * sizeof(bvhgpu_ray_t));
-  const size_t per_stream = ray_bytes + align256(max_chunk * sizeof(bvhgpu_hit_t));
+  const size_t out_bytes = align256(max_chunk * sizeof(bvhgpu_hit_t));
+  const size_t per_stream = ray_bytes + out_bytes + sort_bytes;
   const size_t need = per_stream * NS;
   if (need > s->stage_bytes) {
     cudaStreamSynchronize(st);
@@ -734,38 +786,35 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
     if (e != cudaSuccess) return cuda_error(e, "pipeline wait");
   }
   int rc = BVHGPU_OK;
-  uint64_t k = 0;  // chunk counter over all batches: picks the stream
-  for (int bi = 0; bi < nb && rc == BVHGPU_OK; ++bi) {
-    const HostBatch& B = b[bi];
+  for (size_t k = 0; k < chunks.size() && rc == BVHGPU_OK; ++k) {
+    const HostBatch& B = b[chunks[k].batch];
     const bool closest = B.cfg.kind == BVHGPU_CLOSEST;
     const size_t out_rec = closest ? sizeof(bvhgpu_hit_t) : 1;
-    for (uint64_t first = 0; first < B.n && rc == BVHGPU_OK; first += chunk[bi], ++k) {
-      const uint64_t m = std::min<uint64_t>(chunk[bi], B.n - first);
-      const int si = (int)(k % NS);
-      cudaStream_t cs = s->host_stream[si];
-      uint8_t* base = static_cast<uint8_t*>(s->d_stage) + per_stream * si;
-      auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(base);
-      uint8_t* d_out = base + ray_bytes;
-      e = cudaMemcpyAsync(d_rays, B.rays + first, m * sizeof(bvhgpu_ray_t),
-                          cudaMemcpyHostToDevice, cs);
-      if (e != cudaSuccess) {
-        rc = cuda_error(e, "copy rays in");
-        break;
-      }
-      dev::TraceArgs a;
-      a.rays = d_rays;
-      a.n = m;
-      a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
-      a.occluded = closest ? nullptr : d_out;
-      a.counters = nullptr;
-      a.depth_hist = nullptr;
-      a.stack_cap = stack_cap(s);
-      rc = launch_reordered(s, a, B.cfg, cs);
-      if (rc) break;
-      void* dst = closest ? (void*)(B.hits + first) : (void*)(B.occluded + first);
-      e = cudaMemcpyAsync(dst, d_out, m * out_rec, cudaMemcpyDeviceToHost, cs);
-      if (e != cudaSuccess) rc = cuda_error(e, "copy results out");
+    const uint64_t first = chunks[k].first, m = chunks[k].n;
+    const int si = (int)(k % NS);  // the chunk counter picks the stream
+    cudaStream_t cs = s->host_stream[si];
+    uint8_t* base = static_cast<uint8_t*>(s->d_stage) + per_stream * si;
+    auto* d_rays = reinterpret_cast<bvhgpu_ray_t*>(base);
+    uint8_t* d_out = base + ray_bytes;
+    e = cudaMemcpyAsync(d_rays, B.rays + first, m * sizeof(bvhgpu_ray_t),
+                        cudaMemcpyHostToDevice, cs);
+    if (e != cudaSuccess) {
+      rc = cuda_error(e, "copy rays in");
+      break;
     }
+    dev::TraceArgs a;
+    a.rays = d_rays;
+    a.n = m;
+    a.hits = closest ? reinterpret_cast<bvhgpu_hit_t*>(d_out) : nullptr;
+    a.occluded = closest ? nullptr : d_out;
+    a.counters = nullptr;
+    a.depth_hist = nullptr;
+    a.stack_cap = stack_cap(s);
+    rc = launch_reordered(s, a, B.cfg, cs, sort_bytes ? base + ray_bytes + out_bytes : nullptr);
+    if (rc) break;
+    void* dst = closest ? (void*)(B.hits + first) : (void*)(B.occluded + first);
+    e = cudaMemcpyAsync(dst, d_out, m * out_rec, cudaMemcpyDeviceToHost, cs);
+    if (e != cudaSuccess) rc = cuda_error(e, "copy results out");
   }
   for (int i = 0; i < NS; ++i) {
     cudaEventRecord(s->host_event[i], s->host_stream[i]);
