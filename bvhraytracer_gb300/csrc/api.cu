@@ -677,9 +677,9 @@ int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 // 1: chunks that double from 256 Ki rays up to BVHGPU_HOST_GROW_MAX Mi over
 // the whole call (across batch boundaries), instead of quarters of each
 // batch. Same frame, with the reorder scratch held per stream: median step
-// 8.74-8.75 ms growing to 8 Mi, 8.84-9.15 ms in quarters; growing to 4 Mi
-// (10.42 ms) or 16 Mi (10.27 ms, when the scratch came from the pool) was
-// slower.
+// 8.74-8.75 ms growing to 8 Mi, 8.84-9.15 ms in quarters. (With the scratch
+// allocated per launch from the pool, growing chunks alternated between
+// 8.75 and 10.25 ms per step from run to run.)
 #ifndef BVHGPU_HOST_GROW
 #define BVHGPU_HOST_GROW 1
 #endif
