@@ -729,7 +729,8 @@ def run_batch(a):
 
             best, _ = autotune.tune_branching(
                 tris, batches_fn, pairs=tuple((n, l) for n in (4, 8, 16) for l in (4, 8, 16)),
-                layouts=(("fp32", 0),), time_fn=time_fn, reps=1)
+                layouts=(("fp32", 0),), time_fn=time_fn, reps=1,
+                prefer=(a.branching, a.leaf), margin=0.05)
             _, (bn, bl), bvh, plan, tuned = best
             scene = tuned[("fp32", 0)]
             block, stack = 128, "shared"

@@ -95,14 +95,19 @@ def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFA
 def tune_branching(tris, batches_fn, *, pairs=((4, 4), (4, 8), (8, 4), (8, 8), (16, 4), (16, 8),
                                               (16, 16)),
                    profile: str = "instrumented", reps: int = 2, device: int = 0,
-                   time_fn=None, **kw):
+                   time_fn=None, prefer=None, margin: float = 0.0, **kw):
     """Also picks N and L: builds a BVH per pair, tunes each, returns the pair
     with the lowest total time. ``batches_fn(scene)`` returns the batches to
     time for a scene (secondary rays may depend on the primary hits).
     ``time_fn(scene, batches)``, when given, times the call the batches will
     actually run in (for instance the multi-scene launch of bvhgpu_trace_jobs)
-    and returns its milliseconds; the plan then records that call."""
+    and returns its milliseconds; the plan then records that call.
+    ``prefer`` (a pair among ``pairs``) is kept unless the fastest pair beats
+    it by more than the fraction ``margin``: timings of short launches are
+    noisy, and a pair shared by many scenes keeps their jobs in one launch
+    group."""
     best = None
+    kept = None
     results = {}
     for n, l in pairs:
         bvh = Bvh(tris, n, l)
@@ -117,6 +122,10 @@ def tune_branching(tris, batches_fn, *, pairs=((4, 4), (4, 8), (8, 4), (8, 8), (
                                       scenes={("fp32", 0): scene}, **kw)
         total = sum(ms for _, _, ms in plan.choices)
         results[(n, l)] = total
+        if (n, l) == prefer:
+            kept = (total, (n, l), bvh, plan, scenes)
         if best is None or total < best[0]:
             best = (total, (n, l), bvh, plan, scenes)
+    if kept is not None and best[0] >= kept[0] * (1.0 - margin):
+        best = kept
     return best, results

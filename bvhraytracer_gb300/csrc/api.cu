@@ -59,6 +59,7 @@ struct bvhgpu_scene {
   uint32_t* d_leaf_prim = nullptr;
   uint8_t* d_leaf_depth = nullptr;
   uint32_t* d_child_entry = nullptr;
+  float* d_leaf_bounds = nullptr;
   int* d_status = nullptr;
   uint32_t* d_prim_slot = nullptr;  // uploaded on first FP64 check
   // Queue heads of the persistent scheme: one slot per launch, round robin,
@@ -90,6 +91,7 @@ struct bvhgpu_scene {
     s.boxes_ordered = layout.boxes_ordered ? 1 : 0;
     s.q8_perm = d_q8_perm;
     s.child_entry = d_child_entry;
+    s.leaf_bounds = d_leaf_bounds;
     return s;
   }
   void release() {
@@ -99,6 +101,7 @@ struct bvhgpu_scene {
     cudaFree(d_leaf_prim);
     cudaFree(d_leaf_depth);
     cudaFree(d_child_entry);
+    cudaFree(d_leaf_bounds);
     cudaFree(d_status);
     cudaFree(d_queue);
     cudaFree(d_prim_slot);
@@ -113,6 +116,7 @@ struct bvhgpu_scene {
     d_leaf_prim = nullptr;
     d_leaf_depth = nullptr;
     d_child_entry = nullptr;
+    d_leaf_bounds = nullptr;
     d_status = nullptr;
     d_queue = nullptr;
     d_prim_slot = nullptr;
@@ -492,7 +496,8 @@ int bvhgpu_scene_create(bvhgpu_bvh_t h, const bvhgpu_scene_params_t* params, bvh
   if ((rc = upload(&s->d_nodes, s->layout.nodes)) || (rc = upload(&s->d_leaves, s->layout.leaves)) ||
       (rc = upload(&s->d_leaf_prim, s->layout.leaf_prim)) ||
       (rc = upload(&s->d_leaf_depth, s->layout.leaf_depth)) ||
-      (rc = upload(&s->d_child_entry, s->layout.child_entry))) {
+      (rc = upload(&s->d_child_entry, s->layout.child_entry)) ||
+      (rc = upload(&s->d_leaf_bounds, s->layout.leaf_bounds))) {
     s->release();
     delete s;
     return rc;

@@ -10,6 +10,9 @@
 #endif
 #undef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS BVHGPU_BATCHED_PAIRED
+// The jobs carry no triangle bounds: the pre-test computes them.
+#undef BVHGPU_LEAF_BOUNDS
+#define BVHGPU_LEAF_BOUNDS 0
 
 #include "batched.cuh"
 

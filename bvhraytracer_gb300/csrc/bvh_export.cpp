@@ -310,6 +310,7 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
   out.leaves.assign((size_t)nl * 9 * leaf_memory, 0.0f);
   out.leaf_prim.assign((size_t)nl * leaf_memory, 0xFFFFFFFFu);
   out.leaf_depth.assign(nl, 0);
+  out.leaf_bounds.assign((size_t)nl * 6 * leaf_memory, 0.0f);
   const float qnan = std::numeric_limits<float>::quiet_NaN();
   for (size_t id = 0; id < n; ++id) {
     const CompactNode& c = bvh.nodes[id];
@@ -323,6 +324,11 @@ int build_device_layout(const Bvh& bvh, int gang, int leaf_memory, int node_form
       for (int v = 0; v < 3; ++v)
         for (int a = 0; a < 3; ++a) blk[(v * 3 + a) * real + i] = t.p[v][a];
       out.leaf_prim[k * leaf_memory + i] = t.id;
+      float* bnd = &out.leaf_bounds[k * 6 * leaf_memory];
+      for (int a = 0; a < 3; ++a) {
+        bnd[a * leaf_memory + i] = std::fmin(std::fmin(t.p[0][a], t.p[1][a]), t.p[2][a]);
+        bnd[(3 + a) * leaf_memory + i] = std::fmax(std::fmax(t.p[0][a], t.p[1][a]), t.p[2][a]);
+      }
     }
     if (real != leaf_memory) {
       blk[leaf_memory * 9 - 2] = (float)real;

@@ -71,6 +71,10 @@ struct DeviceLayout {
   std::vector<float> leaves;          // n_leaves * 9 * leaf_memory
   std::vector<uint32_t> leaf_prim;    // n_leaves * leaf_memory (input ids)
   std::vector<uint8_t> leaf_depth;    // n_leaves
+  // n_leaves * 6 * leaf_memory: per triangle slot the smallest (rows 0-2)
+  // and largest (rows 3-5) vertex coordinate along x, y, z (IEEE min / max
+  // of the three vertices), read by the watertight box pre-test.
+  std::vector<float> leaf_bounds;
   uint32_t n_inner = 0, n_leaves = 0;
   uint32_t root_entry = 0;            // stack entry of the root
   uint32_t top_nodes = 0;             // inner nodes laid out first

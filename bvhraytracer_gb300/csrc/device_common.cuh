@@ -183,8 +183,9 @@ template <bool MM> BVHGPU_DEV float tmax2(float a, float b) { return MM ? fmaxf(
 // Watertight ray-triangle test of Triangle::intersect(Ray&)
 // (src/primitives/triangle.cpp:52-249), on points given in the ray's
 // permuted axes (x' = kx, y' = ky, z' = kz). Returns true on a hit with
-// t <= tmax; b1 / b2 are the weights of p1 / p2.
-template <bool MM>
+// t <= tmax; b1 / b2 are the weights of p1 / p2. PRE false: the caller ran
+// the box pre-test and it passed.
+template <bool MM, bool PRE = true>
 BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, float& t_out,
                            float& b1_out, float& b2_out) {
   const float ox = sel3(r.kx, r.o[0], r.o[1], r.o[2]);
@@ -194,7 +195,7 @@ BVHGPU_DEV bool watertight(const float (&p)[3][3], const Ray& r, float tmax, flo
   float p0x = p[0][0] - ox, p0y = p[0][1] - oy, p0z = p[0][2] - oz;
   float p1x = p[1][0] - ox, p1y = p[1][1] - oy, p1z = p[1][2] - oz;
   float p2x = p[2][0] - ox, p2y = p[2][1] - oy, p2z = p[2][2] - oz;
-  {
+  if (PRE) {
     // Per-triangle box pre-test (triangle.cpp:55-79) in the permuted axes
     // (the max / min of three values does not depend on the axis order).
     // The reference computes (min(p) - o) * inv; rounding of a - o is

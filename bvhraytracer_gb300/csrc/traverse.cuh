@@ -41,6 +41,9 @@ struct SceneDev {
   // NodeFmt<N>::NM stack entries per inner node, one per child slot (null:
   // computed from the record).
   const uint32_t* child_entry = nullptr;
+  // 6 * leaf_memory floats per leaf: each triangle slot's vertex minima
+  // (rows 0-2) and maxima (rows 3-5) per axis (read when BVHGPU_LEAF_BOUNDS).
+  const float* leaf_bounds = nullptr;
 };
 
 #ifndef BVHGPU_NEARFAR
@@ -50,6 +53,12 @@ struct SceneDev {
 // packed f32x2 subtract and multiply; 0: one child per instruction.
 #ifndef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS 1
+#endif
+// 1: the instrumented profile's watertight pre-test reads the triangles'
+// stored bounds (SceneDev::leaf_bounds, which every scene view then carries)
+// and loads a triangle's vertices only when it passes.
+#ifndef BVHGPU_LEAF_BOUNDS
+#define BVHGPU_LEAF_BOUNDS 1
 #endif
 // 1: pushes of hit children in child-index order read their stack entries
 // from SceneDev::child_entry; 0: computed from the record.
@@ -483,8 +492,8 @@ struct Best {
 // (the leaf's result is the same); with COUNT true all triangles are tested
 // like the reference.
 template <int PROFILE, int KIND, bool COUNT, bool MM>
-BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax, Best& best,
-                           Counters& ctr) {
+BVHGPU_DEV bool visit_leaf_points(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax,
+                                  Best& best, Counters& ctr) {
   const uint32_t leaf = e & kLeafIndexMask;
   const int cnt = (int)((e >> kLeafCountShift) & 15u) + 1;
   const int gang = sc.gang;
@@ -586,6 +595,86 @@ BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& 
     any = true;
   }
   return any;
+}
+
+// visit_leaf for the instrumented profile with NaN-free rays: watertight()'s
+// box pre-test from the stored bounds (SceneDev::leaf_bounds). Rounding of
+// a - o is monotonic in a, so (min(p) - o) * inv is the min(p - o) * inv that
+// watertight() computes, and the IEEE minima / maxima over the axes do not
+// depend on their order. Two triangles per packed subtract and multiply; a
+// triangle's vertices are loaded only when it passes (about one test in six
+// for ambient-occlusion rays).
+template <int KIND, bool COUNT, bool MM>
+BVHGPU_DEV bool visit_leaf_bounds(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax,
+                                  Best& best, Counters& ctr) {
+  const uint32_t leaf = e & kLeafIndexMask;
+  const int cnt = (int)((e >> kLeafCountShift) & 15u) + 1;
+  const int gang = sc.gang;
+  const int stride = ((cnt - 1) / gang + 1) * gang;
+  const float* blk = sc.leaves + (size_t)leaf * 9 * sc.leaf_memory;
+  if (COUNT) {
+    ctr.leaf_visits++;
+    ctr.tri_tests += (uint32_t)cnt;
+  }
+  bool any = false;
+  const int ax0 = r.kx, ax1 = r.ky, ax2 = r.code;
+  const int lm = sc.leaf_memory;
+  const float* bnd = sc.leaf_bounds + (size_t)leaf * 6 * lm;
+  for (int g = 0; g < cnt; g += 4) {
+    float lo[4][3], hi[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float4 mn = ldg4(bnd + a * lm + g), mx = ldg4(bnd + (3 + a) * lm + g);
+      const uint64_t o2 = f2splat(r.o[a]), s2 = f2splat(r.inv[a]);
+      const float2 n01 = f2unpack(f2mul(f2sub(f2pack(mn.x, mn.y), o2), s2));
+      const float2 n23 = f2unpack(f2mul(f2sub(f2pack(mn.z, mn.w), o2), s2));
+      const float2 x01 = f2unpack(f2mul(f2sub(f2pack(mx.x, mx.y), o2), s2));
+      const float2 x23 = f2unpack(f2mul(f2sub(f2pack(mx.z, mx.w), o2), s2));
+      lo[0][a] = n01.x; lo[1][a] = n01.y; lo[2][a] = n23.x; lo[3][a] = n23.y;
+      hi[0][a] = x01.x; hi[1][a] = x01.y; hi[2][a] = x23.x; hi[3][a] = x23.y;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = g + k;
+      if (i >= cnt) break;
+      const float tmin = fmaxf(fmaxf(fminf(lo[k][0], hi[k][0]), fminf(lo[k][1], hi[k][1])),
+                               fminf(lo[k][2], hi[k][2]));
+      const float tmx = fminf(fminf(fmaxf(lo[k][0], hi[k][0]), fmaxf(lo[k][1], hi[k][1])),
+                              fmaxf(lo[k][2], hi[k][2]));
+      if (tmx < 0 || tmin > tmx || tmax < tmin) continue;
+      float p[3][3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        p[v][0] = __ldg(blk + (v * 3 + ax0) * stride + i);
+        p[v][1] = __ldg(blk + (v * 3 + ax1) * stride + i);
+        p[v][2] = __ldg(blk + (v * 3 + ax2) * stride + i);
+      }
+      float t, b1, b2;
+      if (!watertight<MM, false>(p, r, tmax, t, b1, b2)) continue;
+      if (COUNT) ctr.tri_hits++;
+      any = true;
+      if (KIND == BVHGPU_ANY) {
+        if (!COUNT) return true;
+        continue;
+      }
+      // Each accepted triangle overwrites the hit (triangle.cpp:243).
+      tmax = t;
+      best.leaf = leaf;
+      best.lane = i;
+      best.u = b1;
+      best.v = b2;
+    }
+  }
+  return any;
+}
+
+template <int PROFILE, int KIND, bool COUNT, bool MM>
+BVHGPU_DEV bool visit_leaf(const SceneDev& sc, uint32_t e, const Ray& r, float& tmax, Best& best,
+                           Counters& ctr) {
+  if constexpr (BVHGPU_LEAF_BOUNDS && PROFILE == BVHGPU_PROFILE_INSTRUMENTED && MM)
+    return visit_leaf_bounds<KIND, COUNT, MM>(sc, e, r, tmax, best, ctr);
+  else
+    return visit_leaf_points<PROFILE, KIND, COUNT, MM>(sc, e, r, tmax, best, ctr);
 }
 
 // Visits with the IEEE min / max forms unless the ray can produce a NaN.
@@ -832,10 +921,13 @@ BVHGPU_DEV bool set_insert(uint32_t* tbl, int size, uint32_t key) {
   return false;
 }
 
-template <int N, int PROFILE, int KIND, bool COUNT>
+// Packets of up to 256 rays, two per SM (at most 128 registers): with the
+// stored-bounds leaf test the compiler otherwise takes 142 registers and
+// one packet per SM (bench frame: 42.5 against 27.1 ms).
 #ifndef BVHGPU_STREAM_MIN_BLOCKS
-#define BVHGPU_STREAM_MIN_BLOCKS 1
+#define BVHGPU_STREAM_MIN_BLOCKS 2
 #endif
+template <int N, int PROFILE, int KIND, bool COUNT>
 __global__ void __launch_bounds__(256, BVHGPU_STREAM_MIN_BLOCKS)
     trace_stream_kernel(SceneDev sc, TraceArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];

@@ -59,3 +59,23 @@ def test_branching_search():
     assert pair in ((4, 4), (8, 8)) and set(results) == {(4, 4), (8, 8)}
     assert total == min(results.values())
     assert bvh.info["branching"] == pair[0]
+
+
+def test_branching_search_keeps_the_preferred_pair_within_the_margin():
+    tris = S.clutter(60, seed=4)
+    rays = S.clutter_camera(60, 64, 48, seed=4)
+    fake = {4: 1.0, 8: 1.04}  # milliseconds by node width: N4 4 % faster
+
+    def batches_fn(scene):
+        return _batches(tris, scene, rays)
+
+    def time_fn(scene, batches):
+        return fake[scene.bvh_info["branching"]]
+
+    kw = dict(pairs=((4, 4), (8, 8)), layouts=(("fp32", 0),), time_fn=time_fn)
+    best, results = autotune.tune_branching(tris, batches_fn, prefer=(8, 8), margin=0.05, **kw)
+    assert best[1] == (8, 8) and results == {(4, 4): 1.0, (8, 8): 1.04}
+    best, _ = autotune.tune_branching(tris, batches_fn, prefer=(8, 8), margin=0.02, **kw)
+    assert best[1] == (4, 4)
+    best, _ = autotune.tune_branching(tris, batches_fn, **kw)
+    assert best[1] == (4, 4)
