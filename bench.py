@@ -800,39 +800,48 @@ def run_batch(a):
     with torch.cuda.graph(g1):
         batched(one_launch=True)
     ms_one = timed(g1.replay, a.steps)
+    ms_graph = timed(g.replay, a.steps)
+    # The headline takes the faster launch form, timed again with the clock
+    # sampler: per-scene N / L choices split the per-kind form into one launch
+    # per ray kind and node width, which the single launch does not need.
+    one_form = ms_one < ms_graph
     with ClockSampler(0) as clk:
-        ms_graph = timed(g.replay, a.steps)
+        ms_head = timed(g1.replay if one_form else g.replay, a.steps)
     clocks = clk.summary()
     ms_batched = timed(batched, a.steps)
+    per_kind_launches = len({(k, s_.bvh_info["branching"]) for s_, _, k, _ in jobs_plain})
+    launches = (1 if one_form else per_kind_launches) + (4 if a.job_reorder else 0)
     ms_seq = timed(sequential, a.steps)
     for s_ in {id(j[0]): j[0] for j in jobs_plain}.values():
         s_.status()
     line = {
-        "metric": METRIC, "value": n_rays / (ms_graph / 1e3) / 1e6, "unit": METRIC, "n_gpus": 1,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_graph, "higher_is_better": True,
+        "metric": METRIC, "value": n_rays / (ms_head / 1e3) / 1e6, "unit": METRIC, "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_head, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded terrain and clutter scenes)",
         "config": {
             "workload": f"{a.scenes} scenes in one persistent launch, triangles log-uniform "
                         f"1k-500k, rays log-uniform 4k-2M (primary:shadow:AO 1:1:4)",
             "triangles_total": n_tris, "rays_per_step": n_rays, "jobs": len(jobs_plain),
-            "method": "bvhgpu_trace_jobs (one persistent launch per ray kind over all scenes; "
-                      "speculative any-hit policy, AO jobs grouped into "
-                      f"6x{a.job_reorder}x{a.job_reorder} direction bins"
-                      + (", child-index push order" if a.job_any_order else "")
-                      + ") in a CUDA graph"
-                      if a.job_reorder else
-                      "bvhgpu_trace_jobs (one persistent launch per ray kind over all scenes; "
-                      "speculative any-hit policy) in a CUDA graph",
+            "method": "bvhgpu_trace_jobs ("
+                      + ("one persistent launch for all jobs, closest-hit rays first"
+                         if one_form else
+                         f"one persistent launch per ray kind and node width ({per_kind_launches})")
+                      + " over all scenes; speculative any-hit policy"
+                      + (f", AO jobs grouped into 6x{a.job_reorder}x{a.job_reorder} direction bins"
+                         + (", child-index push order" if a.job_any_order else "")
+                         if a.job_reorder else "")
+                      + ") in a CUDA graph; the faster of the two launch forms",
+            "launch_form": "one launch" if one_form else "per ray kind",
             "ms_batched_graph": ms_graph, "ms_batched_no_graph": ms_batched,
             "ms_one_launch_graph": ms_one, "one_launch_results_identical": bool(same_one),
             "ms_sequential_plain_launches": ms_seq,
-            "speedup_vs_sequential": ms_seq / ms_graph, "results_identical": bool(same),
+            "speedup_vs_sequential": ms_seq / ms_head, "results_identical": bool(same),
             "autotuned_nl": bool(a.tune_nl), "scenes": scenes, "setup_s": round(setup_s, 1),
         },
-        # per step one batched launch per ray kind (closest-hit jobs, any-hit
-        # jobs), plus the four segmented reorder passes
-        "clocks": clocks, "gpu_launches": a.steps * (6 if a.job_reorder else 2),
+        # per step the batched launch(es) of the chosen form plus the four
+        # segmented reorder passes
+        "clocks": clocks, "gpu_launches": a.steps * launches,
     }
     print(json.dumps(line))
 

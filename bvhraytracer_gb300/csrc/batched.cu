@@ -10,7 +10,10 @@
 #endif
 #undef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS BVHGPU_BATCHED_PAIRED
-// The jobs carry no triangle bounds: the pre-test computes them.
+// The jobs carry neither triangle bounds nor per-child entries: the
+// pre-test computes its bounds and pushes decode the record (carrying both
+// in 112-byte job records measured 6.88 against 6.20 ms on the 64-scene
+// batch).
 #undef BVHGPU_LEAF_BOUNDS
 #define BVHGPU_LEAF_BOUNDS 0
 
