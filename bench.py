@@ -41,10 +41,11 @@ METRIC = "Mrays/s"
 # persistent kernel, refill 24, 6 x 10 x 10 direction bins, child-index
 # order), from one ncu capture of `bench.py --workload aolaunch --steps 1
 # --warmup 1` (2,000,000 AO rays, an evenly strided sample of the frame's):
-# the trace kernel 91,570,688 B, the four reorder passes 70,398,208 B. The
+# the trace kernel 101,412,096 B, the four reorder passes 70,406,912 B. The
 # traffic is the ray stream plus the BVH lines that miss L2, so it is scaled
 # to a launch by its ray count.
-NCU_DRAM_BYTES_PER_AO_RAY = {"trace": 91570688 / 2e6, "with_reorder": (91570688 + 70398208) / 2e6}
+NCU_DRAM_BYTES_PER_AO_RAY = {"trace": 101412096 / 2e6,
+                             "with_reorder": (101412096 + 70406912) / 2e6}
 
 
 def parse():
@@ -989,10 +990,10 @@ def run_adjoint(a):
 # the four reorder passes; policy 2, refill 24, 6 x 10 x 10 bins,
 # child-index order), from one ncu capture each of `bench.py --workload
 # aolaunch --objects 32000 --leaf 4 --ao 16 --steps 1 --warmup 1 [--nodes
-# q8]` (2,000,000 strided AO rays): FP32 165,708,544 + 70,393,600 B, Q8
-# 147,883,264 + 70,468,864 B.
-SCALE8M_DRAM_BYTES_PER_AO_RAY = {"fp32": (165708544 + 70393600) / 2e6,
-                                 "q8": (147883264 + 70468864) / 2e6}
+# q8]` (2,000,000 strided AO rays): FP32 209,611,008 + 70,400,256 B, Q8
+# 190,471,680 + 70,404,864 B.
+SCALE8M_DRAM_BYTES_PER_AO_RAY = {"fp32": (209611008 + 70400256) / 2e6,
+                                 "q8": (190471680 + 70404864) / 2e6}
 
 
 def run_scale(a):
