@@ -23,6 +23,14 @@
 #include "batched.cuh"
 #include "adjoint.cuh"
 
+// Streams (and staging regions) of the host-buffer pipeline: a chunk's copy
+// in waits until the chunk this many places earlier has been traced and
+// copied out. 1M-triangle frame, median step: 2 streams 8.63 ms, 3 streams
+// 8.38 ms, 4 streams 8.39 ms.
+#ifndef BVHGPU_HOST_STREAMS
+#define BVHGPU_HOST_STREAMS 3
+#endif
+
 namespace bvhgpu {
 
 static thread_local std::string g_last_error;
@@ -70,12 +78,12 @@ struct bvhgpu_scene {
   int sm_count = 0;
   // Staging for bvhgpu_trace_host (grown on demand): one region per
   // pipeline stream, and the streams / events that order them.
-  static constexpr int kHostStreams = 2;
+  static constexpr int kHostStreams = BVHGPU_HOST_STREAMS;
   std::mutex staging_mu;
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
-  cudaStream_t host_stream[kHostStreams] = {nullptr, nullptr};
-  cudaEvent_t host_event[kHostStreams + 1] = {nullptr, nullptr, nullptr};
+  cudaStream_t host_stream[kHostStreams] = {};
+  cudaEvent_t host_event[kHostStreams + 1] = {};
 
   dev::SceneDev dev_view() const {
     dev::SceneDev s;
