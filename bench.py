@@ -616,7 +616,12 @@ def run_ours(a):
                 "oracle_equal": parity,
                 "l2": "inputs larger than L2 (rays ~%d MB per step); BVH stays L2-resident"
                       % (n_rays * 32 // 2**20),
-                "bvh_bytes": {"nodes_fp32": plain.node_bytes, "leaves": plain.leaf_bytes},
+                # beside the records: one 4-byte stack entry per child slot and
+                # 6 of the leaf block's 9 floats per triangle slot (bounds)
+                "bvh_bytes": {"nodes_fp32": plain.node_bytes, "leaves": plain.leaf_bytes,
+                              "child_entries": plain.node_bytes // plain.node_record_bytes
+                              * (-(-a.branching // 4) * 4) * 4,
+                              "triangle_bounds": plain.leaf_bytes * 6 // 9},
                 "per_kernel_ms": dict(zip(names, per_kernel_ms)),
                 "ms_per_frame_by_method": compare,
                 "setup_s": round(setup_s, 2),
