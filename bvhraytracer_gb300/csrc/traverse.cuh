@@ -49,8 +49,9 @@ struct SceneDev {
 #ifndef BVHGPU_NEARFAR
 #define BVHGPU_NEARFAR 1
 #endif
-// 1: the near / far slab test computes two children's plane distances per
-// packed f32x2 subtract and multiply; 0: one child per instruction.
+// 1: the slab tests of NaN-free rays (near / far and min / max forms)
+// compute two children's plane distances per packed f32x2 subtract and
+// multiply; 0: one child per instruction.
 #ifndef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS 1
 #endif
