@@ -712,10 +712,11 @@ struct HostBatch {
 }  // namespace
 
 // Pipeline of host-buffer traces: the rays of every batch go in chunks over
-// two internal streams, so the copy of one chunk in, the trace of another and
-// the copy of a third out run at the same time, across batch boundaries too.
-// Both streams wait for `st` first; `st` waits for both at the end, and the
-// call returns with the results on the host.
+// BVHGPU_HOST_STREAMS internal streams (chunk k on stream k mod that number),
+// so the copy of one chunk in, the trace of another and the copy of a third
+// out run at the same time, across batch boundaries too. The streams wait
+// for `st` first; `st` waits for all of them at the end, and the call
+// returns with the results on the host.
 static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cudaStream_t st) {
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
