@@ -687,17 +687,33 @@ int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 #ifndef BVHGPU_HOST_CHUNK_MAX
 #define BVHGPU_HOST_CHUNK_MAX 4
 #endif
-// 1: chunks that double from 256 Ki rays up to BVHGPU_HOST_GROW_MAX Mi over
+// 1: chunks that grow from BVHGPU_HOST_GROW_FIRST Ki rays by
+// BVHGPU_HOST_GROW_PCT percent per chunk, up to BVHGPU_HOST_GROW_MAX Mi, over
 // the whole call (across batch boundaries), instead of quarters of each
-// batch. Same frame, with the reorder scratch held per stream: median step
-// 8.74-8.75 ms growing to 8 Mi, 8.84-9.15 ms in quarters. (With the scratch
-// allocated per launch from the pool, growing chunks alternated between
-// 8.75 and 10.25 ms per step from run to run.)
+// batch. Same frame, with the reorder scratch held per stream, two streams:
+// median step 8.74-8.75 ms doubling up to 8 Mi, 8.84-9.15 ms in quarters.
+// (With the scratch allocated per launch from the pool, growing chunks
+// alternated between 8.75 and 10.25 ms per step from run to run.)
+// Three streams, median step by growth / cap (three runs on three GPUs):
+// 200 % / 8 Mi 8.33-8.39 ms, 200 % / 4 Mi 8.36, 175 % / 3 Mi 8.30,
+// 150 % / 8, 6, 4, 3, 2 Mi 8.25, 8.27, 8.03, 8.27, 7.95-8.27,
+// 135 % / 4 Mi 8.06, 125 % / 6, 4, 3, 2 Mi 9.05, 7.88 (twice), 7.91, 7.93,
+// 115 % / 4 Mi 8.05, 110 % / 8 Mi 8.07; first chunk 128 / 256 / 512 Ki at
+// 125 % / 4 Mi: 7.98 / 7.88 / 7.87. A chunk's copy in waits for the copy out
+// of the chunk three before it (same stream, same staging region), so
+// chunks that grow slowly keep the copies ahead of the traces without
+// leaving one large chunk to trace after the last copy.
 #ifndef BVHGPU_HOST_GROW
 #define BVHGPU_HOST_GROW 1
 #endif
 #ifndef BVHGPU_HOST_GROW_MAX
-#define BVHGPU_HOST_GROW_MAX 8
+#define BVHGPU_HOST_GROW_MAX 4
+#endif
+#ifndef BVHGPU_HOST_GROW_PCT
+#define BVHGPU_HOST_GROW_PCT 125
+#endif
+#ifndef BVHGPU_HOST_GROW_FIRST
+#define BVHGPU_HOST_GROW_FIRST 256
 #endif
 
 namespace {
@@ -735,9 +751,9 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
     }
   }
   // The chunks (batch, first ray, rays). Growing: the first chunk is small,
-  // so the copy in that no trace overlaps is short, and each next one twice
-  // as large (copies run faster than traces, so a chunk's copy ends while
-  // the previous chunk traces), up to a cap; a batch's remainder below half
+  // so the copy in that no trace overlaps is short, and each next one a
+  // quarter larger (copies run faster than traces, so a chunk's copy ends
+  // while the previous chunk traces), up to a cap; a batch's remainder below half
   // the current size joins its last chunk. Otherwise: a quarter of each
   // batch, between 256 Ki and 4 Mi rays.
   struct Chunk {
@@ -747,7 +763,7 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
   std::vector<Chunk> chunks;
   uint64_t max_chunk = 0;
   if (BVHGPU_HOST_GROW) {
-    uint64_t size = 256ull << 10;
+    uint64_t size = (uint64_t)BVHGPU_HOST_GROW_FIRST << 10;
     const uint64_t cap = (uint64_t)BVHGPU_HOST_GROW_MAX << 20;
     for (int k = 0; k < nb; ++k) {
       for (uint64_t first = 0; first < b[k].n;) {
@@ -756,7 +772,7 @@ static int trace_host_pipeline(bvhgpu_scene_t s, const HostBatch* b, int nb, cud
         chunks.push_back({k, first, m});
         max_chunk = std::max(max_chunk, m);
         first += m;
-        size = std::min<uint64_t>(size * 2, cap);
+        size = std::min<uint64_t>(size * BVHGPU_HOST_GROW_PCT / 100, cap);
       }
     }
   } else {
