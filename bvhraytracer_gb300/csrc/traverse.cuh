@@ -61,6 +61,11 @@ struct SceneDev {
 #ifndef BVHGPU_LEAF_BOUNDS
 #define BVHGPU_LEAF_BOUNDS 1
 #endif
+// Any-hit leaf visits with stored bounds: all pre-tests first, then the full
+// tests of the passing triangles only.
+#ifndef BVHGPU_LEAF_COMPACT
+#define BVHGPU_LEAF_COMPACT 1
+#endif
 // 1: pushes of hit children in child-index order read their stack entries
 // from SceneDev::child_entry; 0: computed from the record.
 #ifndef BVHGPU_ENTRY_PUSH
@@ -621,6 +626,54 @@ BVHGPU_DEV bool visit_leaf_bounds(const SceneDev& sc, uint32_t e, const Ray& r, 
   const int ax0 = r.kx, ax1 = r.ky, ax2 = r.code;
   const int lm = sc.leaf_memory;
   const float* bnd = sc.leaf_bounds + (size_t)leaf * 6 * lm;
+  if (BVHGPU_LEAF_COMPACT && KIND == BVHGPU_ANY) {
+    // Any-hit rays keep tMax, so every pre-test of the leaf can run first:
+    // a mask of the triangles that pass, then the full tests of those only,
+    // in ascending order as below. The warp then runs as many full tests as
+    // its lanes have passing triangles at most (about one in six passes),
+    // not one per triangle slot in which any lane passes.
+    uint32_t pass = 0;
+    for (int g = 0; g < cnt; g += 4) {
+      float lo[4][3], hi[4][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float4 mn = ldg4(bnd + a * lm + g), mx = ldg4(bnd + (3 + a) * lm + g);
+        const uint64_t o2 = f2splat(r.o[a]), s2 = f2splat(r.inv[a]);
+        const float2 n01 = f2unpack(f2mul(f2sub(f2pack(mn.x, mn.y), o2), s2));
+        const float2 n23 = f2unpack(f2mul(f2sub(f2pack(mn.z, mn.w), o2), s2));
+        const float2 x01 = f2unpack(f2mul(f2sub(f2pack(mx.x, mx.y), o2), s2));
+        const float2 x23 = f2unpack(f2mul(f2sub(f2pack(mx.z, mx.w), o2), s2));
+        lo[0][a] = n01.x; lo[1][a] = n01.y; lo[2][a] = n23.x; lo[3][a] = n23.y;
+        hi[0][a] = x01.x; hi[1][a] = x01.y; hi[2][a] = x23.x; hi[3][a] = x23.y;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float tmin = fmaxf(fmaxf(fminf(lo[k][0], hi[k][0]), fminf(lo[k][1], hi[k][1])),
+                                 fminf(lo[k][2], hi[k][2]));
+        const float tmx = fminf(fminf(fmaxf(lo[k][0], hi[k][0]), fmaxf(lo[k][1], hi[k][1])),
+                                fmaxf(lo[k][2], hi[k][2]));
+        if (!(tmx < 0 || tmin > tmx || tmax < tmin)) pass |= 1u << (g + k);
+      }
+    }
+    pass &= (1u << cnt) - 1u;  // slots past the leaf's count hold padding
+    while (pass) {
+      const int i = __ffs(pass) - 1;
+      pass &= pass - 1u;
+      float p[3][3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        p[v][0] = __ldg(blk + (v * 3 + ax0) * stride + i);
+        p[v][1] = __ldg(blk + (v * 3 + ax1) * stride + i);
+        p[v][2] = __ldg(blk + (v * 3 + ax2) * stride + i);
+      }
+      float t, b1, b2;
+      if (!watertight<MM, false>(p, r, tmax, t, b1, b2)) continue;
+      if (COUNT) ctr.tri_hits++;
+      any = true;
+      if (!COUNT) return true;
+    }
+    return any;
+  }
   for (int g = 0; g < cnt; g += 4) {
     float lo[4][3], hi[4][3];
 #pragma unroll
