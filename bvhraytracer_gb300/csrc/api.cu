@@ -1027,6 +1027,7 @@ int bvhgpu_trace_jobs(const bvhgpu_job_t* jobs, int32_t n_jobs, const bvhgpu_tra
     d.any_index_order = j.any_order ? 1 : 0;
     d.perm = nullptr;
     d.q8_perm = j.scene->d_q8_perm;
+    d.leaf_bounds = j.scene->d_leaf_bounds;
     if (j.reorder && j.n > 1) {
       seg_k = j.reorder;
       seg_off.push_back(seg_bytes);

@@ -10,12 +10,19 @@
 #endif
 #undef BVHGPU_PAIRED_SLABS
 #define BVHGPU_PAIRED_SLABS BVHGPU_BATCHED_PAIRED
-// The jobs carry neither triangle bounds nor per-child entries: the
-// pre-test computes its bounds and pushes decode the record (carrying both
-// in 112-byte job records measured 6.88 against 6.20 ms on the 64-scene
-// batch).
+// The jobs carry no per-child entries: pushes decode the record (entries
+// and triangle bounds both in 112-byte job records measured 6.88 against
+// 6.20 ms on the 64-scene batch). BVHGPU_BATCHED_BOUNDS 1: the leaf pre-test
+// reads the job scene's stored triangle bounds, and any-hit rays run all of
+// a leaf's pre-tests before the full tests of the passing triangles; 0: the
+// pre-test computes the bounds from the vertices. 64-scene batch, one launch
+// per ray kind: 5.77 ms against 6.19 ms (one launch for all jobs: 5.96
+// against 6.23 ms).
+#ifndef BVHGPU_BATCHED_BOUNDS
+#define BVHGPU_BATCHED_BOUNDS 1
+#endif
 #undef BVHGPU_LEAF_BOUNDS
-#define BVHGPU_LEAF_BOUNDS 0
+#define BVHGPU_LEAF_BOUNDS BVHGPU_BATCHED_BOUNDS
 
 #include "batched.cuh"
 

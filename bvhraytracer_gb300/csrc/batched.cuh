@@ -10,7 +10,7 @@
 namespace bvhgpu {
 namespace dev {
 
-constexpr int kMaxJobs = 192;  // 192 jobs x 96 bytes in the parameter block
+constexpr int kMaxJobs = 192;  // 192 jobs x 104 bytes in the parameter block
 
 struct JobDev {
   const uint8_t* nodes;
@@ -34,8 +34,9 @@ struct JobDev {
   // result goes to slot perm[i] (null: i).
   const uint32_t* perm;
   const uint8_t* q8_perm;  // SceneDev::q8_perm of the job's scene
+  const float* leaf_bounds;  // SceneDev::leaf_bounds of the job's scene
 };
-static_assert(sizeof(JobDev) == 96, "job record size");
+static_assert(sizeof(JobDev) == 104, "job record size");
 
 struct JobTable {
   JobDev jobs[kMaxJobs];
@@ -148,6 +149,7 @@ __device__ __forceinline__ void batched_loop(const JobTable& t) {
           sc.boxes_ordered = J.boxes_ordered;
           sc.any_index_order = J.any_index_order;
           sc.q8_perm = J.q8_perm;
+          sc.leaf_bounds = J.leaf_bounds;
           nm = J.nm;
           fmt = J.fmt;
           if (KMODE == 0) kind = J.kind;
