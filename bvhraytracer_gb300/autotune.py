@@ -68,10 +68,32 @@ def _time(scene, rays, kind, opts, profile, reps):
     return e0.elapsed_time(e1) / reps
 
 
+def one_layout(table: dict, n_batches: int, mixed_ms: float, margin: float = 0.03):
+    """The layout to trace every batch of a plan with, or None to keep the
+    per-batch layouts. ``table`` maps (batch, layout, options) to ms. Batches
+    in different layouts go through different scenes, so the host-buffer
+    entry points run one pipeline (and one synchronisation) per scene; one
+    layout for all batches is kept unless the mixed plan is faster by more
+    than ``margin`` of its time."""
+    per_layout = {}
+    for (bi, lay, _), ms in table.items():
+        best = per_layout.setdefault(lay, [None] * n_batches)
+        if best[bi] is None or ms < best[bi]:
+            best[bi] = ms
+    totals = {lay: sum(b) for lay, b in per_layout.items() if all(x is not None for x in b)}
+    if not totals:
+        return None
+    lay = min(totals, key=totals.get)
+    return lay if totals[lay] <= mixed_ms * (1.0 + margin) else None
+
+
 def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFAULT_LAYOUTS,
-               options=DEFAULT_OPTIONS, reps: int = 3, device: int = 0, scenes=None):
+               options=DEFAULT_OPTIONS, reps: int = 3, device: int = 0, scenes=None,
+               layout_margin: float = 0.03):
     """Times every (layout, options) candidate on each ``(rays, kind)`` batch
-    (device tensors) and returns (plan, scenes by layout)."""
+    (device tensors) and returns (plan, scenes by layout). All batches share
+    one layout unless mixing layouts saves more than ``layout_margin`` of the
+    time (see one_layout)."""
     scenes = dict(scenes or {})
     plan = Plan()
     for fmt, top in layouts:
@@ -89,6 +111,13 @@ def tune_scene(bvh: Bvh, batches, *, profile: str = "instrumented", layouts=DEFA
             if best is None or ms < best[2]:
                 best = (lay, opts, ms)
         plan.choices.append(best)
+    lay = one_layout(plan.table, len(batches), sum(c[2] for c in plan.choices), layout_margin)
+    if lay is not None:
+        for bi, c in enumerate(plan.choices):
+            if c[0] == lay:
+                continue
+            key = min((k for k in plan.table if k[0] == bi and k[1] == lay), key=plan.table.get)
+            plan.choices[bi] = (lay, dict(key[2]), plan.table[key])
     return plan, scenes
 
 
