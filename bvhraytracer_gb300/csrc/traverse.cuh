@@ -61,10 +61,11 @@ struct SceneDev {
 #ifndef BVHGPU_LEAF_BOUNDS
 #define BVHGPU_LEAF_BOUNDS 1
 #endif
-// Any-hit leaf visits with stored bounds: all pre-tests first, then the full
-// tests of the passing triangles only.
+// Leaf visits with stored bounds: all pre-tests first, then the full tests of
+// the passing triangles only; 1: any-hit rays, 2: any-hit and closest-hit
+// rays, 0: neither.
 #ifndef BVHGPU_LEAF_COMPACT
-#define BVHGPU_LEAF_COMPACT 1
+#define BVHGPU_LEAF_COMPACT 2
 #endif
 // 1: pushes of hit children in child-index order read their stack entries
 // from SceneDev::child_entry; 0: computed from the record.
@@ -626,12 +627,15 @@ BVHGPU_DEV bool visit_leaf_bounds(const SceneDev& sc, uint32_t e, const Ray& r, 
   const int ax0 = r.kx, ax1 = r.ky, ax2 = r.code;
   const int lm = sc.leaf_memory;
   const float* bnd = sc.leaf_bounds + (size_t)leaf * 6 * lm;
-  if (BVHGPU_LEAF_COMPACT && KIND == BVHGPU_ANY) {
-    // Any-hit rays keep tMax, so every pre-test of the leaf can run first:
-    // a mask of the triangles that pass, then the full tests of those only,
-    // in ascending order as below. The warp then runs as many full tests as
-    // its lanes have passing triangles at most (about one in six passes),
-    // not one per triangle slot in which any lane passes.
+  if ((BVHGPU_LEAF_COMPACT >= 1 && KIND == BVHGPU_ANY) || BVHGPU_LEAF_COMPACT >= 2) {
+    // Every pre-test of the leaf first, with the tMax the ray enters the
+    // leaf with: a mask of the triangles that pass, then the full tests of
+    // those only, in ascending order as below. The warp then runs as many
+    // full tests as its lanes have passing triangles at most (about one in
+    // six passes for ambient-occlusion rays), not one per triangle slot in
+    // which any lane passes. Any-hit rays keep tMax; a closest-hit ray whose
+    // tMax fell at an earlier hit in this leaf repeats the pre-test's tMax
+    // condition (the only one that depends on tMax) before a full test.
     uint32_t pass = 0;
     for (int g = 0; g < cnt; g += 4) {
       float lo[4][3], hi[4][3];
@@ -656,9 +660,20 @@ BVHGPU_DEV bool visit_leaf_bounds(const SceneDev& sc, uint32_t e, const Ray& r, 
       }
     }
     pass &= (1u << cnt) - 1u;  // slots past the leaf's count hold padding
+    const float tmax_in = tmax;
     while (pass) {
       const int i = __ffs(pass) - 1;
       pass &= pass - 1u;
+      if (KIND == BVHGPU_CLOSEST && tmax != tmax_in) {
+        float m[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float lo = (__ldg(bnd + a * lm + i) - r.o[a]) * r.inv[a];
+          const float hi = (__ldg(bnd + (3 + a) * lm + i) - r.o[a]) * r.inv[a];
+          m[a] = fminf(lo, hi);
+        }
+        if (tmax < fmaxf(fmaxf(m[0], m[1]), m[2])) continue;
+      }
       float p[3][3];
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
@@ -670,7 +685,16 @@ BVHGPU_DEV bool visit_leaf_bounds(const SceneDev& sc, uint32_t e, const Ray& r, 
       if (!watertight<MM, false>(p, r, tmax, t, b1, b2)) continue;
       if (COUNT) ctr.tri_hits++;
       any = true;
-      if (!COUNT) return true;
+      if (KIND == BVHGPU_ANY) {
+        if (!COUNT) return true;
+        continue;
+      }
+      // Each accepted triangle overwrites the hit (triangle.cpp:243).
+      tmax = t;
+      best.leaf = leaf;
+      best.lane = i;
+      best.u = b1;
+      best.v = b2;
     }
     return any;
   }
