@@ -251,7 +251,7 @@ def cpu_baseline(a, tris, bvh, primary, shadow, ao, frac, repeats=5):
 
 
 def oracle_check(a, bvh, batches, device_outs, host_outs, rays_per_batch=24_000):
-    """CPU-baseline leg, as the checker: an evenly strided sample of each
+    """CPU-baseline leg, checking results: an evenly strided sample of each
     timed batch (primary hits, shadow and AO occlusion, as the timed device
     launches and the host entry point left them) against the oracle's
     restatement of the reference on the same rays (instrumented profile:

@@ -1,7 +1,7 @@
 """Builds the CPU oracle (test infrastructure) from oracle/bvh_oracle.c and
 oracle/sah_builder.c:
 
-* oracle/_build/liboracle.so — the scalar restatement (the checker): gcc -O2
+* oracle/_build/liboracle.so — the scalar restatement (the oracle proper): gcc -O2
   with -ffp-contract=off (no FMA contraction, so float results match the
   reference's scalar code on x86-64 and aarch64 alike) and OpenMP;
 * oracle/_build/libcpubaseline.so — the timed CPU baseline: the same source

@@ -36,7 +36,7 @@ _lock = threading.Lock()
 
 
 def lib() -> C.CDLL:
-    """The scalar oracle (the checker)."""
+    """The scalar oracle library."""
     global _lib
     with _lock:
         if _lib is None:
