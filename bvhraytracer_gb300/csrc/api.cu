@@ -699,7 +699,9 @@ int bvhgpu_trace_steps(bvhgpu_scene_t s, const bvhgpu_ray_t* rays, uint64_t n,
 // 150 % / 8, 6, 4, 3, 2 Mi 8.25, 8.27, 8.03, 8.27, 7.95-8.27,
 // 135 % / 4 Mi 8.06, 125 % / 6, 4, 3, 2 Mi 9.05, 7.88 (twice), 7.91, 7.93,
 // 115 % / 4 Mi 8.05, 110 % / 8 Mi 8.07; first chunk 128 / 256 / 512 Ki at
-// 125 % / 4 Mi: 7.98 / 7.88 / 7.87. A chunk's copy in waits for the copy out
+// 125 % / 4 Mi: 7.98 / 7.88 / 7.87. With the kernels of a 6.99 ms frame:
+// 125 % / 4 Mi 7.21 ms, 125 % / 2 Mi 7.24, 110 % / 4 Mi 7.39, 150 % / 4 Mi
+// 7.38. A chunk's copy in waits for the copy out
 // of the chunk three before it (same stream, same staging region), so
 // chunks that grow slowly keep the copies ahead of the traces without
 // leaving one large chunk to trace after the last copy.
